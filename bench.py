@@ -1,0 +1,379 @@
+#!/usr/bin/env python
+"""Benchmark of the rule-based blocking hot path: pair-comparisons/s.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
+
+Workload (default): the C2 configuration -- 2,600 x 64,263 seeded synthetic
+bibliographic rows (header line included as data, as the reference reads it),
+5k perturbed true pairs, two rules ((year eq, JW(title) >= 0.89,
+JW(authors) >= 0.85) or (venue eq, JW(title) >= 0.95)), 8 hash partitions.
+A step is one pass of the hot path over the whole workload: equality join,
+Jaro-Winkler pair evaluation and compaction of the matching pairs.
+
+* ``value``: pair-comparisons/s of the engine's default (batched: one
+  persistent work-stealing launch replayed from a CUDA graph) with the inputs
+  resident in HBM; L2 is flushed (256 MiB write) before every timed step and
+  every step is timed with CUDA events on the launching stream.
+* ``plain``: the same with one launch per (partition, rule), like the
+  reference's per-partition submission.
+* ``e2e``: the same metric through the one-shot C-ABI call ``hbx_block`` from
+  host tables to host pair buffers (encode + H2D + run + D2H inside the timed
+  region).
+* ``roofline``: the pair-evaluation kernel against the INT32 issue peak (see
+  the ``roofline`` block for the conventions), ``cpu_baseline``: the oracle
+  (the reference's brute-force algorithm restated in C++) on all host cores.
+
+``--impl reference`` times that CPU implementation alone and prints the same
+line with ``"impl": "reference"``.  With N > 1 GPUs (torchrun) every rank runs
+an independent replica (weak scaling); the path needs no collective.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "pair-comparisons/s, batched vs plain, same GPU, exact set; serving p50/p99 ms"
+UNIT = "pair-comparisons/s"
+WORKLOAD_DESC = ("c2: 2,600 x 64,263 synthetic bibliographic rows (+1 header row each), 5k true "
+                 "pairs, rules (year eq, JW(title)>=0.89, JW(authors)>=0.85) | (venue eq, "
+                 "JW(title)>=0.95), 8 partitions")
+
+
+def _env_int(k, d):
+    try:
+        return int(os.environ.get(k, d))
+    except ValueError:
+        return d
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.device)], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if not self.proc:
+            return out
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        if sm:
+            out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                   "samples": len(sm)}
+        return out
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def _traffic_per_launch():
+    """dram bytes of one k_eval launch on this workload from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "k_eval_c2_traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f).get("dram_bytes_per_launch")
+    except Exception:
+        return None
+
+
+def load_workload(tmpdir: str):
+    import hyperblocker_gb300 as hb
+    from hyperblocker_gb300 import synth
+
+    w = synth.c2()
+    paths = synth.materialize(w, tmpdir)
+    return w, paths
+
+
+def cpu_baseline(paths, n_partitions, target_s=15.0, steps=1, warmup=0, step_fraction=None):
+    """The oracle on all host cores over a bounded sample of left rows.
+
+    Returns dict(value, cores, sample, seconds)."""
+    import numpy as np
+
+    from oracle import api, csvref, rules
+
+    api.build()
+    cl = csvref.read_columns(paths["left"])
+    cr = csvref.read_columns(paths["right"])
+    plan = rules.plan_from_dir(paths["rules"])
+    L, R = api.CTable(cl), api.CTable(cr)
+    n_l = len(cl[0])
+    cores = os.cpu_count() or 1
+    # size the sample: time a small probe, then scale to ~target_s of CPU work
+    if step_fraction is None:
+        probe = np.zeros(n_l, dtype=np.uint8)
+        probe[::64] = 1
+        t = time.perf_counter()
+        api.run_block(L, R, plan, n_partitions, n_threads=cores, left_row_filter=probe)
+        dt = max(time.perf_counter() - t, 1e-3)
+        frac = min(1.0, (target_s / dt) / 64.0)
+    else:
+        frac = step_fraction
+    stride = max(1, int(round(1.0 / frac)))
+    vals, secs, cmps = [], [], []
+    for k in range(warmup + steps):
+        filt = np.zeros(n_l, dtype=np.uint8)
+        filt[(k % stride)::stride] = 1
+        t = time.perf_counter()
+        res = api.run_block(L, R, plan, n_partitions, n_threads=cores, left_row_filter=filt)
+        dt = time.perf_counter() - t
+        if k >= warmup:
+            vals.append(res.pair_comparisons / dt)
+            secs.append(dt)
+            cmps.append(res.pair_comparisons)
+    return {"value": sum(cmps) / sum(secs), "cores": cores, "seconds": sum(secs),
+            "sample": f"every {stride}th left row of the workload per step ({steps} step(s), "
+                      f"{sum(cmps)} pair-comparisons in {sum(secs):.2f} s)"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    with tempfile.TemporaryDirectory() as d:
+        w, paths = load_workload(d)
+        # each step: 1/8 of the left rows, brute force over their partitions
+        cb = cpu_baseline(paths, w.n_partitions, steps=args.steps, warmup=args.warmup,
+                          step_fraction=1.0 / 8.0)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * cb["seconds"] / max(args.steps, 1), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+        "data": "synthetic (seeded, C2 shape)",
+        "config": {"workload": WORKLOAD_DESC, "n_partitions": w.n_partitions, "rules": 2},
+        "cpu_baseline": {"value": cb["value"], "unit": UNIT, "cores": cb["cores"], "kind": "port",
+                         "sample": cb["sample"]},
+        "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_engine(args, rank, world, local_rank):
+    import numpy as np
+    import torch
+
+    import hyperblocker_gb300 as hb
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local_rank)
+    tmp = tempfile.TemporaryDirectory()
+    w, paths = load_workload(tmp.name)
+    ctx = hb.Context(local_rank)
+    plan = hb.Plan.from_rule_dir(paths["rules"], ctx)
+    L = hb.Table.from_csv(paths["left"], ",", ctx)
+    R = hb.Table.from_csv(paths["right"], ",", ctx)
+    sess = hb.Session(ctx, plan, L, R, w.n_partitions)
+    stream = torch.cuda.Stream(device=dev)
+    cap = 1 << 20
+    out_l = torch.empty(cap, dtype=torch.int32, device=dev)
+    out_r = torch.empty(cap, dtype=torch.int32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def step(mode):
+        return sess.run_device(mode, out_l.data_ptr(), out_r.data_ptr(), cap, stream.cuda_stream)
+
+    def timed(mode, k, w_):
+        for _ in range(w_):
+            step(mode)
+        ms, ms_eval, ops, cmp, launches = [], [], [], [], 0
+        with torch.cuda.stream(stream):
+            for _ in range(k):
+                flush.zero_()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                n = step(mode)
+                e1.record(stream)
+                e1.synchronize()
+                ms.append(e0.elapsed_time(e1))
+                st = sess.stats()
+                ms_eval.append(st.ms_eval)
+                ops.append(st.jw_word_ops)
+                cmp.append(st.pair_comparisons)
+                launches += st.n_launches
+        return {"ms": ms, "ms_eval": ms_eval, "ops": ops, "cmp": cmp, "launches": launches,
+                "matches": n}
+
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    t_wall = time.perf_counter()
+    bat = timed("batched", args.steps, args.warmup)
+    torch.cuda.synchronize()
+    wall_batched = time.perf_counter() - t_wall
+    clocks = sampler.stop()
+    pla = timed("plain", args.steps, args.warmup)
+    total_ms = sum(bat["ms"])
+    if dist:
+        t = torch.tensor([total_ms, sum(pla["ms"])], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms, plain_ms = float(t[0]), float(t[1])
+    else:
+        plain_ms = sum(pla["ms"])
+    cmp_step = bat["cmp"][0]
+    value = world * cmp_step * args.steps / (total_ms / 1000.0)
+    plain_value = world * cmp_step * args.steps / (plain_ms / 1000.0)
+
+    # end to end through the one-shot C-ABI call (host tables -> host pairs)
+    e2e_steps = max(1, min(args.steps, 5))
+    hb.block(ctx, plan, L, R, w.n_partitions, hb.INT_MAX, "batched")  # warm
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        pairs, st_e2e = hb.block(ctx, plan, L, R, w.n_partitions, hb.INT_MAX, "batched")
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e = {"value": world * st_e2e.pair_comparisons / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": int(st_e2e.h2d_bytes),
+           "d2h_bytes_per_step": int(8 * st_e2e.n_matches + 64),
+           "ms_per_step": 1000.0 * e2e_s,
+           "includes": "encode (host dictionaries, std::hash partitions, arenas) + H2D + "
+                       "join + evaluation + D2H of the pairs"}
+
+    line = None
+    if rank == 0:
+        peaks = _peaks()
+        props = torch.cuda.get_device_properties(dev)
+        n_sm = props.multi_processor_count
+        sm_max = float(peaks.get("sm_max_mhz") or clocks.get("sm_max_mhz") or 2070.0)
+        # 1 algorithmic op = one 64-bit word operation = 2 INT32 issue slots;
+        # an SM issues 128 INT32 lane-ops per cycle.
+        peak_tops = n_sm * 64 * sm_max * 1e6 / 1e12
+        ms_eval = statistics.mean(bat["ms_eval"])
+        ops = statistics.mean(bat["ops"])
+        achieved = ops / (ms_eval / 1000.0) / 1e12
+        roofline = {
+            "bound": "alu", "kernel": "k_eval (Jaro-Winkler pair evaluation)",
+            "achieved": achieved, "peak": peak_tops, "unit": "Tops/s (64-bit word ops)",
+            "frac": achieved / peak_tops,
+            "traffic": _traffic_per_launch(),
+            "ops_per_launch": ops, "ms_per_launch": ms_eval,
+            "peak_source": f"nominal: {n_sm} SMs x 128 INT32 lanes / 2 per 64-bit op x "
+                           f"{sm_max:.0f} MHz (sm_max_mhz of MEASURED_PEAKS.json); "
+                           "MEASURED_PEAKS.json has no integer-pipe figure",
+            "join_ms_per_step": statistics.mean([m - e for m, e in zip(bat["ms"], bat["ms_eval"])]),
+        }
+        cb = None
+        if world == 1 and not args.no_cpu_baseline:
+            cb = cpu_baseline(paths, w.n_partitions)
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic (seeded PCG64, C2 shape; no dataset download)",
+            "config": {"workload": WORKLOAD_DESC, "n_left_rows": L.n_rows, "n_right_rows": R.n_rows,
+                       "rules": 2, "n_partitions": w.n_partitions, "mode": "batched",
+                       "pair_comparisons_per_step": cmp_step,
+                       "pairs_covered_per_step": int(sess.stats().pairs_covered),
+                       "matches_per_step": int(bat["matches"]),
+                       "l2": "flushed before every timed step (256 MiB write, outside the events)",
+                       "parallelism": f"replicas x{world}"},
+            "plain": {"value": plain_value, "ms_per_step": plain_ms / args.steps,
+                      "launches_per_step": pla["launches"] // max(args.steps, 1)},
+            "batched_vs_plain": value / plain_value,
+            "gpu_launches": bat["launches"],
+            "clocks": {k: clocks[k] for k in ("sm_mhz", "sm_max_mhz", "reasons")},
+            "wall_s_batched": wall_batched,
+            "e2e": e2e,
+            "roofline": roofline,
+        }
+        if cb:
+            line["cpu_baseline"] = {"value": cb["value"], "unit": UNIT, "cores": cb["cores"],
+                                    "kind": "port", "sample": cb["sample"]}
+        print(json.dumps(line), flush=True)
+    sess.close()
+    ctx.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank = _env_int("RANK", 0)
+    world = _env_int("WORLD_SIZE", args.gpus)
+    local_rank = _env_int("LOCAL_RANK", 0)
+    if "WORLD_SIZE" not in os.environ:
+        world = 1 if args.gpus <= 1 else args.gpus
+        if world > 1:
+            print("bench.py: launch N>1 with torch.distributed.run", file=sys.stderr)
+            return 2
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    import __graft_entry__
+
+    __graft_entry__.build()
+    return run_engine(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

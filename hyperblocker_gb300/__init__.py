@@ -1,0 +1,360 @@
+"""GB300 rule-based blocking engine -- Python binding of ``libhbx.so``.
+
+The engine is a drop-in for HyperBlocker's pair-evaluation path: same CLI
+flags, YAML rules, CSV inputs and ``id_l,id_r`` output file, with the pair
+evaluation running as hand-written sm_103a CUDA behind the C ABI declared in
+``include/hbx.h``.  This module only marshals arguments through ctypes; there
+is no Python or CPU fallback, and loading fails loudly when the library has
+not been built (``python -m hyperblocker_gb300.build``).
+
+Mirrors of the reference's interfaces:
+
+* :class:`HyperBlocker` -- ``core/hyperblocker.cuh:45-131`` (constructor
+  arguments and ``Run()``), writing the output file like
+  ``core/components/host_reducer.h:80-90``;
+* :func:`run_cli` -- ``examples/run_hyperblocker.cu:22-59``;
+* :class:`Plan` -- ``core/components/execution_plan_generator.h``
+  (``serialized()`` is its ``SerializedExecutionPlan``);
+* :class:`Table` -- ``core/components/data_mngr.h:46-79`` CSV ingest;
+* :class:`Session` / :func:`block` -- ``HostProducer::AsyncSubmit`` +
+  ``blocking_kernel`` for all partitions (``host_producer.h:109-215``,
+  ``global_func.cuh:104-185``).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+from typing import Dict, List, Optional, Sequence, Tuple
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libhbx.so")
+EXE_PATH = os.path.join(HERE, "_build", "run_hyperblocker_exec")
+INT_MAX = 2147483647
+
+OK, ERR_INVALID_ARG, ERR_CUDA, ERR_OOM, ERR_CAPACITY, ERR_WATCHDOG, ERR_PARSE, ERR_IO, \
+    ERR_UNSUPPORTED = range(9)
+MODE_PLAIN, MODE_BATCHED = 0, 1
+_MODES = {"plain": MODE_PLAIN, "batched": MODE_BATCHED}
+
+
+class HbxError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"hbx status {status}: {message}")
+        self.status = status
+        self.message = message
+
+
+class Opts(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_uint32), ("use_graph", ctypes.c_int32),
+                ("tile_right", ctypes.c_int32), ("warps_per_cta", ctypes.c_int32),
+                ("watchdog_cycles", ctypes.c_uint64)]
+
+
+class Columns(ctypes.Structure):
+    _fields_ = [("n_rows", ctypes.c_int64), ("n_cols", ctypes.c_int32),
+                ("data", ctypes.POINTER(ctypes.c_char_p)),
+                ("offsets", ctypes.POINTER(ctypes.POINTER(ctypes.c_int64)))]
+
+
+class Pairs(ctypes.Structure):
+    _fields_ = [("l_row", ctypes.c_void_p), ("r_row", ctypes.c_void_p),
+                ("capacity", ctypes.c_uint64), ("n_written", ctypes.c_uint64),
+                ("n_required", ctypes.c_uint64)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("pairs_covered", ctypes.c_uint64), ("pair_comparisons", ctypes.c_uint64),
+                ("n_matches", ctypes.c_uint64), ("fma_ambiguous", ctypes.c_uint64),
+                ("long_string_pairs", ctypes.c_uint64), ("n_tiles", ctypes.c_uint64),
+                ("n_partitions_used", ctypes.c_uint32), ("n_launches", ctypes.c_uint32),
+                ("ms_last_run", ctypes.c_double), ("ms_join", ctypes.c_double),
+                ("ms_eval", ctypes.c_double), ("jw_word_ops", ctypes.c_uint64),
+                ("h2d_bytes", ctypes.c_uint64)]
+
+    def as_dict(self) -> Dict[str, float]:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+# Every function include/hbx.h declares: name -> (restype, argtypes).
+_VP = ctypes.c_void_p
+SIGNATURES = {
+    "hbx_ctx_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(Opts), ctypes.POINTER(_VP)]),
+    "hbx_ctx_destroy": (ctypes.c_int, [_VP]),
+    "hbx_last_error": (ctypes.c_char_p, [_VP]),
+    "hbx_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "hbx_plan_from_rule_dir": (ctypes.c_int, [_VP, ctypes.c_char_p, ctypes.POINTER(_VP)]),
+    "hbx_plan_from_yaml": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_char_p), ctypes.c_int32,
+                                          ctypes.POINTER(_VP)]),
+    "hbx_plan_serialized": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_int32),
+                                           ctypes.POINTER(ctypes.POINTER(ctypes.c_int32)),
+                                           ctypes.POINTER(ctypes.POINTER(ctypes.c_char)),
+                                           ctypes.POINTER(ctypes.POINTER(ctypes.c_float))]),
+    "hbx_plan_n_rules": (ctypes.c_int32, [_VP]),
+    "hbx_plan_destroy": (ctypes.c_int, [_VP]),
+    "hbx_table_from_csv": (ctypes.c_int, [_VP, ctypes.c_char_p, ctypes.c_char, ctypes.POINTER(_VP)]),
+    "hbx_table_ingest": (ctypes.c_int, [_VP, ctypes.POINTER(Columns), ctypes.POINTER(_VP)]),
+    "hbx_table_n_rows": (ctypes.c_int64, [_VP]),
+    "hbx_table_n_cols": (ctypes.c_int32, [_VP]),
+    "hbx_table_destroy": (ctypes.c_int, [_VP]),
+    "hbx_session_create": (ctypes.c_int, [_VP, _VP, _VP, _VP, ctypes.c_uint64, ctypes.c_int64,
+                                          ctypes.POINTER(_VP)]),
+    "hbx_session_run": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.POINTER(Pairs), _VP]),
+    "hbx_session_stats": (ctypes.c_int, [_VP, ctypes.POINTER(Stats)]),
+    "hbx_session_destroy": (ctypes.c_int, [_VP]),
+    "hbx_block": (ctypes.c_int, [_VP, _VP, _VP, _VP, ctypes.c_uint64, ctypes.c_int64, ctypes.c_int,
+                                 ctypes.POINTER(Pairs), ctypes.POINTER(Stats)]),
+    "hbx_write_pairs": (ctypes.c_int, [_VP, _VP, _VP, _VP, _VP, ctypes.c_uint64, ctypes.c_char_p]),
+    "hbx_run_cli": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_char_p)]),
+}
+
+_lib: Optional[ctypes.CDLL] = None
+
+
+def lib() -> ctypes.CDLL:
+    """The engine library.  Raises if it has not been built: no fallback."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing; build it with "
+                               "`python -m hyperblocker_gb300.build`")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(status: int, ctx=None) -> None:
+    if status != OK:
+        msg = lib().hbx_last_error(ctx)
+        raise HbxError(status, (msg or b"").decode(errors="replace"))
+
+
+class Context:
+    """A CUDA device + stream for the engine (hbx_ctx)."""
+
+    def __init__(self, device: int = 0, use_graph: bool = True, tile_right: int = 0,
+                 watchdog_cycles: int = 0):
+        o = Opts(ctypes.sizeof(Opts), 1 if use_graph else 0, tile_right, 0, watchdog_cycles)
+        h = _VP()
+        _check(lib().hbx_ctx_create(device, ctypes.byref(o), ctypes.byref(h)))
+        self.h = h
+
+    def close(self) -> None:
+        if self.h:
+            lib().hbx_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+class Plan:
+    """Rules in the reference's order plus the engine's evaluation order."""
+
+    def __init__(self, handle, ctx: Optional[Context] = None):
+        self.h = handle
+        self.ctx = ctx
+
+    @classmethod
+    def from_rule_dir(cls, rule_dir: str, ctx: Optional[Context] = None) -> "Plan":
+        h = _VP()
+        c = ctx.h if ctx else None
+        _check(lib().hbx_plan_from_rule_dir(c, rule_dir.encode(), ctypes.byref(h)), c)
+        return cls(h, ctx)
+
+    @classmethod
+    def from_yaml(cls, docs: Sequence[str], ctx: Optional[Context] = None) -> "Plan":
+        arr = (ctypes.c_char_p * max(len(docs), 1))(*[d.encode() for d in docs])
+        h = _VP()
+        c = ctx.h if ctx else None
+        _check(lib().hbx_plan_from_yaml(c, arr, len(docs), ctypes.byref(h)), c)
+        return cls(h, ctx)
+
+    def serialized(self) -> Tuple[List[int], bytes, List[float]]:
+        n = ctypes.c_int32()
+        pi = ctypes.POINTER(ctypes.c_int32)()
+        pt = ctypes.POINTER(ctypes.c_char)()
+        th = ctypes.POINTER(ctypes.c_float)()
+        _check(lib().hbx_plan_serialized(self.h, ctypes.byref(n), ctypes.byref(pi),
+                                         ctypes.byref(pt), ctypes.byref(th)))
+        k = n.value
+        return [pi[i] for i in range(k)], bytes(pt[i][0] for i in range(k)), [th[i] for i in range(k)]
+
+    @property
+    def n_rules(self) -> int:
+        return lib().hbx_plan_n_rules(self.h)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().hbx_plan_destroy(self.h)
+            self.h = None
+
+
+class Table:
+    """Host table (rows x columns of byte strings), CSV header line included."""
+
+    def __init__(self, handle):
+        self.h = handle
+
+    @classmethod
+    def from_csv(cls, path: str, sep: str = ",", ctx: Optional[Context] = None) -> "Table":
+        h = _VP()
+        c = ctx.h if ctx else None
+        _check(lib().hbx_table_from_csv(c, path.encode(), sep.encode()[:1] or b",", ctypes.byref(h)), c)
+        return cls(h)
+
+    @classmethod
+    def from_columns(cls, cols: Sequence[Sequence[bytes]], ctx: Optional[Context] = None) -> "Table":
+        n_cols = len(cols)
+        n_rows = len(cols[0]) if n_cols else 0
+        datas, offs = [], []
+        for col in cols:
+            if len(col) != n_rows:
+                raise ValueError("columns differ in length")
+            blob = b"".join(col)
+            off = np.zeros(n_rows + 1, dtype=np.int64)
+            if n_rows:
+                off[1:] = np.cumsum([len(x) for x in col])
+            datas.append(ctypes.create_string_buffer(blob, max(len(blob), 1)))
+            offs.append(off)
+        data_arr = (ctypes.c_char_p * max(n_cols, 1))(*[ctypes.cast(d, ctypes.c_char_p) for d in datas])
+        off_arr = (ctypes.POINTER(ctypes.c_int64) * max(n_cols, 1))(
+            *[o.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)) for o in offs])
+        cs = Columns(n_rows, n_cols, ctypes.cast(data_arr, ctypes.POINTER(ctypes.c_char_p)),
+                     ctypes.cast(off_arr, ctypes.POINTER(ctypes.POINTER(ctypes.c_int64))))
+        h = _VP()
+        c = ctx.h if ctx else None
+        _check(lib().hbx_table_ingest(c, ctypes.byref(cs), ctypes.byref(h)), c)
+        return cls(h)
+
+    @property
+    def n_rows(self) -> int:
+        return lib().hbx_table_n_rows(self.h)
+
+    @property
+    def n_cols(self) -> int:
+        return lib().hbx_table_n_cols(self.h)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().hbx_table_destroy(self.h)
+            self.h = None
+
+
+def _mode(mode) -> int:
+    return _MODES[mode] if isinstance(mode, str) else int(mode)
+
+
+class Session:
+    """Both tables encoded for one plan and resident on the GPU."""
+
+    def __init__(self, ctx: Context, plan: Plan, left: Table, right: Table,
+                 n_partitions: int = 1, prefix_idx: int = INT_MAX):
+        h = _VP()
+        _check(lib().hbx_session_create(ctx.h, plan.h, left.h, right.h, n_partitions, prefix_idx,
+                                        ctypes.byref(h)), ctx.h)
+        self.h = h
+        self.ctx = ctx
+        self._keep = (plan, left, right)
+
+    def run_device(self, mode, out_l_ptr: int, out_r_ptr: int, capacity: int,
+                   stream_ptr: Optional[int] = None) -> int:
+        """Runs on device-resident inputs into device buffers; returns matches."""
+        p = Pairs(out_l_ptr, out_r_ptr, capacity, 0, 0)
+        st = lib().hbx_session_run(self.h, _mode(mode), ctypes.byref(p), stream_ptr)
+        if st == ERR_CAPACITY:
+            raise HbxError(st, f"needs capacity {p.n_required}")
+        _check(st, self.ctx.h)
+        return int(p.n_written)
+
+    def stats(self) -> Stats:
+        s = Stats()
+        _check(lib().hbx_session_stats(self.h, ctypes.byref(s)))
+        return s
+
+    def close(self) -> None:
+        if self.h:
+            lib().hbx_session_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def block(ctx: Context, plan: Plan, left: Table, right: Table, n_partitions: int = 1,
+          prefix_idx: int = INT_MAX, mode="batched", capacity: int = 1 << 16):
+    """Host tables -> (pairs (n, 2) uint32 of (left row, right row), stats)."""
+    while True:
+        ol = np.empty(max(capacity, 1), dtype=np.uint32)
+        orr = np.empty(max(capacity, 1), dtype=np.uint32)
+        p = Pairs(ol.ctypes.data, orr.ctypes.data, capacity, 0, 0)
+        s = Stats()
+        st = lib().hbx_block(ctx.h, plan.h, left.h, right.h, n_partitions, prefix_idx, _mode(mode),
+                             ctypes.byref(p), ctypes.byref(s))
+        if st == ERR_CAPACITY:
+            capacity = int(p.n_required)
+            continue
+        _check(st, ctx.h)
+        n = int(p.n_written)
+        return np.stack([ol[:n], orr[:n]], axis=1), s
+
+
+def write_pairs(left: Table, right: Table, pairs: np.ndarray, path: str,
+                ctx: Optional[Context] = None) -> None:
+    pairs = np.ascontiguousarray(pairs, dtype=np.uint32)
+    l = np.ascontiguousarray(pairs[:, 0]) if len(pairs) else np.zeros(1, np.uint32)
+    r = np.ascontiguousarray(pairs[:, 1]) if len(pairs) else np.zeros(1, np.uint32)
+    c = ctx.h if ctx else None
+    _check(lib().hbx_write_pairs(c, left.h, right.h, l.ctypes.data, r.ctypes.data, len(pairs),
+                                 path.encode()), c)
+
+
+def run_cli(argv: Sequence[str]) -> int:
+    """``run_hyperblocker_exec`` in-process; argv[0] is the program name."""
+    arr = (ctypes.c_char_p * len(argv))(*[a.encode() for a in argv])
+    return lib().hbx_run_cli(len(argv), arr)
+
+
+class HyperBlocker:
+    """Mirror of ``sics::hyperblocker::core::HyperBlocker`` (core/hyperblocker.cuh:45-131)."""
+
+    def __init__(self, rule_dir: str, data_path_l: str, data_path_r: str, output_path: str,
+                 n_partitions: int, prefix_hash_predicate_index: int = INT_MAX, sep: str = ",",
+                 scheduler_type: str = "CHBL", mode: str = "batched", device: int = 0):
+        self.ctx = Context(device)
+        self.plan = Plan.from_rule_dir(rule_dir, self.ctx)
+        self.left = Table.from_csv(data_path_l, sep, self.ctx)
+        self.right = Table.from_csv(data_path_r, sep, self.ctx)
+        self.output_path = output_path
+        self.n_partitions = n_partitions
+        self.prefix = prefix_hash_predicate_index
+        self.mode = mode
+        self.last_stats: Optional[Stats] = None
+
+    def Run(self) -> np.ndarray:
+        pairs, st = block(self.ctx, self.plan, self.left, self.right, self.n_partitions,
+                          self.prefix, self.mode)
+        order = np.lexsort((pairs[:, 1], pairs[:, 0])) if len(pairs) else np.zeros(0, np.int64)
+        pairs = pairs[order]
+        if self.output_path:
+            write_pairs(self.left, self.right, pairs, self.output_path, self.ctx)
+        self.last_stats = st
+        return pairs

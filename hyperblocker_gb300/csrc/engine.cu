@@ -1,0 +1,626 @@
+// engine.cu -- device state and launch orchestration behind the C ABI.
+//
+// A session owns one plan's encoding of two tables on the GPU and runs the
+// blocking pipeline of kernels.cu in one of two forms:
+//   PLAIN    per partition, per rule: one evaluation launch, the way the
+//            reference submits one blocking_kernel per partition
+//            (host_producer.h:75-104, 199-203);
+//   BATCHED  every rule x partition in one persistent work-stealing launch;
+//            the whole run (counter reset, joins, launch) is captured once
+//            into a CUDA graph and replayed.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cstdio>
+#include <cstring>
+#include <functional>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "encode.h"
+#include "hbx_core.h"
+#include "kernels.cuh"
+
+#define HBX_CUDA(expr)                                                                        \
+  do {                                                                                        \
+    cudaError_t e_ = (expr);                                                                  \
+    if (e_ != cudaSuccess)                                                                    \
+      ::hbx::fail(e_ == cudaErrorMemoryAllocation ? HBX_ERR_OOM : HBX_ERR_CUDA,               \
+                  std::string(#expr) + ": " + cudaGetErrorString(e_));                        \
+  } while (0)
+
+struct hbx_ctx {
+  int device = 0;
+  int n_sm = 0;
+  size_t smem_optin = 0;
+  cudaStream_t stream = nullptr;
+  hbx_opts opts{};
+  std::string err;
+};
+
+namespace hbx {
+
+template <class T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  DBuf(DBuf&& o) noexcept : p(o.p), n(o.n) {
+    o.p = nullptr;
+    o.n = 0;
+  }
+  DBuf& operator=(DBuf&& o) noexcept {
+    if (this != &o) {
+      reset();
+      p = o.p;
+      n = o.n;
+      o.p = nullptr;
+      o.n = 0;
+    }
+    return *this;
+  }
+  ~DBuf() { reset(); }
+  void reset() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void alloc(size_t count) {
+    reset();
+    if (count == 0) count = 1;
+    HBX_CUDA(cudaMalloc((void**)&p, count * sizeof(T)));
+    n = count;
+  }
+  void upload(const std::vector<T>& v, cudaStream_t s) {
+    alloc(v.size());
+    if (!v.empty()) HBX_CUDA(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+  }
+};
+
+struct RuleBufs {
+  DBuf<uint32_t> key_l, key_r, cnt_l, cnt_r, off_l, off_r, cur_l, cur_r, sorted_l, sorted_r;
+  DBuf<unsigned long long> item_off;
+  DBuf<uint32_t> part_u32;
+  DBuf<unsigned long long> part_u64;
+  uint32_t nb = 0;  // scan CTAs over the key domain
+};
+
+struct SideBufs {
+  DBuf<uint32_t> bucket;
+  DBuf<int32_t> eq, comp;
+  DBuf<uint8_t> arena;
+  DBuf<uint32_t> soff, slen;
+};
+
+template <class T>
+std::vector<T> flatten(const std::vector<std::vector<T>>& v, size_t n_rows) {
+  std::vector<T> out;
+  out.reserve(v.size() * n_rows);
+  for (auto& x : v) out.insert(out.end(), x.begin(), x.end());
+  return out;
+}
+
+}  // namespace hbx
+
+struct hbx_session {
+  hbx_ctx* ctx = nullptr;
+  hbx::Encoded E;
+  hbx::SideBufs L, R;
+  std::vector<hbx::RuleBufs> rb;
+  std::vector<hbx::dev::Rule> h_rules;
+  hbx::DBuf<hbx::dev::Rule> d_rules;
+  hbx::DBuf<unsigned long long> d_rule_base;
+  hbx::DBuf<hbx::dev::Counters> d_ctr;
+  hbx::DBuf<uint32_t> out_l, out_r;
+  hbx::DBuf<uint32_t> bound_idx;              // per rule, n_partitions + 1 key indices
+  hbx::DBuf<unsigned long long> bound_val;    // item_off at those keys
+  hbx::dev::Side side_l{}, side_r{};
+  uint32_t warp_words = 4;
+  uint32_t tile_right = 512;
+  int blocks_per_sm = 1;
+  size_t smem_bytes = 0;
+  cudaGraphExec_t graph = nullptr;
+  uint64_t graph_capacity = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;      // whole run
+  cudaEvent_t ev_eval0 = nullptr, ev_eval1 = nullptr;  // join ends / evaluation ends
+  hbx_stats stats{};
+  ~hbx_session() {
+    if (graph) cudaGraphExecDestroy(graph);
+    for (cudaEvent_t e : {ev0, ev1, ev_eval0, ev_eval1})
+      if (e) cudaEventDestroy(e);
+  }
+};
+
+namespace hbx {
+
+namespace {
+
+constexpr int kThreads = dev::kWarpsPerCta * 32;
+
+void launch_check(const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) fail(HBX_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+int row_grid(uint64_t n, int n_sm) {
+  uint64_t g = (n + 255) / 256;
+  return (int)std::max<uint64_t>(1, std::min<uint64_t>(g, (uint64_t)n_sm * 8));
+}
+
+void setup_session(hbx_session* S) {
+  hbx_ctx* C = S->ctx;
+  const Encoded& E = S->E;
+  cudaStream_t st = C->stream;
+  const uint32_t nL = (uint32_t)E.L.n_rows, nR = (uint32_t)E.R.n_rows;
+  auto up_side = [&](const SideEnc& se, SideBufs& sb, dev::Side& ds, uint32_t n) {
+    sb.bucket.upload(se.bucket, st);
+    sb.eq.upload(flatten(se.eq_codes, (size_t)n), st);
+    sb.comp.upload(flatten(se.comp_codes, (size_t)n), st);
+    sb.arena.upload(se.arena, st);
+    sb.soff.upload(flatten(se.str_off, (size_t)n), st);
+    sb.slen.upload(flatten(se.str_len, (size_t)n), st);
+    ds.bucket = sb.bucket.p;
+    ds.eq_codes = sb.eq.p;
+    ds.comp_codes = sb.comp.p;
+    ds.arena = sb.arena.p;
+    ds.str_off = sb.soff.p;
+    ds.str_len = sb.slen.p;
+    ds.n_rows = n;
+  };
+  up_side(E.L, S->L, S->side_l, nL);
+  up_side(E.R, S->R, S->side_r, nR);
+
+  if (C->opts.tile_right > 0) S->tile_right = (uint32_t)C->opts.tile_right;
+  S->tile_right = std::max<uint32_t>(32, (S->tile_right + 31) / 32 * 32);
+
+  // shared-memory Peq tables: per rule, per similarity predicate
+  const uint32_t NS = E.n_symbols;
+  const size_t smem_cap = std::min<size_t>(C->smem_optin, 200 * 1024);
+  const uint32_t max_warp_words = (uint32_t)(smem_cap / 4 / dev::kWarpsPerCta) / 4 * 4;
+  uint32_t warp_words = 4;
+  S->rb.clear();
+  S->rb.resize(E.rules.size());
+  S->h_rules.assign(E.rules.size(), dev::Rule{});
+  for (size_t r = 0; r < E.rules.size(); r++) {
+    const RuleEnc& re = E.rules[r];
+    dev::Rule& d = S->h_rules[r];
+    d.n_eq = (uint32_t)re.eq_slot.size();
+    d.n_sim = (uint32_t)re.sim_slot_l.size();
+    d.composite = re.composite ? 1u : 0u;
+    d.comp_index = re.composite ? (uint32_t)re.comp_index : 0u;
+    for (size_t e = 0; e < re.eq_slot.size(); e++) {
+      d.eq_slot[e] = (uint32_t)re.eq_slot[e];
+      d.radix[e] = re.radix[e];
+    }
+    uint32_t off = 0;
+    for (size_t s = 0; s < re.sim_slot_l.size(); s++) {
+      d.sim_l[s] = (uint32_t)re.sim_slot_l[s];
+      d.sim_r[s] = (uint32_t)re.sim_slot_r[s];
+      d.thr[s] = re.thr[s];
+      const uint32_t mx = std::min<uint32_t>(E.L.str_maxlen[(size_t)re.sim_slot_l[s]], kFastMaxLen);
+      const uint32_t S32 = mx ? (uint32_t)dev::row_words((int)((mx + 31) / 32)) : 0u;
+      const uint32_t words = (NS * S32 + 3) / 4 * 4;
+      if (S32 && off + words <= max_warp_words) {
+        d.peq_rows_words[s] = S32;
+        d.peq_off[s] = off;
+        off += words;
+      } else {
+        d.peq_rows_words[s] = 0;  // evaluated by the exact per-lane path
+        d.peq_off[s] = 0;
+      }
+    }
+    warp_words = std::max(warp_words, off);
+    d.domain = (uint32_t)re.domain;
+    RuleBufs& b = S->rb[r];
+    b.key_l.alloc(nL);
+    b.key_r.alloc(nR);
+    b.cnt_l.alloc(re.domain);
+    b.cnt_r.alloc(re.domain);
+    b.off_l.alloc(re.domain);
+    b.off_r.alloc(re.domain);
+    b.cur_l.alloc(re.domain);
+    b.cur_r.alloc(re.domain);
+    b.sorted_l.alloc(nL);
+    b.sorted_r.alloc(nR);
+    b.item_off.alloc(re.domain + 1);
+    b.nb = (uint32_t)((re.domain + dev::kScanChunk - 1) / dev::kScanChunk);
+    b.part_u32.alloc(b.nb);
+    b.part_u64.alloc(b.nb);
+    d.key_l = b.key_l.p;
+    d.key_r = b.key_r.p;
+    d.cnt_l = b.cnt_l.p;
+    d.cnt_r = b.cnt_r.p;
+    d.off_l = b.off_l.p;
+    d.off_r = b.off_r.p;
+    d.cur_l = b.cur_l.p;
+    d.cur_r = b.cur_r.p;
+    d.item_off = b.item_off.p;
+    d.sorted_l = b.sorted_l.p;
+    d.sorted_r = b.sorted_r.p;
+  }
+  S->warp_words = warp_words;
+  S->d_rules.upload(S->h_rules, st);
+  S->d_rule_base.alloc(E.rules.size() + 1);
+  S->d_ctr.alloc(1);
+  S->smem_bytes = (size_t)warp_words * 4 * dev::kWarpsPerCta;
+  HBX_CUDA(cudaFuncSetAttribute(dev::k_eval, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)S->smem_bytes));
+  int bps = 0;
+  HBX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, dev::k_eval, kThreads, S->smem_bytes));
+  S->blocks_per_sm = std::max(1, bps);
+
+  // partition boundaries of every rule's key space (plain form)
+  std::vector<uint32_t> idx;
+  for (auto& re : E.rules)
+    for (uint64_t p = 0; p <= E.n_partitions; p++) idx.push_back((uint32_t)re.part_key_begin[p]);
+  S->bound_idx.upload(idx, st);
+  S->bound_val.alloc(idx.size());
+  S->out_l.alloc(1 << 16);
+  S->out_r.alloc(1 << 16);
+  HBX_CUDA(cudaEventCreate(&S->ev0));
+  HBX_CUDA(cudaEventCreate(&S->ev1));
+  HBX_CUDA(cudaEventCreate(&S->ev_eval0));
+  HBX_CUDA(cudaEventCreate(&S->ev_eval1));
+  uint64_t h2d = 0;
+  for (const SideBufs* sb : {&S->L, &S->R})
+    h2d += sb->bucket.n * 4 + sb->eq.n * 4 + sb->comp.n * 4 + sb->arena.n + sb->soff.n * 4 +
+           sb->slen.n * 4;
+  h2d += S->d_rules.n * sizeof(dev::Rule) + S->bound_idx.n * 4;
+  S->stats.h2d_bytes = h2d;
+  HBX_CUDA(cudaStreamSynchronize(st));
+  S->stats.pairs_covered = E.pairs_covered;
+  S->stats.n_partitions_used = E.n_partitions_used;
+}
+
+__global__ void k_gather_bounds(const dev::Rule* rules, uint32_t n_rules, uint32_t per_rule,
+                                const uint32_t* idx, unsigned long long* out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_rules * per_rule) return;
+  out[i] = rules[i / per_rule].item_off[idx[i]];
+}
+
+// Enqueues counter reset + the joins of every rule.  Returns launches.
+uint32_t enqueue_join(hbx_session* S, cudaStream_t st) {
+  uint32_t launches = 0;
+  HBX_CUDA(cudaMemsetAsync(S->d_ctr.p, 0, sizeof(dev::Counters), st));
+  const uint32_t nL = S->side_l.n_rows, nR = S->side_r.n_rows;
+  const int n_sm = S->ctx->n_sm;
+  for (size_t r = 0; r < S->rb.size(); r++) {
+    RuleBufs& b = S->rb[r];
+    const uint32_t D = S->h_rules[r].domain;
+    HBX_CUDA(cudaMemsetAsync(b.cnt_l.p, 0, D * sizeof(uint32_t), st));
+    HBX_CUDA(cudaMemsetAsync(b.cnt_r.p, 0, D * sizeof(uint32_t), st));
+    HBX_CUDA(cudaMemsetAsync(b.cur_l.p, 0, D * sizeof(uint32_t), st));
+    HBX_CUDA(cudaMemsetAsync(b.cur_r.p, 0, D * sizeof(uint32_t), st));
+    if (nL) dev::k_keys_hist<<<row_grid(nL, n_sm), 256, 0, st>>>(S->side_l, S->d_rules.p, (uint32_t)r, 0);
+    if (nR) dev::k_keys_hist<<<row_grid(nR, n_sm), 256, 0, st>>>(S->side_r, S->d_rules.p, (uint32_t)r, 1);
+    dev::k_scan_partial_u32<<<b.nb, 1024, 0, st>>>(b.cnt_l.p, D, b.part_u32.p);
+    dev::k_scan_top_u32<<<1, 1024, 0, st>>>(b.part_u32.p, b.nb);
+    dev::k_scan_final_u32<<<b.nb, 1024, 0, st>>>(b.cnt_l.p, D, b.part_u32.p, b.off_l.p);
+    dev::k_scan_partial_u32<<<b.nb, 1024, 0, st>>>(b.cnt_r.p, D, b.part_u32.p);
+    dev::k_scan_top_u32<<<1, 1024, 0, st>>>(b.part_u32.p, b.nb);
+    dev::k_scan_final_u32<<<b.nb, 1024, 0, st>>>(b.cnt_r.p, D, b.part_u32.p, b.off_r.p);
+    dev::k_items_partial<<<b.nb, 1024, 0, st>>>(S->d_rules.p, (uint32_t)r, S->tile_right,
+                                                b.part_u64.p, &S->d_ctr.p->comparisons);
+    dev::k_scan_top_u64<<<1, 1024, 0, st>>>(b.part_u64.p, b.nb);
+    dev::k_items_final<<<b.nb, 1024, 0, st>>>(S->d_rules.p, (uint32_t)r, S->tile_right, b.part_u64.p);
+    if (nL) dev::k_scatter<<<row_grid(nL, n_sm), 256, 0, st>>>(S->side_l, S->d_rules.p, (uint32_t)r, 0);
+    if (nR) dev::k_scatter<<<row_grid(nR, n_sm), 256, 0, st>>>(S->side_r, S->d_rules.p, (uint32_t)r, 1);
+    launches += 9 + (nL ? 2 : 0) + (nR ? 2 : 0);
+  }
+  dev::k_rule_base<<<1, 32, 0, st>>>(S->d_rules.p, (uint32_t)S->rb.size(), S->d_rule_base.p);
+  launches++;
+  launch_check("join kernels");
+  return launches;
+}
+
+dev::EvalParams eval_params(hbx_session* S) {
+  dev::EvalParams P{};
+  P.L = S->side_l;
+  P.R = S->side_r;
+  P.rules = S->d_rules.p;
+  P.n_rules = (uint32_t)S->rb.size();
+  P.n_symbols = S->E.n_symbols;
+  P.rule_item_base = S->d_rule_base.p;
+  P.tile_right = S->tile_right;
+  P.warp_words = S->warp_words;
+  P.out_l = S->out_l.p;
+  P.out_r = S->out_r.p;
+  P.capacity = S->out_l.n;
+  P.ctr = S->d_ctr.p;
+  P.watchdog_cycles = S->ctx->opts.watchdog_cycles;
+  return P;
+}
+
+uint32_t enqueue_batched(hbx_session* S, cudaStream_t st) {
+  uint32_t launches = enqueue_join(S, st);
+  dev::EvalParams P = eval_params(S);
+  P.item_begin = 0;
+  P.item_end = 0;
+  P.range_is_device = 1;
+  const int grid = S->ctx->n_sm * S->blocks_per_sm;
+  HBX_CUDA(cudaEventRecord(S->ev_eval0, st));
+  dev::k_eval<<<grid, kThreads, S->smem_bytes, st>>>(P);
+  launch_check("k_eval");
+  HBX_CUDA(cudaEventRecord(S->ev_eval1, st));
+  return launches + 1;
+}
+
+void grow_output(hbx_session* S, uint64_t need) {
+  uint64_t cap = S->out_l.n;
+  while (cap < need) cap *= 2;
+  S->out_l.alloc(cap);
+  S->out_r.alloc(cap);
+  if (S->graph) {
+    cudaGraphExecDestroy(S->graph);
+    S->graph = nullptr;
+  }
+}
+
+dev::Counters read_counters(hbx_session* S, cudaStream_t st) {
+  dev::Counters c{};
+  HBX_CUDA(cudaMemcpyAsync(&c, S->d_ctr.p, sizeof c, cudaMemcpyDeviceToHost, st));
+  HBX_CUDA(cudaStreamSynchronize(st));
+  return c;
+}
+
+// One run into the session's own output buffers; returns the counters.
+dev::Counters run_once(hbx_session* S, hbx_mode mode, cudaStream_t st, uint32_t* launches) {
+  const bool use_graph = S->ctx->opts.use_graph != 0;
+  if (mode == HBX_MODE_BATCHED) {
+    if (use_graph) {
+      if (!S->graph) {
+        cudaGraph_t g = nullptr;
+        HBX_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        uint32_t n = 0;
+        try {
+          n = enqueue_batched(S, st);
+        } catch (...) {
+          cudaStreamEndCapture(st, &g);
+          if (g) cudaGraphDestroy(g);
+          throw;
+        }
+        HBX_CUDA(cudaStreamEndCapture(st, &g));
+        cudaError_t e = cudaGraphInstantiate(&S->graph, g, 0);
+        cudaGraphDestroy(g);
+        HBX_CUDA(e);
+        S->stats.n_launches = n;
+      }
+      HBX_CUDA(cudaGraphLaunch(S->graph, st));
+      *launches = S->stats.n_launches;
+    } else {
+      *launches = enqueue_batched(S, st);
+    }
+    return read_counters(S, st);
+  }
+  // PLAIN: join, then one launch per (partition, rule)
+  uint32_t n = enqueue_join(S, st);
+  const uint32_t n_rules = (uint32_t)S->rb.size();
+  const uint32_t per_rule = (uint32_t)S->E.n_partitions + 1;
+  const uint32_t total = n_rules * per_rule;
+  k_gather_bounds<<<(total + 255) / 256, 256, 0, st>>>(S->d_rules.p, n_rules, per_rule,
+                                                       S->bound_idx.p, S->bound_val.p);
+  n++;
+  launch_check("k_gather_bounds");
+  std::vector<unsigned long long> bounds(total), base(n_rules + 1);
+  HBX_CUDA(cudaMemcpyAsync(bounds.data(), S->bound_val.p, total * sizeof(unsigned long long),
+                           cudaMemcpyDeviceToHost, st));
+  HBX_CUDA(cudaMemcpyAsync(base.data(), S->d_rule_base.p, (n_rules + 1) * sizeof(unsigned long long),
+                           cudaMemcpyDeviceToHost, st));
+  HBX_CUDA(cudaStreamSynchronize(st));
+  dev::EvalParams P = eval_params(S);
+  P.range_is_device = 0;
+  const int max_grid = S->ctx->n_sm * S->blocks_per_sm;
+  HBX_CUDA(cudaEventRecord(S->ev_eval0, st));
+  for (uint64_t p = 0; p < S->E.n_partitions; p++) {
+    for (uint32_t r = 0; r < n_rules; r++) {
+      const unsigned long long b0 = base[r] + bounds[(size_t)r * per_rule + p];
+      const unsigned long long b1 = base[r] + bounds[(size_t)r * per_rule + p + 1];
+      if (b1 <= b0) continue;
+      P.item_begin = b0;
+      P.item_end = b1;
+      HBX_CUDA(cudaMemsetAsync(&S->d_ctr.p->work_next, 0, sizeof(unsigned long long), st));
+      const unsigned long long ctas = (b1 - b0 + dev::kWarpsPerCta - 1) / dev::kWarpsPerCta;
+      const int grid = (int)std::min<unsigned long long>(ctas, (unsigned long long)max_grid);
+      dev::k_eval<<<grid, kThreads, S->smem_bytes, st>>>(P);
+      n++;
+      launch_check("k_eval (plain)");
+    }
+  }
+  HBX_CUDA(cudaEventRecord(S->ev_eval1, st));
+  *launches = n;
+  S->stats.n_launches = n;
+  return read_counters(S, st);
+}
+
+}  // namespace
+
+void session_run(hbx_session* S, hbx_mode mode, cudaStream_t st) {
+  HBX_CUDA(cudaSetDevice(S->ctx->device));
+  uint32_t launches = 0;
+  for (int attempt = 0; attempt < 8; attempt++) {
+    HBX_CUDA(cudaEventRecord(S->ev0, st));
+    dev::Counters c = run_once(S, mode, st, &launches);
+    HBX_CUDA(cudaEventRecord(S->ev1, st));
+    HBX_CUDA(cudaEventSynchronize(S->ev1));
+    float ms = 0, ms_join = 0, ms_eval = 0;
+    HBX_CUDA(cudaEventElapsedTime(&ms, S->ev0, S->ev1));
+    HBX_CUDA(cudaEventElapsedTime(&ms_join, S->ev0, S->ev_eval0));
+    HBX_CUDA(cudaEventElapsedTime(&ms_eval, S->ev_eval0, S->ev_eval1));
+    S->stats.ms_last_run = ms;
+    S->stats.ms_join = ms_join;
+    S->stats.ms_eval = ms_eval;
+    S->stats.jw_word_ops = c.jw_word_ops;
+    S->stats.pair_comparisons = c.comparisons;
+    S->stats.n_matches = c.out_count;
+    S->stats.fma_ambiguous = c.ambiguous;
+    S->stats.long_string_pairs = c.long_pairs;
+    S->stats.n_launches = launches;
+    unsigned long long total_items = 0;
+    HBX_CUDA(cudaMemcpyAsync(&total_items, S->d_rule_base.p + S->rb.size(), sizeof total_items,
+                             cudaMemcpyDeviceToHost, st));
+    HBX_CUDA(cudaStreamSynchronize(st));
+    S->stats.n_tiles = total_items;
+    if (c.watchdog_trips) fail(HBX_ERR_WATCHDOG, "evaluation stopped by the watchdog budget");
+    if (c.items_done != total_items)
+      fail(HBX_ERR_CUDA, "evaluation finished " + std::to_string(c.items_done) + " of " +
+                             std::to_string(total_items) + " work items");
+    if (c.out_count <= S->out_l.n) return;
+    grow_output(S, c.out_count);
+  }
+  fail(HBX_ERR_CAPACITY, "output kept growing");
+}
+
+}  // namespace hbx
+
+// ============================================================== C ABI (CUDA)
+namespace {
+
+hbx_status guard(hbx_ctx* ctx, const std::function<void()>& f) {
+  try {
+    f();
+    if (ctx) ctx->err.clear();
+    return HBX_OK;
+  } catch (const hbx::Error& e) {
+    if (ctx) ctx->err = e.what();
+    return e.status;
+  } catch (const std::bad_alloc&) {
+    if (ctx) ctx->err = "host out of memory";
+    return HBX_ERR_OOM;
+  } catch (const std::exception& e) {
+    if (ctx) ctx->err = e.what();
+    return HBX_ERR_INVALID_ARG;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+hbx_status hbx_ctx_create(int device, const hbx_opts* opts, hbx_ctx** out) {
+  if (!out) return HBX_ERR_INVALID_ARG;
+  *out = nullptr;
+  auto ctx = std::make_unique<hbx_ctx>();
+  ctx->opts.struct_size = sizeof(hbx_opts);
+  ctx->opts.use_graph = 1;
+  if (opts) {
+    if (opts->struct_size != sizeof(hbx_opts)) return HBX_ERR_INVALID_ARG;
+    ctx->opts = *opts;
+  }
+  hbx_status s = guard(ctx.get(), [&] {
+    int n = 0;
+    HBX_CUDA(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) hbx::fail(HBX_ERR_INVALID_ARG, "no such CUDA device");
+    ctx->device = device;
+    HBX_CUDA(cudaSetDevice(device));
+    cudaDeviceProp prop;
+    HBX_CUDA(cudaGetDeviceProperties(&prop, device));
+    ctx->n_sm = prop.multiProcessorCount;
+    ctx->smem_optin = prop.sharedMemPerBlockOptin;
+    HBX_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+  });
+  if (s != HBX_OK) return s;
+  *out = ctx.release();
+  return HBX_OK;
+}
+
+hbx_status hbx_ctx_destroy(hbx_ctx* ctx) {
+  if (!ctx) return HBX_ERR_INVALID_ARG;
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return HBX_OK;
+}
+
+const char* hbx_host_last_error(void);
+
+const char* hbx_last_error(const hbx_ctx* ctx) {
+  return ctx ? ctx->err.c_str() : hbx_host_last_error();
+}
+
+void hbx_internal_set_error(hbx_ctx* ctx, const char* msg) {
+  if (ctx) ctx->err = msg ? msg : "";
+}
+
+hbx_status hbx_session_create(hbx_ctx* ctx, const hbx_plan* plan, const hbx_table* left,
+                              const hbx_table* right, uint64_t n_partitions, int64_t prefix_idx,
+                              hbx_session** out) {
+  if (!ctx || !plan || !left || !right || !out) return HBX_ERR_INVALID_ARG;
+  *out = nullptr;
+  auto S = std::make_unique<hbx_session>();
+  S->ctx = ctx;
+  hbx_status st = guard(ctx, [&] {
+    if (prefix_idx != INT_MAX && (prefix_idx < 0 || prefix_idx > INT_MAX))
+      hbx::fail(HBX_ERR_INVALID_ARG, "prefix_idx out of range");
+    HBX_CUDA(cudaSetDevice(ctx->device));
+    S->E = hbx::encode(plan->p, left->t, right->t, n_partitions, prefix_idx);
+    hbx::setup_session(S.get());
+  });
+  if (st != HBX_OK) return st;
+  *out = S.release();
+  return HBX_OK;
+}
+
+hbx_status hbx_session_run(hbx_session* s, hbx_mode mode, hbx_pairs* out, void* stream) {
+  if (!s || !out) return HBX_ERR_INVALID_ARG;
+  if (mode != HBX_MODE_PLAIN && mode != HBX_MODE_BATCHED) return HBX_ERR_INVALID_ARG;
+  return guard(s->ctx, [&] {
+    cudaStream_t st = stream ? (cudaStream_t)stream : s->ctx->stream;
+    hbx::session_run(s, mode, st);
+    const uint64_t n = s->stats.n_matches;
+    out->n_required = n;
+    out->n_written = 0;
+    if (n > out->capacity) hbx::fail(HBX_ERR_CAPACITY, "output capacity below the match count");
+    if (n) {
+      if (!out->l_row || !out->r_row) hbx::fail(HBX_ERR_INVALID_ARG, "null output pointer");
+      HBX_CUDA(cudaMemcpyAsync(out->l_row, s->out_l.p, n * 4, cudaMemcpyDeviceToDevice, st));
+      HBX_CUDA(cudaMemcpyAsync(out->r_row, s->out_r.p, n * 4, cudaMemcpyDeviceToDevice, st));
+      HBX_CUDA(cudaStreamSynchronize(st));
+    }
+    out->n_written = n;
+  });
+}
+
+hbx_status hbx_session_stats(const hbx_session* s, hbx_stats* out) {
+  if (!s || !out) return HBX_ERR_INVALID_ARG;
+  *out = s->stats;
+  return HBX_OK;
+}
+
+hbx_status hbx_session_destroy(hbx_session* s) {
+  if (!s) return HBX_ERR_INVALID_ARG;
+  cudaSetDevice(s->ctx->device);
+  delete s;
+  return HBX_OK;
+}
+
+hbx_status hbx_block(hbx_ctx* ctx, const hbx_plan* plan, const hbx_table* left,
+                     const hbx_table* right, uint64_t n_partitions, int64_t prefix_idx,
+                     hbx_mode mode, hbx_pairs* out, hbx_stats* stats) {
+  if (!ctx || !out) return HBX_ERR_INVALID_ARG;
+  hbx_session* s = nullptr;
+  hbx_status st = hbx_session_create(ctx, plan, left, right, n_partitions, prefix_idx, &s);
+  if (st != HBX_OK) return st;
+  st = guard(ctx, [&] {
+    hbx::session_run(s, mode, ctx->stream);
+    const uint64_t n = s->stats.n_matches;
+    out->n_required = n;
+    out->n_written = 0;
+    if (stats) *stats = s->stats;
+    if (n > out->capacity) hbx::fail(HBX_ERR_CAPACITY, "output capacity below the match count");
+    if (n) {
+      if (!out->l_row || !out->r_row) hbx::fail(HBX_ERR_INVALID_ARG, "null output pointer");
+      HBX_CUDA(cudaMemcpyAsync(out->l_row, s->out_l.p, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+      HBX_CUDA(cudaMemcpyAsync(out->r_row, s->out_r.p, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+      HBX_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+    out->n_written = n;
+  });
+  hbx_session_destroy(s);
+  return st;
+}
+
+}  // extern "C"

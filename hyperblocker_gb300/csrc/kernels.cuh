@@ -1,0 +1,128 @@
+// kernels.cuh -- sm_103a device code of the blocking engine.
+//
+// Pipeline per run (all on one stream; the batched form is a CUDA graph):
+//   1. k_keys_hist    join key of every row per rule (partition bucket and
+//                     equality dictionary codes in mixed radix, or a dense
+//                     composite id) + histogram of keys per side.
+//   2. scan kernels   exclusive scans: row offsets per key, and work items
+//                     per key (a work item = one left row x up to TR right rows
+//                     of one candidate block).
+//   3. k_scatter      rows grouped by key (counting sort) -> candidate blocks
+//                     L_key x R_key.
+//   4. k_eval         persistent, warp-granular work stealing over the items
+//                     of every rule: the warp's left string becomes a Peq
+//                     bitmask table in shared memory (built with __match_any),
+//                     each lane runs bit-parallel Jaro over one right string,
+//                     Jaro-Winkler is decided exactly, survivors leave by
+//                     warp-aggregated atomics.
+//
+// Semantics reproduced (reference = HyperBlocker):
+//   * pairs are compared only inside a partition (data_mngr.h:150-216, the
+//     bucket is part of every join key);
+//   * a pair matches when some rule has all equalities true and all
+//     similarities !(JW < (double)threshold) (global_func.cuh:120-167);
+//   * Jaro match count m of device_func.cuh:54-132 equals the size of a
+//     maximum matching between equal characters at distance <= h,
+//     h = (min(len1, len2) + 1) / 2, whenever the shorter string has at most
+//     256 bytes; longer pairs run the reference's own loop order (jaro_m_ref);
+//   * the Jaro value is (float)(((double)(m/ls + m/ll) + 1.0) / 3.0) with IEEE
+//     float quotients, and JW = fma((1 - j) * p, 0.1, j) clamped to 1 with an
+//     uncapped common prefix p (device_func.cuh:210-231).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace hbx {
+namespace dev {
+
+constexpr int kMaxEq = 8;
+constexpr int kMaxSim = 8;
+constexpr int kWarpsPerCta = 8;
+// words per symbol row of a Peq table for a left string of w 32-bit words
+__host__ __device__ constexpr int row_words(int w) { return w <= 1 ? 1 : w <= 2 ? 2 : w <= 4 ? 4 : 8; }
+constexpr float kDecisionMargin = 1e-4f;  // |approx JW - thr| below this -> exact path
+
+struct Side {
+  const uint32_t* bucket;
+  const int32_t* eq_codes;    // [n_eq_slots][n_rows]
+  const int32_t* comp_codes;  // [n_comp][n_rows]
+  const uint8_t* arena;       // symbol strings, 16-byte aligned, zero padded
+  const uint32_t* str_off;    // [n_str_slots][n_rows], units of 16 bytes
+  const uint32_t* str_len;    // [n_str_slots][n_rows]
+  uint32_t n_rows;
+};
+
+struct Rule {
+  uint32_t n_eq, n_sim, composite, comp_index;
+  uint32_t eq_slot[kMaxEq];
+  uint32_t radix[kMaxEq];
+  uint32_t sim_l[kMaxSim], sim_r[kMaxSim];
+  float thr[kMaxSim];
+  uint32_t peq_rows_words[kMaxSim];  // words per symbol row reserved (1,2,4,8), 0 = none
+  uint32_t peq_off[kMaxSim];         // word offset of the sim's table in a warp region
+  uint32_t domain;
+  uint32_t* key_l;
+  uint32_t* key_r;
+  uint32_t* cnt_l;
+  uint32_t* cnt_r;
+  uint32_t* off_l;
+  uint32_t* off_r;
+  uint32_t* cur_l;
+  uint32_t* cur_r;
+  unsigned long long* item_off;  // [domain + 1]
+  uint32_t* sorted_l;
+  uint32_t* sorted_r;
+};
+
+struct Counters {
+  unsigned long long out_count;
+  unsigned long long comparisons;
+  unsigned long long ambiguous;
+  unsigned long long long_pairs;
+  unsigned long long work_next;
+  unsigned long long watchdog_trips;
+  unsigned long long items_done;
+  unsigned long long jw_word_ops;  // algorithmic work of the JW evaluations
+};
+
+struct EvalParams {
+  Side L, R;
+  const Rule* rules;
+  uint32_t n_rules;
+  uint32_t n_symbols;
+  const unsigned long long* rule_item_base;  // [n_rules + 1], global item space
+  // item range [item_begin, item_end) in the global space; the batched form
+  // covers every rule, the plain form one (partition, rule).
+  unsigned long long item_begin;
+  unsigned long long item_end;
+  int range_is_device;  // 1: item_end = rule_item_base[n_rules] (read on device)
+  uint32_t tile_right;  // TR
+  uint32_t warp_words;  // shared-memory words per warp
+  uint32_t* out_l;
+  uint32_t* out_r;
+  unsigned long long capacity;
+  Counters* ctr;
+  unsigned long long watchdog_cycles;  // 0 = no budget
+};
+
+// ------------------------------------------------------------------ join
+__global__ void k_keys_hist(Side S, const Rule* rules, uint32_t rule, int side);
+__global__ void k_scatter(Side S, const Rule* rules, uint32_t rule, int side);
+__global__ void k_scan_partial_u32(const uint32_t* in, uint32_t n, uint32_t* partial);
+__global__ void k_scan_top_u32(uint32_t* partial, uint32_t nb);
+__global__ void k_scan_final_u32(const uint32_t* in, uint32_t n, const uint32_t* partial,
+                                 uint32_t* out);
+__global__ void k_items_partial(const Rule* rules, uint32_t rule, uint32_t tile_right,
+                                unsigned long long* partial, unsigned long long* comparisons);
+__global__ void k_scan_top_u64(unsigned long long* partial, uint32_t nb);
+__global__ void k_items_final(const Rule* rules, uint32_t rule, uint32_t tile_right,
+                              const unsigned long long* partial);
+__global__ void k_rule_base(const Rule* rules, uint32_t n_rules, unsigned long long* base);
+// ------------------------------------------------------------------ evaluation
+__global__ void k_eval(EvalParams P);
+
+constexpr uint32_t kScanChunk = 4096;  // elements per CTA in the scans (1024 threads x 4)
+
+}  // namespace dev
+}  // namespace hbx

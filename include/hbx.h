@@ -1,0 +1,177 @@
+/* hbx.h -- C ABI of the GB300 rule-based blocking engine (libhbx.so).
+ *
+ * The engine evaluates HyperBlocker rules (equalities + Jaro-Winkler
+ * similarity predicates, OR across rules, AND within a rule) over every
+ * left x right pair of the reference's hash partitions and returns the
+ * matching (left row, right row) pairs.  Row numbers count CSV lines from 0,
+ * the header line included, because the reference reads the header as data
+ * (core/components/data_mngr.h:48-51, rapidcsv LabelParams(-1, -1)).
+ *
+ * Every call returns an hbx_status; no C++ exception crosses this boundary.
+ * hbx_last_error() gives the text of the last failure on a context.
+ * A context is used by one host thread at a time.
+ *
+ * Reference interfaces replaced (paths inside the HyperBlocker project):
+ *   examples/run_hyperblocker.cu:22-59         -> hbx_run_cli
+ *   core/hyperblocker.cuh:45-131 (HyperBlocker) -> hbx_ctx_* / hbx_block
+ *   core/components/execution_plan_generator.h:64-155
+ *                                               -> hbx_plan_from_rule_dir,
+ *                                                  hbx_plan_from_yaml,
+ *                                                  hbx_plan_serialized
+ *   core/components/data_mngr.h:46-79 (CSV ingest)
+ *                                               -> hbx_table_from_csv,
+ *                                                  hbx_table_ingest
+ *   core/components/data_mngr.h:81-222 (partitioning) +
+ *   core/components/host_producer.h:109-215 (AsyncSubmit) +
+ *   core/gpu/global_func.cuh:104-185 (blocking_kernel)
+ *                                               -> hbx_session_create /
+ *                                                  hbx_session_run, hbx_block
+ *   core/components/host_reducer.h:80-90 (WriteMatch)
+ *                                               -> hbx_write_pairs
+ */
+#ifndef HBX_H_
+#define HBX_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum hbx_status {
+  HBX_OK = 0,
+  HBX_ERR_INVALID_ARG = 1,
+  HBX_ERR_CUDA = 2,
+  HBX_ERR_OOM = 3,
+  HBX_ERR_CAPACITY = 4,   /* output buffer too small; n_required is set, nothing partial */
+  HBX_ERR_WATCHDOG = 5,   /* a device loop exceeded its time budget and stopped */
+  HBX_ERR_PARSE = 6,      /* malformed CSV or YAML rule */
+  HBX_ERR_IO = 7,         /* file could not be read or written */
+  HBX_ERR_UNSUPPORTED = 8 /* input the engine refuses (undefined in the reference) */
+} hbx_status;
+
+typedef enum hbx_mode {
+  /* one launch per (partition, rule), like the reference's per-partition
+   * AsyncSubmit loop (host_producer.h:75-104) */
+  HBX_MODE_PLAIN = 0,
+  /* every rule x partition in one persistent work-stealing launch, replayed
+   * from a CUDA graph */
+  HBX_MODE_BATCHED = 1
+} hbx_mode;
+
+typedef struct hbx_ctx hbx_ctx;
+typedef struct hbx_plan hbx_plan;
+typedef struct hbx_table hbx_table;
+typedef struct hbx_session hbx_session;
+typedef struct hbx_server hbx_server;
+
+typedef struct hbx_opts {
+  uint32_t struct_size;      /* sizeof(hbx_opts) */
+  int32_t use_graph;         /* batched mode replays a CUDA graph (default 1) */
+  int32_t tile_right;        /* right rows per tile, 0 = autotuned/default */
+  int32_t warps_per_cta;     /* left rows per tile, 0 = autotuned/default */
+  uint64_t watchdog_cycles;  /* per-CTA SM-cycle budget of the persistent loop, 0 = none */
+} hbx_opts;
+
+/* Column-major host strings: cell (r, c) is data[c][offsets[c][r] .. offsets[c][r+1]). */
+typedef struct hbx_columns {
+  int64_t n_rows;
+  int32_t n_cols;
+  const char* const* data;
+  const int64_t* const* offsets;
+} hbx_columns;
+
+/* Output pair buffer.  hbx_session_run takes device pointers, hbx_block
+ * host pointers. */
+typedef struct hbx_pairs {
+  uint32_t* l_row;
+  uint32_t* r_row;
+  uint64_t capacity;
+  uint64_t n_written;   /* out */
+  uint64_t n_required;  /* out: total matches (also when HBX_ERR_CAPACITY) */
+} hbx_pairs;
+
+typedef struct hbx_stats {
+  uint64_t pairs_covered;     /* sum over partitions of |L_p| * |R_p| */
+  uint64_t pair_comparisons;  /* (rule, l, r) triples whose equalities hold */
+  uint64_t n_matches;         /* distinct matching pairs */
+  uint64_t fma_ambiguous;     /* JW decisions that differ with/without FMA (reported) */
+  uint64_t long_string_pairs; /* JW evaluations whose shorter string > 256 bytes */
+  uint64_t n_tiles;           /* work items of the last run */
+  uint32_t n_partitions_used; /* partitions with both sides non-empty */
+  uint32_t n_launches;        /* kernels launched by the last run */
+  double ms_last_run;         /* device time of the last run (CUDA events) */
+  double ms_join;             /* device time of the equality join phase */
+  double ms_eval;             /* device time of the pair-evaluation kernel(s) */
+  uint64_t jw_word_ops;       /* algorithmic 64-bit word operations of the JW phase */
+  uint64_t h2d_bytes;         /* bytes uploaded when the session was created */
+} hbx_stats;
+
+/* ---- context ------------------------------------------------------------ */
+hbx_status hbx_ctx_create(int device, const hbx_opts* opts, hbx_ctx** out);
+hbx_status hbx_ctx_destroy(hbx_ctx* ctx);
+const char* hbx_last_error(const hbx_ctx* ctx);
+const char* hbx_status_string(hbx_status s);
+
+/* ---- rules (yaml_config.h:37-75, execution_plan_generator.h:64-155) ----- */
+/* Reads every entry of rule_dir in directory order, decodes each as a rule,
+ * orders rules like the reference (std::sort on equality-list size,
+ * descending) and compiles the evaluation order (equalities first, then
+ * similarity predicates by measured selectivity and cost). */
+hbx_status hbx_plan_from_rule_dir(hbx_ctx* ctx, const char* rule_dir, hbx_plan** out);
+/* Same from in-memory YAML documents, given in directory order. */
+hbx_status hbx_plan_from_yaml(hbx_ctx* ctx, const char* const* docs, int32_t n_docs,
+                              hbx_plan** out);
+/* The reference's serialized plan (execution_plan_generator.h:25-31). */
+hbx_status hbx_plan_serialized(const hbx_plan* plan, int32_t* length,
+                               const int32_t** pred_index, const char** pred_type,
+                               const float** pred_threshold);
+int32_t hbx_plan_n_rules(const hbx_plan* plan);
+hbx_status hbx_plan_destroy(hbx_plan* plan);
+
+/* ---- tables (data_mngr.h:46-79) ----------------------------------------- */
+hbx_status hbx_table_from_csv(hbx_ctx* ctx, const char* path, char sep, hbx_table** out);
+hbx_status hbx_table_ingest(hbx_ctx* ctx, const hbx_columns* cols, hbx_table** out);
+int64_t hbx_table_n_rows(const hbx_table* t);
+int32_t hbx_table_n_cols(const hbx_table* t);
+hbx_status hbx_table_destroy(hbx_table* t);
+
+/* ---- blocking ------------------------------------------------------------ */
+/* Encodes both tables for the plan (partition buckets with the reference's
+ * std::hash, int32 dictionary codes for equality columns, 16-byte-aligned
+ * length-prefixed string arenas), uploads them and sizes the device state.
+ * prefix_idx = INT32_MAX disables the reference's prefix hash. */
+hbx_status hbx_session_create(hbx_ctx* ctx, const hbx_plan* plan, const hbx_table* left,
+                              const hbx_table* right, uint64_t n_partitions, int64_t prefix_idx,
+                              hbx_session** out);
+/* Runs the pair evaluation on device-resident inputs; out holds DEVICE
+ * pointers.  stream may be NULL (the context's stream).  Returns when the
+ * pairs are in out (synchronous on the stream). */
+hbx_status hbx_session_run(hbx_session* s, hbx_mode mode, hbx_pairs* out, void* stream);
+hbx_status hbx_session_stats(const hbx_session* s, hbx_stats* out);
+hbx_status hbx_session_destroy(hbx_session* s);
+
+/* One call from host tables to host pairs: session create + run + copy back.
+ * out holds HOST pointers. */
+hbx_status hbx_block(hbx_ctx* ctx, const hbx_plan* plan, const hbx_table* left,
+                     const hbx_table* right, uint64_t n_partitions, int64_t prefix_idx,
+                     hbx_mode mode, hbx_pairs* out, hbx_stats* stats);
+
+/* Appends "<id_l>,<id_r>\n" lines (column 0 of each table), like
+ * host_reducer.h:80-90.  Pairs are written in the order given. */
+hbx_status hbx_write_pairs(hbx_ctx* ctx, const hbx_table* left, const hbx_table* right,
+                           const uint32_t* l_row, const uint32_t* r_row, uint64_t n,
+                           const char* path);
+
+/* The run_hyperblocker_exec command line (examples/run_hyperblocker.cu:22-59):
+ * -data_l -data_r -rule_dir -o -n_partitions [-sep -scheduler -read_header
+ * -prefix_hash_pred_idx], plus -hbx_mode=plain|batched.  Returns a process
+ * exit code (0 on success). */
+int hbx_run_cli(int argc, const char* const* argv);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HBX_H_ */

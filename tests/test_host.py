@@ -1,0 +1,132 @@
+"""Host logic of the engine without a GPU: CSV tokenization, YAML rule
+decoding, plan serialization and ordering, error statuses, output writer."""
+import os
+
+import numpy as np
+import pytest
+
+import hyperblocker_gb300 as hb
+from oracle import api, csvref, rules
+from hyperblocker_gb300 import synth
+
+README_RULE = """Preconditions:
+  # There are two relation tables, each with 5 columns.
+  Relations:
+    - [0, 0, 1, 2, 3, 4]
+    - [1, 0, 1, 2, 3, 4]
+  # The equality predicate is on the 4th column.
+  Equalities:
+    - [0, 1, 4, 4]
+  Sim:
+    - [0, 1, 1, 1, 2, 2]
+  Threshold:
+    - [0, 1, 0.89, 0.85]
+Conseq:
+  Option:
+    Equality
+  # The ID is in the 0th column.
+  Equality:
+    [0, 1, 0, 0]
+"""
+
+
+@pytest.mark.parametrize("data", [
+    b'"id","t"\r\n1,"a, b"\r\n2,"say ""hi"""\r\n',
+    b'id,t\n1,plain\n2,"quoted"\n3,',
+    b'\xef\xbb\xbfid,t\n1,x\n',
+    b'a,b\n"x""y",z\n"q",w"x\n',
+    b'a,b\n1,\n,2\n',
+])
+def test_csv_matches_rapidcsv_restatement(built, tmp_path, data):
+    p = tmp_path / "t.csv"
+    p.write_bytes(data)
+    want = csvref.read_columns(str(p))
+    t = hb.Table.from_csv(str(p))
+    assert t.n_rows == len(want[0])
+    assert t.n_cols == len(want)
+    # ids come back through the writer, byte for byte
+    out = tmp_path / "o.csv"
+    n = t.n_rows
+    pairs = np.stack([np.arange(n), np.arange(n)], 1).astype(np.uint32)
+    hb.write_pairs(t, t, pairs, str(out))
+    got = out.read_bytes().split(b"\n")[:-1]
+    assert got == [c.split(b"\0")[0] + b"," + c.split(b"\0")[0] for c in want[0]]
+
+
+@pytest.mark.parametrize("data", [b"a,b,c\n1,2\n", b'a,b\n"unterminated,q\n'])
+def test_csv_short_row_is_parse_error(built, tmp_path, data):
+    """rapidcsv's GetColumn throws on a short row; the engine reports PARSE."""
+    p = tmp_path / "t.csv"
+    p.write_bytes(data)
+    with pytest.raises(ValueError):
+        csvref.read_columns(str(p))
+    with pytest.raises(hb.HbxError) as e:
+        hb.Table.from_csv(str(p))
+    assert e.value.status == hb.ERR_PARSE
+
+
+def _oracle_plan(docs):
+    api.build()
+    return rules.serialize(rules.sort_rules([rules.decode_rule(rules.parse_yaml(d)) for d in docs]))
+
+
+@pytest.mark.parametrize("docs", [
+    [README_RULE],
+    [synth.rule_yaml([4], [(1, 0.89), (2, 0.85)]), synth.rule_yaml([3], [(1, 0.95)])],
+    [synth.rule_yaml([], [(1, 0.7)]), synth.rule_yaml([3, 4], [(2, 0.8)]),
+     synth.rule_yaml([4], [(1, 0.6)])],
+    # 20 rules: std::sort is not an insertion sort above 16 elements
+    [synth.rule_yaml([3] * (k % 3), [(1, 0.5 + 0.01 * k)]) for k in range(20)],
+    # two similarities on the same left column: the first threshold wins
+    [README_RULE.replace("[0, 1, 1, 1, 2, 2]", "[0, 1, 1, 1, 1, 2]")],
+])
+def test_plan_matches_reference_serialization(built, docs):
+    want = _oracle_plan(docs)
+    p = hb.Plan.from_yaml(docs)
+    pi, pt, th = p.serialized()
+    assert pi == want.pred_index
+    assert pt == want.pred_type
+    assert np.array_equal(np.float32(th), np.float32(want.pred_threshold))
+    assert p.n_rules == len(docs)
+
+
+@pytest.mark.parametrize("doc,status", [
+    ("Preconditions:\n  Relations:\n    - [0]\n    - [1]\n  Equalities:\n    - [0, 1, 4, 4]\n"
+     "  Sim:\n    - [0, 1, 1, 1]\nConseq:\n  Equality:\n    [0, 1, 0, 0]\n", hb.ERR_UNSUPPORTED),
+    ("just: one\n", hb.ERR_PARSE),
+    ("Preconditions:\n  Relations: [\n", hb.ERR_PARSE),
+    (README_RULE.replace("[0, 1, 0.89, 0.85]", "[0, 1, 0.89]"), hb.ERR_UNSUPPORTED),
+    (README_RULE.replace("[0, 1, 4, 4]", "[0, 1, 4]"), hb.ERR_UNSUPPORTED),
+    (README_RULE.replace("[0, 1, 4, 4]", "[0, 1, x, 4]"), hb.ERR_PARSE),
+])
+def test_bad_rules_are_refused(built, doc, status):
+    with pytest.raises(hb.HbxError) as e:
+        hb.Plan.from_yaml([doc])
+    assert e.value.status == status
+
+
+def test_rule_dir_errors(built, tmp_path):
+    with pytest.raises(hb.HbxError) as e:
+        hb.Plan.from_rule_dir(str(tmp_path / "missing"))
+    assert e.value.status == hb.ERR_IO
+    (tmp_path / "r").mkdir()
+    with pytest.raises(hb.HbxError) as e:
+        hb.Plan.from_rule_dir(str(tmp_path / "r"))
+    assert e.value.status == hb.ERR_PARSE
+
+
+def test_rule_dir_order_is_directory_order(built, tmp_path):
+    d = tmp_path / "rules"
+    d.mkdir()
+    docs = [synth.rule_yaml([4], [(1, 0.89)]), synth.rule_yaml([3], [(1, 0.95)])]
+    for k, doc in enumerate(docs):
+        (d / f"{k}.yaml").write_text(doc)
+    want = rules.plan_from_dir(str(d))
+    pi, pt, th = hb.Plan.from_rule_dir(str(d)).serialized()
+    assert pi == want.pred_index and pt == want.pred_type
+
+
+def test_cli_rejects_unknown_flag(built):
+    assert hb.run_cli(["run_hyperblocker_exec", "-no_such_flag=1"]) == 1
+    assert hb.run_cli(["run_hyperblocker_exec", "-n_partitions=abc"]) == 1
+    assert hb.run_cli(["run_hyperblocker_exec", "-hbx_mode=fast"]) == 1
