@@ -93,7 +93,7 @@ struct SideBufs {
   DBuf<uint32_t> bucket;
   DBuf<int32_t> eq, comp;
   DBuf<uint8_t> arena;
-  DBuf<uint32_t> soff, slen;
+  DBuf<uint4> meta;
 };
 
 template <class T>
@@ -120,7 +120,9 @@ struct hbx_session {
   hbx::DBuf<unsigned long long> bound_val;    // item_off at those keys
   hbx::dev::Side side_l{}, side_r{};
   uint32_t warp_words = 4;
-  uint32_t tile_right = 512;
+  uint32_t tile_right = 128;
+  uint32_t list_off = 0;
+  uint32_t queue_off = 0;
   int blocks_per_sm = 1;
   size_t smem_bytes = 0;
   cudaGraphExec_t graph = nullptr;
@@ -161,26 +163,44 @@ void setup_session(hbx_session* S) {
     sb.eq.upload(flatten(se.eq_codes, (size_t)n), st);
     sb.comp.upload(flatten(se.comp_codes, (size_t)n), st);
     sb.arena.upload(se.arena, st);
-    sb.soff.upload(flatten(se.str_off, (size_t)n), st);
-    sb.slen.upload(flatten(se.str_len, (size_t)n), st);
+    // per string: {offset / 16, length, first 8 symbols (0 past the end)}
+    std::vector<uint4> meta;
+    meta.reserve(se.str_off.size() * (size_t)n);
+    for (size_t slot = 0; slot < se.str_off.size(); slot++)
+      for (uint32_t i = 0; i < n; i++) {
+        const uint32_t off = se.str_off[slot][i], len = se.str_len[slot][i];
+        uint8_t pre[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (uint32_t k = 0; k < 8 && k < len; k++) pre[k] = se.arena[(size_t)off * 16 + k];
+        uint4 m;
+        m.x = off;
+        m.y = len;
+        m.z = (uint32_t)pre[0] | (uint32_t)pre[1] << 8 | (uint32_t)pre[2] << 16 | (uint32_t)pre[3] << 24;
+        m.w = (uint32_t)pre[4] | (uint32_t)pre[5] << 8 | (uint32_t)pre[6] << 16 | (uint32_t)pre[7] << 24;
+        meta.push_back(m);
+      }
+    sb.meta.upload(meta, st);
+    HBX_CUDA(cudaStreamSynchronize(st));  // the host vector dies at scope end
     ds.bucket = sb.bucket.p;
     ds.eq_codes = sb.eq.p;
     ds.comp_codes = sb.comp.p;
     ds.arena = sb.arena.p;
-    ds.str_off = sb.soff.p;
-    ds.str_len = sb.slen.p;
+    ds.str_meta = sb.meta.p;
     ds.n_rows = n;
   };
   up_side(E.L, S->L, S->side_l, nL);
   up_side(E.R, S->R, S->side_r, nR);
 
-  if (C->opts.tile_right > 0) S->tile_right = (uint32_t)C->opts.tile_right;
-  S->tile_right = std::max<uint32_t>(32, (S->tile_right + 31) / 32 * 32);
-
   // shared-memory Peq tables: per rule, per similarity predicate
   const uint32_t NS = E.n_symbols;
   const size_t smem_cap = std::min<size_t>(C->smem_optin, 200 * 1024);
-  const uint32_t max_warp_words = (uint32_t)(smem_cap / 4 / dev::kWarpsPerCta) / 4 * 4;
+  if (C->opts.tile_right > 0) S->tile_right = (uint32_t)C->opts.tile_right;
+  S->tile_right = std::min<uint32_t>(2048, std::max<uint32_t>(32, (S->tile_right + 31) / 32 * 32));
+  const uint32_t cap_warp_words = (uint32_t)(smem_cap / 4 / dev::kWarpsPerCta) / 4 * 4;
+  // per warp: Peq tables, then a row list (tile_right words) and a scan queue
+  // (tile_right x 16 bytes)
+  const uint32_t list_queue_words = 5 * S->tile_right;
+  if (list_queue_words + 4 > cap_warp_words) fail(HBX_ERR_INVALID_ARG, "tile_right too large");
+  const uint32_t max_warp_words = cap_warp_words - list_queue_words;
   uint32_t warp_words = 4;
   S->rb.clear();
   S->rb.resize(E.rules.size());
@@ -242,11 +262,18 @@ void setup_session(hbx_session* S) {
     d.sorted_l = b.sorted_l.p;
     d.sorted_r = b.sorted_r.p;
   }
-  S->warp_words = warp_words;
+  // each warp's row list and scan queue follow its Peq tables
+  S->list_off = warp_words;
+  S->queue_off = warp_words + S->tile_right;
+  S->warp_words = S->queue_off + 4 * S->tile_right;
   S->d_rules.upload(S->h_rules, st);
   S->d_rule_base.alloc(E.rules.size() + 1);
   S->d_ctr.alloc(1);
-  S->smem_bytes = (size_t)warp_words * 4 * dev::kWarpsPerCta;
+  // every warp region (Peq tables + queue) lies inside the dynamic allocation
+  S->smem_bytes = (size_t)S->warp_words * 4 * dev::kWarpsPerCta;
+  if (S->queue_off % 4 || S->queue_off + 4 * S->tile_right > S->warp_words ||
+      S->warp_words > cap_warp_words)
+    fail(HBX_ERR_CUDA, "shared-memory layout exceeds its allocation");
   HBX_CUDA(cudaFuncSetAttribute(dev::k_eval, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)S->smem_bytes));
   int bps = 0;
@@ -267,8 +294,7 @@ void setup_session(hbx_session* S) {
   HBX_CUDA(cudaEventCreate(&S->ev_eval1));
   uint64_t h2d = 0;
   for (const SideBufs* sb : {&S->L, &S->R})
-    h2d += sb->bucket.n * 4 + sb->eq.n * 4 + sb->comp.n * 4 + sb->arena.n + sb->soff.n * 4 +
-           sb->slen.n * 4;
+    h2d += sb->bucket.n * 4 + sb->eq.n * 4 + sb->comp.n * 4 + sb->arena.n + sb->meta.n * 16;
   h2d += S->d_rules.n * sizeof(dev::Rule) + S->bound_idx.n * 4;
   S->stats.h2d_bytes = h2d;
   HBX_CUDA(cudaStreamSynchronize(st));
@@ -328,6 +354,8 @@ dev::EvalParams eval_params(hbx_session* S) {
   P.rule_item_base = S->d_rule_base.p;
   P.tile_right = S->tile_right;
   P.warp_words = S->warp_words;
+  P.list_off = S->list_off;
+  P.queue_off = S->queue_off;
   P.out_l = S->out_l.p;
   P.out_r = S->out_r.p;
   P.capacity = S->out_l.n;
@@ -343,10 +371,12 @@ uint32_t enqueue_batched(hbx_session* S, cudaStream_t st) {
   P.item_end = 0;
   P.range_is_device = 1;
   const int grid = S->ctx->n_sm * S->blocks_per_sm;
-  HBX_CUDA(cudaEventRecord(S->ev_eval0, st));
+  // External: inside stream capture a plain record would only be a capture
+  // dependency marker; this makes it an event-record node that can be timed.
+  HBX_CUDA(cudaEventRecordWithFlags(S->ev_eval0, st, cudaEventRecordExternal));
   dev::k_eval<<<grid, kThreads, S->smem_bytes, st>>>(P);
   launch_check("k_eval");
-  HBX_CUDA(cudaEventRecord(S->ev_eval1, st));
+  HBX_CUDA(cudaEventRecordWithFlags(S->ev_eval1, st, cudaEventRecordExternal));
   return launches + 1;
 }
 

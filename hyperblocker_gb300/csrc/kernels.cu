@@ -289,69 +289,6 @@ __device__ __forceinline__ void load_row(const uint32_t* row, uint32_t (&pe)[S])
   }
 }
 
-// Jaro match count m of left string a (Peq table `tab`, la <= 32*W) and right
-// string b: greedy over b's positions i, taking the lowest unmatched position
-// of a inside [i - h, i + h]; that greedy is a maximum matching, the same
-// count the reference's loops produce when min(la, lb) <= 256.
-template <int W>
-__device__ __forceinline__ uint32_t bitpar_m(const uint32_t* __restrict__ tab, uint32_t la,
-                                             const uint8_t* __restrict__ b, uint32_t lb) {
-  constexpr int S = row_words(W);
-  const uint32_t h = (min(la, lb) + 1u) >> 1;
-  const uint32_t n_iter = min(lb, la + h);
-  uint32_t win[W], mt[W];
-#pragma unroll
-  for (int k = 0; k < W; k++) {
-    const int nb = (int)h + 1 - 32 * k;
-    win[k] = nb >= 32 ? 0xffffffffu : (nb <= 0 ? 0u : ((1u << nb) - 1u));
-    mt[k] = 0u;
-  }
-  const uint4* bp = reinterpret_cast<const uint4*>(b);
-  for (uint32_t base = 0; base < n_iter; base += 16) {
-    const uint4 ch = __ldg(bp + (base >> 4));
-    const uint32_t wv[4] = {ch.x, ch.y, ch.z, ch.w};
-#pragma unroll
-    for (int q = 0; q < 4; q++) {
-      if (base + 4u * q >= n_iter) break;
-      const uint32_t wd = wv[q];
-#pragma unroll
-      for (int c = 0; c < 4; c++) {
-        const uint32_t sym = (wd >> (8 * c)) & 0xffu;
-        uint32_t pe[S];
-        load_row<S>(tab + sym * S, pe);
-        uint32_t x[W], n[W];
-#pragma unroll
-        for (int k = 0; k < W; k++) x[k] = pe[k] & win[k] & ~mt[k];
-        Neg<W>::run(x, n);
-#pragma unroll
-        for (int k = 0; k < W; k++) mt[k] |= x[k] & n[k];
-        const uint32_t grow = (base + 4u * q + (uint32_t)c) < h ? 1u : 0u;
-#pragma unroll
-        for (int k = W - 1; k > 0; k--) win[k] = __funnelshift_l(win[k - 1], win[k], 1);
-        win[0] = (win[0] << 1) | grow;
-      }
-    }
-  }
-  uint32_t m = 0;
-#pragma unroll
-  for (int k = 0; k < W; k++) m += __popc(mt[k]);
-  return m;
-}
-
-__device__ __noinline__ uint32_t bitpar_dispatch(uint32_t W, const uint32_t* tab, uint32_t la,
-                                                 const uint8_t* b, uint32_t lb) {
-  switch (W) {
-    case 1: return bitpar_m<1>(tab, la, b, lb);
-    case 2: return bitpar_m<2>(tab, la, b, lb);
-    case 3: return bitpar_m<3>(tab, la, b, lb);
-    case 4: return bitpar_m<4>(tab, la, b, lb);
-    case 5: return bitpar_m<5>(tab, la, b, lb);
-    case 6: return bitpar_m<6>(tab, la, b, lb);
-    case 7: return bitpar_m<7>(tab, la, b, lb);
-    default: return bitpar_m<8>(tab, la, b, lb);
-  }
-}
-
 // The reference's Jaro loops (device_func.cuh:71-111) on symbol strings, with
 // position 256 usable like any other (the reference's uint16_t idx[256] is
 // indexed at 256 there).  Used for pairs whose left string is longer than the
@@ -441,47 +378,51 @@ __device__ __noinline__ bool jw_exact(uint32_t m, uint32_t ls, uint32_t ll, uint
   return !fail_fma;
 }
 
-// Decision from the match count: a float estimate settles every pair whose
-// JW lies farther than kDecisionMargin from the threshold (estimate error is
-// below 2e-6); the rest take the exact path.
-__device__ __forceinline__ bool jw_decide(uint32_t m, uint32_t la, uint32_t lb, const uint8_t* a,
-                                          const uint8_t* b, float thr,
-                                          unsigned long long* ambiguous) {
-  const uint32_t ls = min(la, lb), ll = max(la, lb);
+// Decision from the match count m and the common prefix p: a float estimate
+// settles every pair whose JW lies farther than kDecisionMargin from the
+// threshold (the estimate's error is below 2e-6); the rest take the exact path.
+__device__ __forceinline__ bool jw_decide(uint32_t m, uint32_t ls, uint32_t ll, uint32_t p,
+                                          float thr, unsigned long long* ambiguous) {
   const float fm = (float)m;
   const float ja = m ? (__fdividef(fm, (float)ls) + __fdividef(fm, (float)ll) + 1.0f) * (1.0f / 3.0f)
                      : 0.0f;
-  if (ja >= thr + kDecisionMargin) return true;  // the prefix term is never negative
-  const uint32_t p = m ? prefix_len(a, b, ls) : 0u;
   const float jwa = ja + (1.0f - ja) * (0.1f * (float)p);
   if (jwa >= thr + kDecisionMargin) return true;
   if (jwa < thr - kDecisionMargin) return false;
   return jw_exact(m, ls, ll, p, thr, ambiguous);
 }
 
-// Algorithmic work of one Jaro-Winkler evaluation in 64-bit word operations:
-// 6 per character of the scanned string per 64-bit word of the window string
-// (Peq lookup, window AND, ANDNOT matched, lowest-bit isolate x2, OR), the
-// prefix compare in 32-bit steps, and 16 for the count and the formula.
-__device__ __forceinline__ unsigned long long jw_word_ops(uint32_t la, uint32_t lb) {
-  const uint32_t ls = min(la, lb), ll = max(la, lb);
-  const uint32_t h = (ls + 1u) >> 1;
-  const uint32_t to = min(ls + h, ll);
-  return 6ull * to * ((ls + 63u) >> 6) + 2ull * ((ls + 3u) >> 2) + 16ull;
+// Smallest match count that can still reach the threshold, lowered by a
+// safety margin: every m below the returned value gives JW < thr exactly.
+// JW >= thr needs j >= (thr - c) / (1 - c) with c = 0.1 p, and
+// j = (m/ls + m/ll + 1) / 3.  JW grows with m by at least
+// 0.1 * (1/ls) / 3 >= 1.3e-4 per match (c <= 0.9, shorter length ls <= 256 on
+// the path that uses this), so staying 0.05 matches below the real-valued
+// bound keeps a 6.5e-6 gap, far above the float rounding of j (6e-8) and of
+// this computation (< 3e-4 matches).  p >= 10 reaches 1.0: no bound.  A NaN
+// threshold never fails a pair in the reference, so it gives no bound either.
+__device__ __forceinline__ int m_need_lo(uint32_t ls, uint32_t ll, uint32_t p, float thr) {
+  if (p >= 10u) return 0;
+  const float c = 0.1f * (float)p;
+  const float jn = (thr - c) / (1.0f - c);
+  const float mr = (3.0f * jn - 1.0f) / (1.0f / (float)ls + 1.0f / (float)ll);
+  const float v = ceilf(mr - 0.05f);
+  if (!(v > 0.0f)) return 0;
+  return v > 1.0e6f ? 1000000 : (int)v;
 }
 
 // Slow exact similarity check of one pair (any lengths).
 __device__ __noinline__ bool sim_pass_slow(const Side& L, const Side& R, uint32_t slot_l,
                                            uint32_t slot_r, uint32_t lrow, uint32_t rrow, float thr,
                                            Counters* ctr) {
-  const uint32_t la = L.str_len[(size_t)slot_l * L.n_rows + lrow];
-  const uint32_t lb = R.str_len[(size_t)slot_r * R.n_rows + rrow];
-  const uint8_t* a = L.arena + 16ull * L.str_off[(size_t)slot_l * L.n_rows + lrow];
-  const uint8_t* b = R.arena + 16ull * R.str_off[(size_t)slot_r * R.n_rows + rrow];
+  const uint4 ma = L.str_meta[(size_t)slot_l * L.n_rows + lrow];
+  const uint4 mb = R.str_meta[(size_t)slot_r * R.n_rows + rrow];
+  const uint32_t la = ma.y, lb = mb.y;
+  const uint8_t* a = L.arena + 16ull * ma.x;
+  const uint8_t* b = R.arena + 16ull * mb.x;
   if (la == 0 || lb == 0) return jw_exact(0, la, lb, 0, thr, &ctr->ambiguous);
   const uint32_t mn = min(la, lb);
   if (mn > 256) atomicAdd(&ctr->long_pairs, 1ull);
-  atomicAdd(&ctr->jw_word_ops, jw_word_ops(la, lb));
   const uint32_t m = jaro_m_ref(a, la, b, lb);
   const uint32_t p = prefix_len(a, b, mn);
   return jw_exact(m, mn, max(la, lb), p, thr, &ctr->ambiguous);
@@ -542,11 +483,274 @@ __device__ __forceinline__ uint32_t find_key(const unsigned long long* item_off,
   return lo;
 }
 
-__global__ void __launch_bounds__(kWarpsPerCta * 32) k_eval(EvalParams P) {
+// Algorithmic work of one Jaro-Winkler evaluation in 64-bit word operations:
+// 6 per scanned character per 64-bit word of the Peq string (Peq lookup,
+// window AND, ANDNOT matched, lowest-bit isolate x2, OR), the prefix compare
+// in 32-bit steps and 16 for the count and the formula.
+__device__ __forceinline__ unsigned long long scan_ops(uint32_t scanned, uint32_t ls) {
+  return 6ull * scanned * ((ls + 63u) >> 6) + 2ull * ((ls + 3u) >> 2) + 16ull;
+}
+
+// One character step of the bit-parallel match count: x = the unmatched
+// positions of the left string equal to `sym` inside the window; the lowest
+// one becomes matched; the window [i - h, i + h] moves one position right
+// (and only grows while i < h).
+template <int W, int S>
+__device__ __forceinline__ void bp_step(const uint32_t* __restrict__ tab, uint32_t sym,
+                                        uint32_t (&win)[W], uint32_t (&mt)[W], uint32_t grow) {
+  uint32_t pe[S];
+  load_row<S>(tab + sym * S, pe);
+  uint32_t x[W], n[W];
+#pragma unroll
+  for (int k = 0; k < W; k++) x[k] = pe[k] & win[k] & ~mt[k];
+  Neg<W>::run(x, n);
+#pragma unroll
+  for (int k = 0; k < W; k++) mt[k] |= x[k] & n[k];
+#pragma unroll
+  for (int k = W - 1; k > 0; k--) win[k] = __funnelshift_l(win[k - 1], win[k], 1);
+  win[0] = (win[0] << 1) | grow;
+}
+
+struct Stage {
+  const uint32_t* tab;      // Peq table of the left string (shared memory)
+  const uint8_t* a;         // left string (symbols, 16-byte aligned)
+  uint32_t la;
+  uint32_t a_pre0, a_pre1;  // its first 8 symbols
+  float thr;
+  uint32_t slot_r;          // string slot of the right column
+  const uint32_t* list_g;   // first stage: right rows in global memory, else null
+  uint32_t* list_s;         // later stages read their rows here; survivors go here
+  uint4* q;                 // pairs that need a scan: {row, offset/16, length, p<<16|need}
+  uint32_t n;               // rows in the input list
+  bool last;                // survivors are final matches
+};
+
+// Emits final matches of one warp step with one atomic per warp.
+__device__ __forceinline__ void emit(const EvalParams& P, bool pass, uint32_t lrow, uint32_t rrow,
+                                     int lane) {
+  const unsigned pm = __ballot_sync(kFull, pass);
+  if (!pm) return;
+  unsigned long long base = 0;
+  if (lane == 0) base = atomicAdd(&P.ctr->out_count, (unsigned long long)__popc(pm));
+  base = __shfl_sync(kFull, base, 0);
+  if (pass) {
+    const unsigned long long pos = base + __popc(pm & ((1u << lane) - 1u));
+    if (pos < P.capacity) {
+      P.out_l[pos] = lrow;
+      P.out_r[pos] = rrow;
+    }
+  }
+}
+
+// Passes of one warp step: final (dedup + emit) or into the next stage's list.
+__device__ __forceinline__ void route(const EvalParams& P, const Stage& A, bool pass, uint32_t r,
+                                      uint32_t lrow, uint32_t rrow, int lane, uint32_t* lw) {
+  if (A.last) {
+    if (pass && r > 0) pass = !earlier_rule_matches(P, r, lrow, rrow);
+    emit(P, pass, lrow, rrow, lane);
+  } else {
+    const unsigned pm = __ballot_sync(kFull, pass);
+    if (pass) A.list_s[*lw + __popc(pm & ((1u << lane) - 1u))] = rrow;
+    *lw += __popc(pm);
+  }
+}
+
+// Common prefix of two 8-symbol little-endian prefixes; 8 when they agree.
+__device__ __forceinline__ uint32_t prefix8(uint32_t a0, uint32_t a1, uint32_t b0, uint32_t b1) {
+  uint32_t d = a0 ^ b0;
+  if (d) return (uint32_t)(__ffs(d) - 1) >> 3;
+  d = a1 ^ b1;
+  if (d) return 4u + ((uint32_t)(__ffs(d) - 1) >> 3);
+  return 8u;
+}
+
+constexpr uint32_t kPrefixUnknown = 0xffu;
+
+// Filter pass: one 16-byte metadata load per right row gives its length and
+// first 8 symbols, hence the common prefix p (when below 8) and the match
+// count the threshold needs; rows that cannot reach it are dropped here, the
+// rest are queued for the scan.  Returns the number queued (warp-uniform);
+// *lw counts rows already passed on (empty strings decided here).
+__device__ __noinline__ uint32_t filter_pass(const EvalParams& P, const Stage& A, uint32_t r,
+                                             uint32_t lrow, uint32_t* lw,
+                                             unsigned long long* ops) {
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const uint32_t nR = P.R.n_rows;
+  uint32_t qn = 0;
+  for (uint32_t e0 = 0; e0 < A.n; e0 += 32) {
+    const uint32_t e = e0 + (uint32_t)lane;
+    const bool act = e < A.n;
+    const uint32_t rrow = act ? (A.list_g ? A.list_g[e] : A.list_s[e]) : 0u;
+    const uint4 m = act ? P.R.str_meta[(size_t)A.slot_r * nR + rrow] : make_uint4(0, 0, 0, 0);
+    bool pass = false, scan = false;
+    uint32_t p = 0;
+    int need = 0;
+    if (act) {
+      const uint32_t lb = m.y;
+      if (lb == 0) {
+        pass = jw_exact(0, A.la, 0, 0, A.thr, &P.ctr->ambiguous);
+      } else {
+        const uint32_t ls = min(A.la, lb), ll = max(A.la, lb);
+        const uint32_t p8 = prefix8(A.a_pre0, A.a_pre1, m.z, m.w);
+        if (p8 == 8u && ls > 8u) {
+          scan = true;  // prefix longer than 8: measured exactly before the scan
+          p = kPrefixUnknown;
+        } else {
+          p = min(p8, ls);
+          need = m_need_lo(ls, ll, p, A.thr);
+          const uint32_t n_iter = min(lb, A.la + ((ls + 1u) >> 1));
+          if (need > (int)min(n_iter, ls)) {
+            *ops += scan_ops(0, ls);  // cannot reach the threshold
+          } else {
+            scan = true;
+          }
+        }
+      }
+    }
+    const unsigned qm = __ballot_sync(kFull, scan);
+    if (scan) A.q[qn + __popc(qm & lt)] = make_uint4(rrow, m.x, m.y, (p << 16) | (uint32_t)need);
+    qn += __popc(qm);
+    route(P, A, pass, r, lrow, rrow, lane, lw);
+  }
+  __syncwarp();
+  return qn;
+}
+
+// Scan pass over the queue: lanes take the next queued pair as soon as theirs
+// is decided, so no lane waits for a longer string in a neighbour lane; every
+// loop turn scans one 4-character word for every busy lane.  A pair stops as
+// soon as even matching every remaining character stays below its bound.
+template <int W>
+__device__ __noinline__ void scan_pass(const EvalParams& P, const Stage& A, uint32_t qn, uint32_t r,
+                                       uint32_t lrow, uint32_t* lw, unsigned long long* ops) {
+  constexpr int S = row_words(W);
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  uint32_t next = 0;
+  bool busy = false;
+  uint32_t rrow = 0, ls = 0, ll = 0, i = 0, n_iter = 0, h = 0, p = 0;
+  int allowed = 0;
+  const uint8_t* b = nullptr;
+  uint32_t c0 = 0, c1 = 0, c2 = 0, c3 = 0;
+  uint32_t win[W], mt[W];
+#pragma unroll
+  for (int k = 0; k < W; k++) win[k] = mt[k] = 0u;
+  for (;;) {
+    bool fin = false, pass = false;
+    const unsigned idle = __ballot_sync(kFull, !busy);
+    if (next < qn) {
+      const uint32_t e = next + __popc(idle & lt);
+      next += __popc(idle);
+      if (!busy && e < qn) {
+        const uint4 qe = A.q[e];
+        rrow = qe.x;
+        b = P.R.arena + 16ull * qe.y;
+        const uint32_t lb = qe.z;
+        ls = min(A.la, lb);
+        ll = max(A.la, lb);
+        h = (ls + 1u) >> 1;
+        n_iter = min(lb, A.la + h);
+        p = qe.w >> 16;
+        int need = (int)(qe.w & 0xffffu);
+        if (p == kPrefixUnknown) {
+          p = prefix_len(A.a, b, ls);
+          need = m_need_lo(ls, ll, p, A.thr);
+        }
+        if (need > (int)min(n_iter, ls)) {
+          fin = true;
+          *ops += scan_ops(0, ls);
+        } else {
+          allowed = (int)n_iter - need;
+          i = 0;
+          busy = true;
+#pragma unroll
+          for (int k = 0; k < W; k++) {
+            const int nb = (int)h + 1 - 32 * k;
+            win[k] = nb >= 32 ? 0xffffffffu : (nb <= 0 ? 0u : ((1u << nb) - 1u));
+            mt[k] = 0u;
+          }
+        }
+      }
+    }
+    if (busy) {
+      if ((i & 15u) == 0) {
+        const uint4 v = __ldg(reinterpret_cast<const uint4*>(b + i));
+        c0 = v.x;
+        c1 = v.y;
+        c2 = v.z;
+        c3 = v.w;
+      }
+      const uint32_t wd = c0;
+      c0 = c1;
+      c1 = c2;
+      c2 = c3;
+#pragma unroll
+      for (int c = 0; c < 4; c++)
+        bp_step<W, S>(A.tab, (wd >> (8 * c)) & 0xffu, win, mt, (i + (uint32_t)c) < h ? 1u : 0u);
+      i += 4;
+      if (i >= n_iter || (i & 15u) == 0) {
+        uint32_t m = 0;
+#pragma unroll
+        for (int k = 0; k < W; k++) m += __popc(mt[k]);
+        if (i >= n_iter) {
+          fin = true;
+          busy = false;
+          *ops += scan_ops(n_iter, ls);
+          pass = jw_decide(m, ls, ll, p, A.thr, &P.ctr->ambiguous);
+        } else if ((int)(i - m) > allowed) {
+          fin = true;  // even matching every remaining character stays below
+          busy = false;
+          *ops += scan_ops(i, ls);
+        }
+      }
+    }
+    route(P, A, fin && pass, r, lrow, rrow, lane, lw);
+    if (!__any_sync(kFull, busy) && next >= qn) break;
+  }
+  __syncwarp();
+}
+
+__device__ __forceinline__ void scan_dispatch(uint32_t W, const EvalParams& P, const Stage& A,
+                                              uint32_t qn, uint32_t r, uint32_t lrow, uint32_t* lw,
+                                              unsigned long long* ops) {
+  switch (W) {
+    case 1: scan_pass<1>(P, A, qn, r, lrow, lw, ops); break;
+    case 2: scan_pass<2>(P, A, qn, r, lrow, lw, ops); break;
+    case 3: scan_pass<3>(P, A, qn, r, lrow, lw, ops); break;
+    case 4: scan_pass<4>(P, A, qn, r, lrow, lw, ops); break;
+    case 5: scan_pass<5>(P, A, qn, r, lrow, lw, ops); break;
+    case 6: scan_pass<6>(P, A, qn, r, lrow, lw, ops); break;
+    case 7: scan_pass<7>(P, A, qn, r, lrow, lw, ops); break;
+    default: scan_pass<8>(P, A, qn, r, lrow, lw, ops); break;
+  }
+}
+
+// Stage over a left string the fast path does not take (longer than 256
+// bytes, or no room for its table): the reference's own loops per lane.
+__device__ __noinline__ uint32_t run_stage_slow(const EvalParams& P, const Stage& A, uint32_t s_l,
+                                                uint32_t r, uint32_t lrow) {
+  const int lane = threadIdx.x & 31;
+  uint32_t lw = 0;
+  for (uint32_t e0 = 0; e0 < A.n; e0 += 32) {
+    const uint32_t e = e0 + (uint32_t)lane;
+    const bool act = e < A.n;
+    const uint32_t rrow = act ? (A.list_g ? A.list_g[e] : A.list_s[e]) : 0u;
+    const bool pass = act && sim_pass_slow(P.L, P.R, s_l, A.slot_r, lrow, rrow, A.thr, P.ctr);
+    __syncwarp();
+    route(P, A, pass, r, lrow, rrow, lane, &lw);
+  }
+  __syncwarp();
+  return lw;
+}
+
+__global__ void __launch_bounds__(kWarpsPerCta * 32, 3) k_eval(EvalParams P) {
   extern __shared__ __align__(16) uint32_t smem[];
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   uint32_t* region = smem + (size_t)warp * P.warp_words;
+  uint32_t* list_s = region + P.list_off;
+  uint4* q = reinterpret_cast<uint4*>(region + P.queue_off);
   const unsigned long long end = P.range_is_device ? P.rule_item_base[P.n_rules] : P.item_end;
   const long long t_start = clock64();
   // warp-level cache of the last (rule, key) item range
@@ -583,53 +787,47 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_eval(EvalParams P) {
     const uint32_t rb0 = R.off_r[key] + ri * P.tile_right;
     const uint32_t rb1 = min(rb0 + P.tile_right, R.off_r[key] + nr);
 
-    uint32_t built = 0;
-    for (uint32_t rb = rb0; rb < rb1; rb += 32) {
-      const uint32_t idx = rb + (uint32_t)lane;
-      const bool act = idx < rb1;
-      const uint32_t rrow = act ? R.sorted_r[idx] : 0u;
-      bool pass = act;
-      for (uint32_t s = 0; s < R.n_sim; s++) {
-        if (!__ballot_sync(kFull, pass)) break;
-        const uint32_t sl = R.sim_l[s], sr = R.sim_r[s];
-        const uint32_t la = P.L.str_len[(size_t)sl * P.L.n_rows + lrow];
-        const uint8_t* a = P.L.arena + 16ull * P.L.str_off[(size_t)sl * P.L.n_rows + lrow];
-        const uint32_t W = (la + 31u) >> 5;
-        const bool fast = la > 0 && la <= 256 && R.peq_rows_words[s] >= (uint32_t)row_words((int)W);
-        uint32_t* tab = region + R.peq_off[s];
-        if (fast && !((built >> s) & 1u)) {
-          build_peq(tab, (uint32_t)row_words((int)W), P.n_symbols, a, la, lane);
-          built |= 1u << s;
-        }
-        if (pass) {
-          if (fast) {
-            const uint32_t lb = P.R.str_len[(size_t)sr * P.R.n_rows + rrow];
-            const uint8_t* b = P.R.arena + 16ull * P.R.str_off[(size_t)sr * P.R.n_rows + rrow];
-            if (lb == 0) {
-              pass = jw_exact(0, la, 0, 0, R.thr[s], &P.ctr->ambiguous);
-            } else {
-              const uint32_t m = bitpar_dispatch(W, tab, la, b, lb);
-              ops += jw_word_ops(la, lb);
-              pass = jw_decide(m, la, lb, a, b, R.thr[s], &P.ctr->ambiguous);
-            }
-          } else {
-            pass = sim_pass_slow(P.L, P.R, sl, sr, lrow, rrow, R.thr[s], P.ctr);
-          }
-        }
+    if (R.n_sim == 0) {  // equalities only: every candidate matches
+      for (uint32_t rb = rb0; rb < rb1; rb += 32) {
+        const uint32_t idx = rb + (uint32_t)lane;
+        const uint32_t rrow = idx < rb1 ? R.sorted_r[idx] : 0u;
+        bool pass = idx < rb1;
+        if (pass && r > 0) pass = !earlier_rule_matches(P, r, lrow, rrow);
+        emit(P, pass, lrow, rrow, lane);
       }
-      if (pass && r > 0) pass = !earlier_rule_matches(P, r, lrow, rrow);
-      const unsigned mask = __ballot_sync(kFull, pass);
-      if (mask) {
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(&P.ctr->out_count, (unsigned long long)__popc(mask));
-        base = __shfl_sync(kFull, base, 0);
-        if (pass) {
-          const unsigned long long pos = base + __popc(mask & ((1u << lane) - 1u));
-          if (pos < P.capacity) {
-            P.out_l[pos] = lrow;
-            P.out_r[pos] = rrow;
+    } else {
+      Stage A;
+      A.list_g = R.sorted_r + rb0;
+      A.list_s = list_s;
+      A.q = q;
+      A.n = rb1 - rb0;
+      for (uint32_t s = 0; s < R.n_sim && A.n > 0; s++) {
+        const uint32_t sl = R.sim_l[s];
+        const uint4 am = P.L.str_meta[(size_t)sl * P.L.n_rows + lrow];
+        A.la = am.y;
+        A.a = P.L.arena + 16ull * am.x;
+        A.a_pre0 = am.z;
+        A.a_pre1 = am.w;
+        A.thr = R.thr[s];
+        A.slot_r = R.sim_r[s];
+        A.last = s + 1 == R.n_sim;
+        const uint32_t W = (A.la + 31u) >> 5;
+        const bool fast =
+            A.la > 0 && A.la <= 256 && R.peq_rows_words[s] >= (uint32_t)row_words((int)W);
+        uint32_t lw = 0;
+        if (fast) {
+          const uint32_t qn = filter_pass(P, A, r, lrow, &lw, &ops);
+          if (qn) {
+            uint32_t* tab = region + R.peq_off[s];
+            build_peq(tab, (uint32_t)row_words((int)W), P.n_symbols, A.a, A.la, lane);
+            A.tab = tab;
+            scan_dispatch(W, P, A, qn, r, lrow, &lw, &ops);
           }
+        } else {
+          lw = run_stage_slow(P, A, sl, r, lrow);
         }
+        A.list_g = nullptr;
+        A.n = lw;
       }
     }
     done++;

@@ -11,9 +11,12 @@
 //                     L_key x R_key.
 //   4. k_eval         persistent, warp-granular work stealing over the items
 //                     of every rule: the warp's left string becomes a Peq
-//                     bitmask table in shared memory (built with __match_any),
-//                     each lane runs bit-parallel Jaro over one right string,
-//                     Jaro-Winkler is decided exactly, survivors leave by
+//                     bitmask table in shared memory (built with __match_any);
+//                     a rule's similarity predicates run as stages over a
+//                     shared-memory queue of survivors; inside a stage lanes
+//                     take the next right row as soon as theirs is decided
+//                     (bit-parallel Jaro, exact early-fail bound), so lanes do
+//                     not wait on longer strings; matches leave by
 //                     warp-aggregated atomics.
 //
 // Semantics reproduced (reference = HyperBlocker):
@@ -48,8 +51,9 @@ struct Side {
   const int32_t* eq_codes;    // [n_eq_slots][n_rows]
   const int32_t* comp_codes;  // [n_comp][n_rows]
   const uint8_t* arena;       // symbol strings, 16-byte aligned, zero padded
-  const uint32_t* str_off;    // [n_str_slots][n_rows], units of 16 bytes
-  const uint32_t* str_len;    // [n_str_slots][n_rows]
+  // [n_str_slots][n_rows]: {offset / 16, length, symbols 0-3, symbols 4-7}
+  // (symbols past the end of the string are 0)
+  const uint4* str_meta;
   uint32_t n_rows;
 };
 
@@ -98,7 +102,9 @@ struct EvalParams {
   unsigned long long item_end;
   int range_is_device;  // 1: item_end = rule_item_base[n_rules] (read on device)
   uint32_t tile_right;  // TR
-  uint32_t warp_words;  // shared-memory words per warp
+  uint32_t warp_words;  // shared-memory words per warp: Peq tables, row list, scan queue
+  uint32_t list_off;    // word offset of the warp's row list (tile_right words)
+  uint32_t queue_off;   // word offset of the warp's scan queue (tile_right x uint4)
   uint32_t* out_l;
   uint32_t* out_r;
   unsigned long long capacity;
