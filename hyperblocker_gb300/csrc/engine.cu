@@ -86,7 +86,8 @@ struct RuleBufs {
   DBuf<unsigned long long> item_off;
   DBuf<uint32_t> part_u32;
   DBuf<unsigned long long> part_u64;
-  uint32_t nb = 0;  // scan CTAs over the key domain
+  uint32_t nb = 0;    // scan CTAs over the join key domain
+  uint32_t nb_l = 0;  // scan CTAs over the left key domain (word classes x keys)
 };
 
 struct SideBufs {
@@ -116,6 +117,7 @@ struct hbx_session {
   hbx::DBuf<unsigned long long> d_rule_base;
   hbx::DBuf<hbx::dev::Counters> d_ctr;
   hbx::DBuf<uint32_t> out_l, out_r;
+  hbx::DBuf<unsigned long long> seen;  // reported-pair set (plans with several rules)
   hbx::DBuf<uint32_t> bound_idx;              // per rule, n_partitions + 1 key indices
   hbx::DBuf<unsigned long long> bound_val;    // item_off at those keys
   hbx::dev::Side side_l{}, side_r{};
@@ -196,9 +198,9 @@ void setup_session(hbx_session* S) {
   if (C->opts.tile_right > 0) S->tile_right = (uint32_t)C->opts.tile_right;
   S->tile_right = std::min<uint32_t>(2048, std::max<uint32_t>(32, (S->tile_right + 31) / 32 * 32));
   const uint32_t cap_warp_words = (uint32_t)(smem_cap / 4 / dev::kWarpsPerCta) / 4 * 4;
-  // per warp: Peq tables, then a row list (tile_right words) and a scan queue
-  // (tile_right x 16 bytes)
-  const uint32_t list_queue_words = 5 * S->tile_right;
+  // per warp: Peq tables, then a row list (tile_right words) and the scan
+  // ring (kRingEntries x 16 bytes)
+  const uint32_t list_queue_words = S->tile_right + 4 * dev::kRingEntries;
   if (list_queue_words + 4 > cap_warp_words) fail(HBX_ERR_INVALID_ARG, "tile_right too large");
   const uint32_t max_warp_words = cap_warp_words - list_queue_words;
   uint32_t warp_words = 4;
@@ -235,21 +237,29 @@ void setup_session(hbx_session* S) {
     }
     warp_words = std::max(warp_words, off);
     d.domain = (uint32_t)re.domain;
+    // group left rows by the word class of the first similarity predicate's
+    // string, unless that would make the left key domain too large
+    const bool split = !re.sim_slot_l.empty() &&
+                       re.domain * dev::kWordClasses <= (uint64_t)kMaxKeyDomain * 4;
+    d.n_wclass = split ? dev::kWordClasses : 1u;
+    d.wclass_slot = split ? (uint32_t)re.sim_slot_l[0] : 0u;
+    d.domain_l = d.n_wclass * d.domain;
     RuleBufs& b = S->rb[r];
     b.key_l.alloc(nL);
     b.key_r.alloc(nR);
-    b.cnt_l.alloc(re.domain);
+    b.cnt_l.alloc(d.domain_l);
     b.cnt_r.alloc(re.domain);
-    b.off_l.alloc(re.domain);
+    b.off_l.alloc(d.domain_l);
     b.off_r.alloc(re.domain);
-    b.cur_l.alloc(re.domain);
+    b.cur_l.alloc(d.domain_l);
     b.cur_r.alloc(re.domain);
     b.sorted_l.alloc(nL);
     b.sorted_r.alloc(nR);
-    b.item_off.alloc(re.domain + 1);
+    b.item_off.alloc((size_t)d.domain_l + 1);
     b.nb = (uint32_t)((re.domain + dev::kScanChunk - 1) / dev::kScanChunk);
-    b.part_u32.alloc(b.nb);
-    b.part_u64.alloc(b.nb);
+    b.nb_l = (uint32_t)((d.domain_l + dev::kScanChunk - 1) / dev::kScanChunk);
+    b.part_u32.alloc(std::max(b.nb, b.nb_l));
+    b.part_u64.alloc(b.nb_l);
     d.key_l = b.key_l.p;
     d.key_r = b.key_r.p;
     d.cnt_l = b.cnt_l.p;
@@ -262,16 +272,16 @@ void setup_session(hbx_session* S) {
     d.sorted_l = b.sorted_l.p;
     d.sorted_r = b.sorted_r.p;
   }
-  // each warp's row list and scan queue follow its Peq tables
+  // each warp's row list and scan ring follow its Peq tables
   S->list_off = warp_words;
   S->queue_off = warp_words + S->tile_right;
-  S->warp_words = S->queue_off + 4 * S->tile_right;
+  S->warp_words = S->queue_off + 4 * dev::kRingEntries;
   S->d_rules.upload(S->h_rules, st);
   S->d_rule_base.alloc(E.rules.size() + 1);
   S->d_ctr.alloc(1);
   // every warp region (Peq tables + queue) lies inside the dynamic allocation
   S->smem_bytes = (size_t)S->warp_words * 4 * dev::kWarpsPerCta;
-  if (S->queue_off % 4 || S->queue_off + 4 * S->tile_right > S->warp_words ||
+  if (S->queue_off % 4 || S->queue_off + 4 * dev::kRingEntries > S->warp_words ||
       S->warp_words > cap_warp_words)
     fail(HBX_ERR_CUDA, "shared-memory layout exceeds its allocation");
   HBX_CUDA(cudaFuncSetAttribute(dev::k_eval, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -280,14 +290,20 @@ void setup_session(hbx_session* S) {
   HBX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, dev::k_eval, kThreads, S->smem_bytes));
   S->blocks_per_sm = std::max(1, bps);
 
-  // partition boundaries of every rule's key space (plain form)
+  // partition boundaries of every rule's left key space, per word class
+  // (plain form): entry (rule, class, p) = first left key of partition p
   std::vector<uint32_t> idx;
-  for (auto& re : E.rules)
-    for (uint64_t p = 0; p <= E.n_partitions; p++) idx.push_back((uint32_t)re.part_key_begin[p]);
+  for (size_t r = 0; r < E.rules.size(); r++)
+    for (uint32_t c = 0; c < dev::kWordClasses; c++)
+      for (uint64_t p = 0; p <= E.n_partitions; p++) {
+        const uint32_t cc = std::min<uint32_t>(c, S->h_rules[r].n_wclass - 1);
+        idx.push_back(cc * S->h_rules[r].domain + (uint32_t)E.rules[r].part_key_begin[p]);
+      }
   S->bound_idx.upload(idx, st);
   S->bound_val.alloc(idx.size());
   S->out_l.alloc(1 << 16);
   S->out_r.alloc(1 << 16);
+  if (E.rules.size() > 1) S->seen.alloc(1 << 17);
   HBX_CUDA(cudaEventCreate(&S->ev0));
   HBX_CUDA(cudaEventCreate(&S->ev1));
   HBX_CUDA(cudaEventCreate(&S->ev_eval0));
@@ -313,27 +329,30 @@ __global__ void k_gather_bounds(const dev::Rule* rules, uint32_t n_rules, uint32
 uint32_t enqueue_join(hbx_session* S, cudaStream_t st) {
   uint32_t launches = 0;
   HBX_CUDA(cudaMemsetAsync(S->d_ctr.p, 0, sizeof(dev::Counters), st));
+  if (S->seen.p) HBX_CUDA(cudaMemsetAsync(S->seen.p, 0xff, S->seen.n * sizeof(unsigned long long), st));
   const uint32_t nL = S->side_l.n_rows, nR = S->side_r.n_rows;
   const int n_sm = S->ctx->n_sm;
   for (size_t r = 0; r < S->rb.size(); r++) {
     RuleBufs& b = S->rb[r];
     const uint32_t D = S->h_rules[r].domain;
-    HBX_CUDA(cudaMemsetAsync(b.cnt_l.p, 0, D * sizeof(uint32_t), st));
+    const uint32_t DL = S->h_rules[r].domain_l;
+    HBX_CUDA(cudaMemsetAsync(b.cnt_l.p, 0, DL * sizeof(uint32_t), st));
     HBX_CUDA(cudaMemsetAsync(b.cnt_r.p, 0, D * sizeof(uint32_t), st));
-    HBX_CUDA(cudaMemsetAsync(b.cur_l.p, 0, D * sizeof(uint32_t), st));
+    HBX_CUDA(cudaMemsetAsync(b.cur_l.p, 0, DL * sizeof(uint32_t), st));
     HBX_CUDA(cudaMemsetAsync(b.cur_r.p, 0, D * sizeof(uint32_t), st));
     if (nL) dev::k_keys_hist<<<row_grid(nL, n_sm), 256, 0, st>>>(S->side_l, S->d_rules.p, (uint32_t)r, 0);
     if (nR) dev::k_keys_hist<<<row_grid(nR, n_sm), 256, 0, st>>>(S->side_r, S->d_rules.p, (uint32_t)r, 1);
-    dev::k_scan_partial_u32<<<b.nb, 1024, 0, st>>>(b.cnt_l.p, D, b.part_u32.p);
-    dev::k_scan_top_u32<<<1, 1024, 0, st>>>(b.part_u32.p, b.nb);
-    dev::k_scan_final_u32<<<b.nb, 1024, 0, st>>>(b.cnt_l.p, D, b.part_u32.p, b.off_l.p);
+    dev::k_scan_partial_u32<<<b.nb_l, 1024, 0, st>>>(b.cnt_l.p, DL, b.part_u32.p);
+    dev::k_scan_top_u32<<<1, 1024, 0, st>>>(b.part_u32.p, b.nb_l);
+    dev::k_scan_final_u32<<<b.nb_l, 1024, 0, st>>>(b.cnt_l.p, DL, b.part_u32.p, b.off_l.p);
     dev::k_scan_partial_u32<<<b.nb, 1024, 0, st>>>(b.cnt_r.p, D, b.part_u32.p);
     dev::k_scan_top_u32<<<1, 1024, 0, st>>>(b.part_u32.p, b.nb);
     dev::k_scan_final_u32<<<b.nb, 1024, 0, st>>>(b.cnt_r.p, D, b.part_u32.p, b.off_r.p);
-    dev::k_items_partial<<<b.nb, 1024, 0, st>>>(S->d_rules.p, (uint32_t)r, S->tile_right,
-                                                b.part_u64.p, &S->d_ctr.p->comparisons);
-    dev::k_scan_top_u64<<<1, 1024, 0, st>>>(b.part_u64.p, b.nb);
-    dev::k_items_final<<<b.nb, 1024, 0, st>>>(S->d_rules.p, (uint32_t)r, S->tile_right, b.part_u64.p);
+    dev::k_items_partial<<<b.nb_l, 1024, 0, st>>>(S->d_rules.p, (uint32_t)r, S->tile_right,
+                                                  b.part_u64.p, &S->d_ctr.p->comparisons);
+    dev::k_scan_top_u64<<<1, 1024, 0, st>>>(b.part_u64.p, b.nb_l);
+    dev::k_items_final<<<b.nb_l, 1024, 0, st>>>(S->d_rules.p, (uint32_t)r, S->tile_right,
+                                                b.part_u64.p);
     if (nL) dev::k_scatter<<<row_grid(nL, n_sm), 256, 0, st>>>(S->side_l, S->d_rules.p, (uint32_t)r, 0);
     if (nR) dev::k_scatter<<<row_grid(nR, n_sm), 256, 0, st>>>(S->side_r, S->d_rules.p, (uint32_t)r, 1);
     launches += 9 + (nL ? 2 : 0) + (nR ? 2 : 0);
@@ -361,15 +380,15 @@ dev::EvalParams eval_params(hbx_session* S) {
   P.capacity = S->out_l.n;
   P.ctr = S->d_ctr.p;
   P.watchdog_cycles = S->ctx->opts.watchdog_cycles;
+  P.seen = S->seen.p;
+  P.seen_mask = S->seen.p ? S->seen.n - 1 : 0;
   return P;
 }
 
 uint32_t enqueue_batched(hbx_session* S, cudaStream_t st) {
   uint32_t launches = enqueue_join(S, st);
   dev::EvalParams P = eval_params(S);
-  P.item_begin = 0;
-  P.item_end = 0;
-  P.range_is_device = 1;
+  P.n_seg = 0;  // every work item of every rule
   const int grid = S->ctx->n_sm * S->blocks_per_sm;
   // External: inside stream capture a plain record would only be a capture
   // dependency marker; this makes it an event-record node that can be timed.
@@ -385,6 +404,11 @@ void grow_output(hbx_session* S, uint64_t need) {
   while (cap < need) cap *= 2;
   S->out_l.alloc(cap);
   S->out_r.alloc(cap);
+  if (S->seen.p) {
+    uint64_t slots = S->seen.n;
+    while (slots < 2 * cap) slots *= 2;  // load factor stays at or below one half
+    if (slots != S->seen.n) S->seen.alloc(slots);
+  }
   if (S->graph) {
     cudaGraphExecDestroy(S->graph);
     S->graph = nullptr;
@@ -430,7 +454,8 @@ dev::Counters run_once(hbx_session* S, hbx_mode mode, cudaStream_t st, uint32_t*
   // PLAIN: join, then one launch per (partition, rule)
   uint32_t n = enqueue_join(S, st);
   const uint32_t n_rules = (uint32_t)S->rb.size();
-  const uint32_t per_rule = (uint32_t)S->E.n_partitions + 1;
+  const uint32_t per_class = (uint32_t)S->E.n_partitions + 1;
+  const uint32_t per_rule = per_class * dev::kWordClasses;
   const uint32_t total = n_rules * per_rule;
   k_gather_bounds<<<(total + 255) / 256, 256, 0, st>>>(S->d_rules.p, n_rules, per_rule,
                                                        S->bound_idx.p, S->bound_val.p);
@@ -443,18 +468,25 @@ dev::Counters run_once(hbx_session* S, hbx_mode mode, cudaStream_t st, uint32_t*
                            cudaMemcpyDeviceToHost, st));
   HBX_CUDA(cudaStreamSynchronize(st));
   dev::EvalParams P = eval_params(S);
-  P.range_is_device = 0;
   const int max_grid = S->ctx->n_sm * S->blocks_per_sm;
   HBX_CUDA(cudaEventRecord(S->ev_eval0, st));
   for (uint64_t p = 0; p < S->E.n_partitions; p++) {
     for (uint32_t r = 0; r < n_rules; r++) {
-      const unsigned long long b0 = base[r] + bounds[(size_t)r * per_rule + p];
-      const unsigned long long b1 = base[r] + bounds[(size_t)r * per_rule + p + 1];
-      if (b1 <= b0) continue;
-      P.item_begin = b0;
-      P.item_end = b1;
+      // the partition's items: one range per word class
+      P.n_seg = 0;
+      unsigned long long n_items = 0;
+      for (uint32_t c = 0; c < S->h_rules[r].n_wclass; c++) {
+        const size_t k = (size_t)r * per_rule + (size_t)c * per_class + p;
+        const unsigned long long b0 = base[r] + bounds[k], b1 = base[r] + bounds[k + 1];
+        if (b1 <= b0) continue;
+        P.seg_begin[P.n_seg] = b0;
+        P.seg_end[P.n_seg] = b1;
+        P.n_seg++;
+        n_items += b1 - b0;
+      }
+      if (!n_items) continue;
       HBX_CUDA(cudaMemsetAsync(&S->d_ctr.p->work_next, 0, sizeof(unsigned long long), st));
-      const unsigned long long ctas = (b1 - b0 + dev::kWarpsPerCta - 1) / dev::kWarpsPerCta;
+      const unsigned long long ctas = (n_items + dev::kWarpsPerCta - 1) / dev::kWarpsPerCta;
       const int grid = (int)std::min<unsigned long long>(ctas, (unsigned long long)max_grid);
       dev::k_eval<<<grid, kThreads, S->smem_bytes, st>>>(P);
       n++;
@@ -499,8 +531,8 @@ void session_run(hbx_session* S, hbx_mode mode, cudaStream_t st) {
     if (c.items_done != total_items)
       fail(HBX_ERR_CUDA, "evaluation finished " + std::to_string(c.items_done) + " of " +
                              std::to_string(total_items) + " work items");
-    if (c.out_count <= S->out_l.n) return;
-    grow_output(S, c.out_count);
+    if (c.out_count <= S->out_l.n && c.seen_overflow == 0) return;
+    grow_output(S, std::max<uint64_t>(c.out_count + c.seen_overflow, S->out_l.n + 1));
   }
   fail(HBX_ERR_CAPACITY, "output kept growing");
 }

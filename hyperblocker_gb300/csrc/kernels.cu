@@ -22,9 +22,11 @@ __global__ void k_keys_hist(Side S, const Rule* rules, uint32_t rule, int side) 
   const Rule& R = rules[rule];
   uint32_t* keys = side ? R.key_r : R.key_l;
   uint32_t* cnt = side ? R.cnt_r : R.cnt_l;
+  const bool split = !side && R.n_wclass > 1;
   for (uint32_t row = blockIdx.x * blockDim.x + threadIdx.x; row < S.n_rows;
        row += gridDim.x * blockDim.x) {
-    const uint32_t k = row_key(S, R, row);
+    uint32_t k = row_key(S, R, row);
+    if (split) k += R.domain * word_class(S.str_meta[(size_t)R.wclass_slot * S.n_rows + row].y);
     keys[row] = k;
     atomicAdd(cnt + k, 1u);
   }
@@ -121,10 +123,11 @@ __global__ void k_scan_final_u32(const uint32_t* in, uint32_t n, const uint32_t*
   }
 }
 
-__device__ __forceinline__ unsigned long long key_items(const Rule& R, uint32_t key,
+// Work items of left key j (word class j / D, join key j % D).
+__device__ __forceinline__ unsigned long long key_items(const Rule& R, uint32_t j,
                                                         uint32_t tile_right,
                                                         unsigned long long* pairs) {
-  const uint32_t nl = R.cnt_l[key], nr = R.cnt_r[key];
+  const uint32_t nl = R.cnt_l[j], nr = R.cnt_r[j % R.domain];
   *pairs = (unsigned long long)nl * nr;
   if (!nl || !nr) return 0;
   return (unsigned long long)nl * ((nr + tile_right - 1) / tile_right);
@@ -138,7 +141,7 @@ __global__ void k_items_partial(const Rule* rules, uint32_t rule, uint32_t tile_
   const uint64_t base = (uint64_t)blockIdx.x * kScanChunk + threadIdx.x * 4u;
   unsigned long long v = 0, pr = 0;
   for (int k = 0; k < 4; k++)
-    if (base + k < R.domain) {
+    if (base + k < R.domain_l) {
       unsigned long long p;
       v += key_items(R, (uint32_t)(base + k), tile_right, &p);
       pr += p;
@@ -158,15 +161,15 @@ __global__ void k_items_final(const Rule* rules, uint32_t rule, uint32_t tile_ri
   const uint64_t base = (uint64_t)blockIdx.x * kScanChunk + threadIdx.x * 4u;
   unsigned long long v[4], sum = 0, p;
   for (int k = 0; k < 4; k++) {
-    v[k] = (base + k < R.domain) ? key_items(R, (uint32_t)(base + k), tile_right, &p) : 0ull;
+    v[k] = (base + k < R.domain_l) ? key_items(R, (uint32_t)(base + k), tile_right, &p) : 0ull;
     sum += v[k];
   }
   unsigned long long ex =
       block_excl_scan<unsigned long long>(sum, s_warp, &s_total) + partial[blockIdx.x];
   for (int k = 0; k < 4; k++) {
-    if (base + k < R.domain) R.item_off[base + k] = ex;
+    if (base + k < R.domain_l) R.item_off[base + k] = ex;
     ex += v[k];
-    if (base + k + 1 == R.domain) R.item_off[R.domain] = ex;
+    if (base + k + 1 == R.domain_l) R.item_off[R.domain_l] = ex;
   }
 }
 
@@ -175,7 +178,7 @@ __global__ void k_rule_base(const Rule* rules, uint32_t n_rules, unsigned long l
     unsigned long long acc = 0;
     for (uint32_t r = 0; r < n_rules; r++) {
       base[r] = acc;
-      acc += rules[r].item_off[rules[r].domain];
+      acc += rules[r].item_off[rules[r].domain_l];
     }
     base[n_rules] = acc;
   }
@@ -428,30 +431,6 @@ __device__ __noinline__ bool sim_pass_slow(const Side& L, const Side& R, uint32_
   return jw_exact(m, mn, max(la, lb), p, thr, &ctr->ambiguous);
 }
 
-// Does an earlier rule (index < r) also match (lrow, rrow)?  Then that rule
-// reports the pair, and this one must not report it again.
-__device__ __noinline__ bool earlier_rule_matches(const EvalParams& P, uint32_t r, uint32_t lrow,
-                                                  uint32_t rrow) {
-  for (uint32_t j = 0; j < r; j++) {
-    const Rule& Q = P.rules[j];
-    bool eq = true;
-    if (Q.composite) {
-      eq = P.L.comp_codes[(size_t)Q.comp_index * P.L.n_rows + lrow] ==
-           P.R.comp_codes[(size_t)Q.comp_index * P.R.n_rows + rrow];
-    } else {
-      for (uint32_t e = 0; e < Q.n_eq && eq; e++)
-        eq = P.L.eq_codes[(size_t)Q.eq_slot[e] * P.L.n_rows + lrow] ==
-             P.R.eq_codes[(size_t)Q.eq_slot[e] * P.R.n_rows + rrow];
-    }
-    if (!eq) continue;
-    bool all = true;
-    for (uint32_t s = 0; s < Q.n_sim && all; s++)
-      all = sim_pass_slow(P.L, P.R, Q.sim_l[s], Q.sim_r[s], lrow, rrow, Q.thr[s], P.ctr);
-    if (all) return true;
-  }
-  return false;
-}
-
 // Peq table of the warp's left string: row `sym` (stride S words) has bit j of
 // word k set when a[32k + j] == sym.  Built with __match_any_sync: lanes that
 // hold the same symbol agree on the mask, the lowest of them stores it.
@@ -483,12 +462,17 @@ __device__ __forceinline__ uint32_t find_key(const unsigned long long* item_off,
   return lo;
 }
 
-// Algorithmic work of one Jaro-Winkler evaluation in 64-bit word operations:
-// 6 per scanned character per 64-bit word of the Peq string (Peq lookup,
-// window AND, ANDNOT matched, lowest-bit isolate x2, OR), the prefix compare
-// in 32-bit steps and 16 for the count and the formula.
-__device__ __forceinline__ unsigned long long scan_ops(uint32_t scanned, uint32_t ls) {
-  return 6ull * scanned * ((ls + 63u) >> 6) + 2ull * ((ls + 3u) >> 2) + 16ull;
+// Algorithmic work of one Jaro-Winkler evaluation (one pair, one similarity
+// predicate) in 64-bit word operations, the per-unit figure the roofline uses:
+// 6 per scanned character per 64-bit word of the shorter string (Peq lookup,
+// window AND, ANDNOT matched, lowest-bit isolate x2, OR) over
+// to = min(ls + h, ll) characters, the prefix compare in 32-bit steps and 16
+// for the count and the formula.  It is counted for every evaluation, also
+// for pairs the bound settles without a scan.
+__device__ __forceinline__ unsigned long long jw_eval_ops(uint32_t ls, uint32_t ll) {
+  const uint32_t h = (ls + 1u) >> 1;
+  const uint32_t to = min(ls + h, ll);
+  return 6ull * to * ((ls + 63u) >> 6) + 2ull * ((ls + 3u) >> 2) + 16ull;
 }
 
 // One character step of the bit-parallel match count: x = the unmatched
@@ -520,14 +504,36 @@ struct Stage {
   uint32_t slot_r;          // string slot of the right column
   const uint32_t* list_g;   // first stage: right rows in global memory, else null
   uint32_t* list_s;         // later stages read their rows here; survivors go here
-  uint4* q;                 // pairs that need a scan: {row, offset/16, length, p<<16|need}
+  uint4* q;                 // ring (kRing) of pairs to scan: {row, offset/16, length, p<<16|need}
   uint32_t n;               // rows in the input list
   bool last;                // survivors are final matches
 };
 
 // Emits final matches of one warp step with one atomic per warp.
+// First report of a pair?  With several rules a pair can match more than one
+// of them (the reference stops at the first rule that passes,
+// global_func.cuh:161-165); a device hash set of emitted (left, right) keys
+// keeps exactly one report.  Open addressing with linear probing over
+// seen_mask + 1 slots (all ones = empty); if the probe runs past its limit the
+// set is too small: the pair is counted in seen_overflow and the host reruns
+// with a larger set.
+__device__ __forceinline__ bool first_report(const EvalParams& P, uint32_t lrow, uint32_t rrow) {
+  const unsigned long long key = ((unsigned long long)lrow << 32) | rrow;
+  unsigned long long h = key * 0x9E3779B97F4A7C15ull;
+  h ^= h >> 29;
+  for (unsigned long long probe = 0; probe <= P.seen_mask; probe++) {
+    const unsigned long long slot = (h + probe) & P.seen_mask;
+    const unsigned long long prev = atomicCAS(P.seen + slot, ~0ull, key);
+    if (prev == ~0ull) return true;
+    if (prev == key) return false;
+  }
+  atomicAdd(&P.ctr->seen_overflow, 1ull);
+  return false;
+}
+
 __device__ __forceinline__ void emit(const EvalParams& P, bool pass, uint32_t lrow, uint32_t rrow,
                                      int lane) {
+  if (pass && P.seen) pass = first_report(P, lrow, rrow);
   const unsigned pm = __ballot_sync(kFull, pass);
   if (!pm) return;
   unsigned long long base = 0;
@@ -546,7 +552,6 @@ __device__ __forceinline__ void emit(const EvalParams& P, bool pass, uint32_t lr
 __device__ __forceinline__ void route(const EvalParams& P, const Stage& A, bool pass, uint32_t r,
                                       uint32_t lrow, uint32_t rrow, int lane, uint32_t* lw) {
   if (A.last) {
-    if (pass && r > 0) pass = !earlier_rule_matches(P, r, lrow, rrow);
     emit(P, pass, lrow, rrow, lane);
   } else {
     const unsigned pm = __ballot_sync(kFull, pass);
@@ -565,69 +570,67 @@ __device__ __forceinline__ uint32_t prefix8(uint32_t a0, uint32_t a1, uint32_t b
 }
 
 constexpr uint32_t kPrefixUnknown = 0xffu;
+constexpr uint32_t kRing = kRingEntries;  // per-warp ring of pairs waiting for a scan
 
-// Filter pass: one 16-byte metadata load per right row gives its length and
-// first 8 symbols, hence the common prefix p (when below 8) and the match
-// count the threshold needs; rows that cannot reach it are dropped here, the
-// rest are queued for the scan.  Returns the number queued (warp-uniform);
-// *lw counts rows already passed on (empty strings decided here).
-__device__ __noinline__ uint32_t filter_pass(const EvalParams& P, const Stage& A, uint32_t r,
-                                             uint32_t lrow, uint32_t* lw,
-                                             unsigned long long* ops) {
+// Filter one batch of 32 input rows: one 16-byte metadata load per right row
+// gives its length and first 8 symbols, hence the common prefix p (when below
+// 8) and the match count the threshold needs; rows that cannot reach it are
+// decided here, the rest are appended to the ring of pairs to scan.
+// Empty right strings are decided here too.  Returns the rows appended.
+__device__ __forceinline__ uint32_t filter_batch(const EvalParams& P, const Stage& A, uint32_t e0,
+                                                 uint32_t tail, uint32_t r, uint32_t lrow,
+                                                 uint32_t* lw, unsigned long long* ops) {
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
   const uint32_t nR = P.R.n_rows;
-  uint32_t qn = 0;
-  for (uint32_t e0 = 0; e0 < A.n; e0 += 32) {
-    const uint32_t e = e0 + (uint32_t)lane;
-    const bool act = e < A.n;
-    const uint32_t rrow = act ? (A.list_g ? A.list_g[e] : A.list_s[e]) : 0u;
-    const uint4 m = act ? P.R.str_meta[(size_t)A.slot_r * nR + rrow] : make_uint4(0, 0, 0, 0);
-    bool pass = false, scan = false;
-    uint32_t p = 0;
-    int need = 0;
-    if (act) {
-      const uint32_t lb = m.y;
-      if (lb == 0) {
-        pass = jw_exact(0, A.la, 0, 0, A.thr, &P.ctr->ambiguous);
+  const uint32_t e = e0 + (uint32_t)lane;
+  const bool act = e < A.n;
+  const uint32_t rrow = act ? (A.list_g ? A.list_g[e] : A.list_s[e]) : 0u;
+  const uint4 m = act ? P.R.str_meta[(size_t)A.slot_r * nR + rrow] : make_uint4(0, 0, 0, 0);
+  bool pass = false, scan = false;
+  uint32_t p = 0;
+  int need = 0;
+  if (act) {
+    const uint32_t lb = m.y;
+    if (lb == 0) {
+      pass = jw_exact(0, A.la, 0, 0, A.thr, &P.ctr->ambiguous);
+    } else {
+      const uint32_t ls = min(A.la, lb), ll = max(A.la, lb);
+      *ops += jw_eval_ops(ls, ll);
+      const uint32_t p8 = prefix8(A.a_pre0, A.a_pre1, m.z, m.w);
+      if (p8 == 8u && ls > 8u) {
+        scan = true;  // prefix longer than 8: measured exactly before the scan
+        p = kPrefixUnknown;
       } else {
-        const uint32_t ls = min(A.la, lb), ll = max(A.la, lb);
-        const uint32_t p8 = prefix8(A.a_pre0, A.a_pre1, m.z, m.w);
-        if (p8 == 8u && ls > 8u) {
-          scan = true;  // prefix longer than 8: measured exactly before the scan
-          p = kPrefixUnknown;
-        } else {
-          p = min(p8, ls);
-          need = m_need_lo(ls, ll, p, A.thr);
-          const uint32_t n_iter = min(lb, A.la + ((ls + 1u) >> 1));
-          if (need > (int)min(n_iter, ls)) {
-            *ops += scan_ops(0, ls);  // cannot reach the threshold
-          } else {
-            scan = true;
-          }
-        }
+        p = min(p8, ls);
+        need = m_need_lo(ls, ll, p, A.thr);
+        const uint32_t n_iter = min(lb, A.la + ((ls + 1u) >> 1));
+        scan = need <= (int)min(n_iter, ls);  // else the threshold is out of reach
       }
     }
-    const unsigned qm = __ballot_sync(kFull, scan);
-    if (scan) A.q[qn + __popc(qm & lt)] = make_uint4(rrow, m.x, m.y, (p << 16) | (uint32_t)need);
-    qn += __popc(qm);
-    route(P, A, pass, r, lrow, rrow, lane, lw);
   }
-  __syncwarp();
-  return qn;
+  const unsigned qm = __ballot_sync(kFull, scan);
+  if (scan)
+    A.q[(tail + __popc(qm & lt)) & (kRing - 1)] =
+        make_uint4(rrow, m.x, m.y, (p << 16) | (uint32_t)need);
+  route(P, A, pass, r, lrow, rrow, lane, lw);
+  return __popc(qm);
 }
 
-// Scan pass over the queue: lanes take the next queued pair as soon as theirs
-// is decided, so no lane waits for a longer string in a neighbour lane; every
-// loop turn scans one 4-character word for every busy lane.  A pair stops as
-// soon as even matching every remaining character stays below its bound.
+// One similarity stage of one work item.  Lanes take the next queued pair as
+// soon as theirs is decided, and the queue is refilled by filter batches as
+// it drains, so lanes stay busy whatever the strings' lengths and however
+// many rows the filter drops.  Every loop turn scans one 4-character word for
+// every busy lane; a pair stops as soon as even matching every remaining
+// character stays below its bound.  Survivors go to the next stage's row
+// list (or out, in the last stage); returns their count.
 template <int W>
-__device__ __noinline__ void scan_pass(const EvalParams& P, const Stage& A, uint32_t qn, uint32_t r,
-                                       uint32_t lrow, uint32_t* lw, unsigned long long* ops) {
+__device__ __noinline__ uint32_t run_stage(const EvalParams& P, const Stage& A, uint32_t r,
+                                           uint32_t lrow, unsigned long long* ops) {
   constexpr int S = row_words(W);
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
-  uint32_t next = 0;
+  uint32_t in_pos = 0, head = 0, tail = 0, lw = 0;
   bool busy = false;
   uint32_t rrow = 0, ls = 0, ll = 0, i = 0, n_iter = 0, h = 0, p = 0;
   int allowed = 0;
@@ -637,42 +640,46 @@ __device__ __noinline__ void scan_pass(const EvalParams& P, const Stage& A, uint
 #pragma unroll
   for (int k = 0; k < W; k++) win[k] = mt[k] = 0u;
   for (;;) {
-    bool fin = false, pass = false;
     const unsigned idle = __ballot_sync(kFull, !busy);
-    if (next < qn) {
-      const uint32_t e = next + __popc(idle & lt);
-      next += __popc(idle);
-      if (!busy && e < qn) {
-        const uint4 qe = A.q[e];
-        rrow = qe.x;
-        b = P.R.arena + 16ull * qe.y;
-        const uint32_t lb = qe.z;
-        ls = min(A.la, lb);
-        ll = max(A.la, lb);
-        h = (ls + 1u) >> 1;
-        n_iter = min(lb, A.la + h);
-        p = qe.w >> 16;
-        int need = (int)(qe.w & 0xffffu);
-        if (p == kPrefixUnknown) {
-          p = prefix_len(A.a, b, ls);
-          need = m_need_lo(ls, ll, p, A.thr);
-        }
-        if (need > (int)min(n_iter, ls)) {
-          fin = true;
-          *ops += scan_ops(0, ls);
-        } else {
-          allowed = (int)n_iter - need;
-          i = 0;
-          busy = true;
+    const uint32_t n_idle = __popc(idle);
+    // refill the ring until it holds a pair for every idle lane
+    while (tail - head < n_idle && in_pos < A.n && tail - head <= kRing - 32) {
+      tail += filter_batch(P, A, in_pos, tail, r, lrow, &lw, ops);
+      in_pos += 32;
+    }
+    bool fin = false, pass = false;
+    const uint32_t avail = tail - head;
+    const uint32_t rank = __popc(idle & lt);
+    if (!busy && rank < avail) {
+      const uint4 qe = A.q[(head + rank) & (kRing - 1)];
+      rrow = qe.x;
+      b = P.R.arena + 16ull * qe.y;
+      const uint32_t lb = qe.z;
+      ls = min(A.la, lb);
+      ll = max(A.la, lb);
+      h = (ls + 1u) >> 1;
+      n_iter = min(lb, A.la + h);
+      p = qe.w >> 16;
+      int need = (int)(qe.w & 0xffffu);
+      if (p == kPrefixUnknown) {
+        p = prefix_len(A.a, b, ls);
+        need = m_need_lo(ls, ll, p, A.thr);
+      }
+      if (need > (int)min(n_iter, ls)) {
+        fin = true;
+      } else {
+        allowed = (int)n_iter - need;
+        i = 0;
+        busy = true;
 #pragma unroll
-          for (int k = 0; k < W; k++) {
-            const int nb = (int)h + 1 - 32 * k;
-            win[k] = nb >= 32 ? 0xffffffffu : (nb <= 0 ? 0u : ((1u << nb) - 1u));
-            mt[k] = 0u;
-          }
+        for (int k = 0; k < W; k++) {
+          const int nb = (int)h + 1 - 32 * k;
+          win[k] = nb >= 32 ? 0xffffffffu : (nb <= 0 ? 0u : ((1u << nb) - 1u));
+          mt[k] = 0u;
         }
       }
     }
+    head += min(n_idle, avail);
     if (busy) {
       if ((i & 15u) == 0) {
         const uint4 v = __ldg(reinterpret_cast<const uint4*>(b + i));
@@ -696,52 +703,65 @@ __device__ __noinline__ void scan_pass(const EvalParams& P, const Stage& A, uint
         if (i >= n_iter) {
           fin = true;
           busy = false;
-          *ops += scan_ops(n_iter, ls);
           pass = jw_decide(m, ls, ll, p, A.thr, &P.ctr->ambiguous);
         } else if ((int)(i - m) > allowed) {
           fin = true;  // even matching every remaining character stays below
           busy = false;
-          *ops += scan_ops(i, ls);
         }
       }
     }
-    route(P, A, fin && pass, r, lrow, rrow, lane, lw);
-    if (!__any_sync(kFull, busy) && next >= qn) break;
+    route(P, A, fin && pass, r, lrow, rrow, lane, &lw);
+    if (!__any_sync(kFull, busy) && head == tail && in_pos >= A.n) break;
   }
   __syncwarp();
-}
-
-__device__ __forceinline__ void scan_dispatch(uint32_t W, const EvalParams& P, const Stage& A,
-                                              uint32_t qn, uint32_t r, uint32_t lrow, uint32_t* lw,
-                                              unsigned long long* ops) {
-  switch (W) {
-    case 1: scan_pass<1>(P, A, qn, r, lrow, lw, ops); break;
-    case 2: scan_pass<2>(P, A, qn, r, lrow, lw, ops); break;
-    case 3: scan_pass<3>(P, A, qn, r, lrow, lw, ops); break;
-    case 4: scan_pass<4>(P, A, qn, r, lrow, lw, ops); break;
-    case 5: scan_pass<5>(P, A, qn, r, lrow, lw, ops); break;
-    case 6: scan_pass<6>(P, A, qn, r, lrow, lw, ops); break;
-    case 7: scan_pass<7>(P, A, qn, r, lrow, lw, ops); break;
-    default: scan_pass<8>(P, A, qn, r, lrow, lw, ops); break;
-  }
+  return lw;
 }
 
 // Stage over a left string the fast path does not take (longer than 256
 // bytes, or no room for its table): the reference's own loops per lane.
 __device__ __noinline__ uint32_t run_stage_slow(const EvalParams& P, const Stage& A, uint32_t s_l,
-                                                uint32_t r, uint32_t lrow) {
+                                                uint32_t r, uint32_t lrow,
+                                                unsigned long long* ops) {
   const int lane = threadIdx.x & 31;
   uint32_t lw = 0;
   for (uint32_t e0 = 0; e0 < A.n; e0 += 32) {
     const uint32_t e = e0 + (uint32_t)lane;
     const bool act = e < A.n;
     const uint32_t rrow = act ? (A.list_g ? A.list_g[e] : A.list_s[e]) : 0u;
-    const bool pass = act && sim_pass_slow(P.L, P.R, s_l, A.slot_r, lrow, rrow, A.thr, P.ctr);
+    bool pass = false;
+    if (act) {
+      const uint32_t lb = P.R.str_meta[(size_t)A.slot_r * P.R.n_rows + rrow].y;
+      if (lb && A.la) *ops += jw_eval_ops(min(A.la, lb), max(A.la, lb));
+      pass = sim_pass_slow(P.L, P.R, s_l, A.slot_r, lrow, rrow, A.thr, P.ctr);
+    }
     __syncwarp();
     route(P, A, pass, r, lrow, rrow, lane, &lw);
   }
   __syncwarp();
   return lw;
+}
+
+__device__ __forceinline__ uint32_t stage_dispatch(uint32_t W, const EvalParams& P, const Stage& A,
+                                                   uint32_t r, uint32_t lrow,
+                                                   unsigned long long* ops) {
+  switch (W) {
+    case 1: return run_stage<1>(P, A, r, lrow, ops);
+    case 2: return run_stage<2>(P, A, r, lrow, ops);
+    case 3: return run_stage<3>(P, A, r, lrow, ops);
+    case 4: return run_stage<4>(P, A, r, lrow, ops);
+    default: return run_stage<8>(P, A, r, lrow, ops);
+  }
+}
+
+// Maps a position of the launch's work list to a global work item: the list
+// is the concatenation of the segments [seg_begin[k], seg_end[k]).
+__device__ __forceinline__ unsigned long long seg_item(const EvalParams& P, unsigned long long v) {
+  for (uint32_t k = 0; k < P.n_seg; k++) {
+    const unsigned long long len = P.seg_end[k] - P.seg_begin[k];
+    if (v < len) return P.seg_begin[k] + v;
+    v -= len;
+  }
+  return ~0ull;
 }
 
 __global__ void __launch_bounds__(kWarpsPerCta * 32, 3) k_eval(EvalParams P) {
@@ -751,39 +771,46 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, 3) k_eval(EvalParams P) {
   uint32_t* region = smem + (size_t)warp * P.warp_words;
   uint32_t* list_s = region + P.list_off;
   uint4* q = reinterpret_cast<uint4*>(region + P.queue_off);
-  const unsigned long long end = P.range_is_device ? P.rule_item_base[P.n_rules] : P.item_end;
+  unsigned long long n_work = 0;  // length of this launch's work list
+  if (P.n_seg == 0) {
+    n_work = P.rule_item_base[P.n_rules];
+  } else {
+    for (uint32_t k = 0; k < P.n_seg; k++) n_work += P.seg_end[k] - P.seg_begin[k];
+  }
   const long long t_start = clock64();
-  // warp-level cache of the last (rule, key) item range
+  // warp-level cache of the last (rule, left key) item range
   uint32_t c_rule = 0xffffffffu, c_key = 0;
   unsigned long long c_lo = 1, c_hi = 0;
   unsigned long long done = 0;
   unsigned long long ops = 0;
 
   for (;;) {
-    unsigned long long it = 0;
-    if (lane == 0) it = P.item_begin + atomicAdd(&P.ctr->work_next, 1ull);
-    it = __shfl_sync(kFull, it, 0);
-    if (it >= end) break;
+    unsigned long long v = 0;
+    if (lane == 0) v = atomicAdd(&P.ctr->work_next, 1ull);
+    v = __shfl_sync(kFull, v, 0);
+    if (v >= n_work) break;
     if (P.watchdog_cycles && (unsigned long long)(clock64() - t_start) > P.watchdog_cycles) {
       if (lane == 0) atomicAdd(&P.ctr->watchdog_trips, 1ull);
       break;
     }
+    const unsigned long long it = P.n_seg ? seg_item(P, v) : v;
     uint32_t r = 0;
     while (r + 1 < P.n_rules && P.rule_item_base[r + 1] <= it) r++;
     const Rule& R = P.rules[r];
     const unsigned long long local = it - P.rule_item_base[r];
     if (r != c_rule || local < c_lo || local >= c_hi) {
       c_rule = r;
-      c_key = find_key(R.item_off, R.domain, local);
+      c_key = find_key(R.item_off, R.domain_l, local);
       c_lo = R.item_off[c_key];
       c_hi = R.item_off[c_key + 1];
     }
-    const uint32_t key = c_key;
+    const uint32_t jl = c_key;            // left key (word class, join key)
+    const uint32_t key = jl % R.domain;   // join key
     const unsigned long long in_key = local - c_lo;
-    const uint32_t nl = R.cnt_l[key], nr = R.cnt_r[key];
+    const uint32_t nl = R.cnt_l[jl], nr = R.cnt_r[key];
     const uint32_t ri = (uint32_t)(in_key / nl);
     const uint32_t li = (uint32_t)(in_key - (unsigned long long)ri * nl);
-    const uint32_t lrow = R.sorted_l[R.off_l[key] + li];
+    const uint32_t lrow = R.sorted_l[R.off_l[jl] + li];
     const uint32_t rb0 = R.off_r[key] + ri * P.tile_right;
     const uint32_t rb1 = min(rb0 + P.tile_right, R.off_r[key] + nr);
 
@@ -791,9 +818,7 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, 3) k_eval(EvalParams P) {
       for (uint32_t rb = rb0; rb < rb1; rb += 32) {
         const uint32_t idx = rb + (uint32_t)lane;
         const uint32_t rrow = idx < rb1 ? R.sorted_r[idx] : 0u;
-        bool pass = idx < rb1;
-        if (pass && r > 0) pass = !earlier_rule_matches(P, r, lrow, rrow);
-        emit(P, pass, lrow, rrow, lane);
+        emit(P, idx < rb1, lrow, rrow, lane);
       }
     } else {
       Stage A;
@@ -814,20 +839,17 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, 3) k_eval(EvalParams P) {
         const uint32_t W = (A.la + 31u) >> 5;
         const bool fast =
             A.la > 0 && A.la <= 256 && R.peq_rows_words[s] >= (uint32_t)row_words((int)W);
-        uint32_t lw = 0;
+        uint32_t n_next;
         if (fast) {
-          const uint32_t qn = filter_pass(P, A, r, lrow, &lw, &ops);
-          if (qn) {
-            uint32_t* tab = region + R.peq_off[s];
-            build_peq(tab, (uint32_t)row_words((int)W), P.n_symbols, A.a, A.la, lane);
-            A.tab = tab;
-            scan_dispatch(W, P, A, qn, r, lrow, &lw, &ops);
-          }
+          uint32_t* tab = region + R.peq_off[s];
+          build_peq(tab, (uint32_t)row_words((int)W), P.n_symbols, A.a, A.la, lane);
+          A.tab = tab;
+          n_next = stage_dispatch(W, P, A, r, lrow, &ops);
         } else {
-          lw = run_stage_slow(P, A, sl, r, lrow);
+          n_next = run_stage_slow(P, A, sl, r, lrow, &ops);
         }
         A.list_g = nullptr;
-        A.n = lw;
+        A.n = n_next;
       }
     }
     done++;

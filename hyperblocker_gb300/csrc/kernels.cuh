@@ -65,19 +65,35 @@ struct Rule {
   float thr[kMaxSim];
   uint32_t peq_rows_words[kMaxSim];  // words per symbol row reserved (1,2,4,8), 0 = none
   uint32_t peq_off[kMaxSim];         // word offset of the sim's table in a warp region
-  uint32_t domain;
+  uint32_t domain;    // D: join keys
+  // Left rows are grouped by (word class, key): the word class is the number
+  // of 32-symbol words of the left string of the first similarity predicate
+  // (1, 2, 3, 4, more).  Work items are ordered class by class, so warps that
+  // run at the same time mostly run the same scan variant.
+  uint32_t n_wclass;  // 1 (no split) or kWordClasses
+  uint32_t wclass_slot;  // left string slot that decides the class
+  uint32_t domain_l;  // n_wclass * D: left keys
   uint32_t* key_l;
   uint32_t* key_r;
-  uint32_t* cnt_l;
-  uint32_t* cnt_r;
-  uint32_t* off_l;
-  uint32_t* off_r;
+  uint32_t* cnt_l;  // [domain_l]
+  uint32_t* cnt_r;  // [domain]
+  uint32_t* off_l;  // [domain_l]
+  uint32_t* off_r;  // [domain]
   uint32_t* cur_l;
   uint32_t* cur_r;
-  unsigned long long* item_off;  // [domain + 1]
+  unsigned long long* item_off;  // [domain_l + 1]
   uint32_t* sorted_l;
   uint32_t* sorted_r;
 };
+
+constexpr uint32_t kWordClasses = 5;
+constexpr uint32_t kMaxSegments = 8;
+constexpr uint32_t kRingEntries = 64;
+
+__host__ __device__ inline uint32_t word_class(uint32_t len) {
+  const uint32_t w = (len + 31u) >> 5;
+  return w == 0 ? 0u : (w > kWordClasses ? kWordClasses - 1 : w - 1);
+}
 
 struct Counters {
   unsigned long long out_count;
@@ -88,6 +104,7 @@ struct Counters {
   unsigned long long watchdog_trips;
   unsigned long long items_done;
   unsigned long long jw_word_ops;  // algorithmic work of the JW evaluations
+  unsigned long long seen_overflow;  // pairs the duplicate set had no room for
 };
 
 struct EvalParams {
@@ -96,20 +113,24 @@ struct EvalParams {
   uint32_t n_rules;
   uint32_t n_symbols;
   const unsigned long long* rule_item_base;  // [n_rules + 1], global item space
-  // item range [item_begin, item_end) in the global space; the batched form
-  // covers every rule, the plain form one (partition, rule).
-  unsigned long long item_begin;
-  unsigned long long item_end;
-  int range_is_device;  // 1: item_end = rule_item_base[n_rules] (read on device)
+  // Work list of the launch: every item (n_seg == 0, the batched form), or the
+  // concatenation of item ranges [seg_begin[k], seg_end[k]) (the plain form:
+  // one partition of one rule, one range per word class).
+  uint32_t n_seg;
+  unsigned long long seg_begin[kMaxSegments];
+  unsigned long long seg_end[kMaxSegments];
   uint32_t tile_right;  // TR
-  uint32_t warp_words;  // shared-memory words per warp: Peq tables, row list, scan queue
+  uint32_t warp_words;  // shared-memory words per warp: Peq tables, row list, scan ring
   uint32_t list_off;    // word offset of the warp's row list (tile_right words)
-  uint32_t queue_off;   // word offset of the warp's scan queue (tile_right x uint4)
+  uint32_t queue_off;   // word offset of the warp's scan ring (kRingEntries x uint4)
   uint32_t* out_l;
   uint32_t* out_r;
   unsigned long long capacity;
   Counters* ctr;
   unsigned long long watchdog_cycles;  // 0 = no budget
+  // set of reported (left, right) keys when the plan has several rules, else null
+  unsigned long long* seen;
+  unsigned long long seen_mask;  // slots - 1 (a power of two minus one)
 };
 
 // ------------------------------------------------------------------ join
