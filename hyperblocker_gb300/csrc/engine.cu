@@ -16,6 +16,7 @@
 #include <cstring>
 #include <functional>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -284,8 +285,17 @@ void setup_session(hbx_session* S) {
   if (S->queue_off % 4 || S->queue_off + 4 * dev::kRingEntries > S->warp_words ||
       S->warp_words > cap_warp_words)
     fail(HBX_ERR_CUDA, "shared-memory layout exceeds its allocation");
-  HBX_CUDA(cudaFuncSetAttribute(dev::k_eval, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)S->smem_bytes));
+  {
+    // The limit belongs to the kernel, process-wide: only ever raise it, so a
+    // session needing less never lowers it under another live session.
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lock(mu);
+    cudaFuncAttributes fa;
+    HBX_CUDA(cudaFuncGetAttributes(&fa, dev::k_eval));
+    if ((size_t)fa.maxDynamicSharedSizeBytes < S->smem_bytes)
+      HBX_CUDA(cudaFuncSetAttribute(dev::k_eval, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)S->smem_bytes));
+  }
   int bps = 0;
   HBX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, dev::k_eval, kThreads, S->smem_bytes));
   S->blocks_per_sm = std::max(1, bps);
