@@ -108,6 +108,10 @@ SIGNATURES = {
                                  ctypes.POINTER(Pairs), ctypes.POINTER(Stats)]),
     "hbx_write_pairs": (ctypes.c_int, [_VP, _VP, _VP, _VP, _VP, ctypes.c_uint64, ctypes.c_char_p]),
     "hbx_run_cli": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_char_p)]),
+    "hbx_block_static": (ctypes.c_int, [ctypes.c_int, _VP, _VP, _VP, ctypes.c_uint64,
+                                        ctypes.c_int64, ctypes.POINTER(Pairs), _VP,
+                                        ctypes.POINTER(Stats)]),
+    "hbx_static_last_error": (ctypes.c_char_p, []),
 }
 
 _lib: Optional[ctypes.CDLL] = None

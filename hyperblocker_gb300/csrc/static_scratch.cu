@@ -1,0 +1,381 @@
+// static_scratch.cu -- hbx_block_static: the blocking pipeline with no device
+// memory allocation of its own.
+//
+// Some callers cannot call cudaMalloc: an application whose device memory is
+// carved up up-front by another runtime or a memory pool it does not share,
+// a process running under a fixed device-memory budget, or a latency-critical
+// loop that cannot afford cudaMalloc/cudaFree, which may synchronize the whole
+// device.  For them this entry point runs the same kernels as hbx_block (the
+// equality join, the Jaro-Winkler evaluation and the duplicate set), but every
+// buffer they need -- the encoded tables, the join's histograms, offsets and
+// sorted rows, the counters and the duplicate set -- is carved out of one
+// file-scope device array of kStaticScratchBytes (64 MiB).  The caller passes
+// the tables and the output buffers; nothing here calls cudaMalloc, cudaFree,
+// or any other allocating routine (no streams, events or graphs are created).
+//
+// Costs and limits, stated for the caller:
+//   * every GPU that loads libhbx.so holds the 64 MiB array until the process
+//     exits;
+//   * an input whose encoding, join state and duplicate set do not fit is
+//     refused with HBX_ERR_INVALID_ARG and a message with the bytes needed;
+//   * every call shares the one array and keeps the previous call's contents
+//     (whatever must start at zero is cleared by the call itself), so calls
+//     whose work overlaps on the GPU -- from several host threads, or on
+//     several streams without ordering between them -- race and corrupt each
+//     other;
+//   * the first call on a device looks up the array's device address (once
+//     per device, with that device current); make that first call before any
+//     stream capture begins.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "encode.h"
+#include "hbx_core.h"
+#include "kernels.cuh"
+
+namespace {
+
+constexpr size_t kStaticScratchBytes = 64ull << 20;
+constexpr int kMaxDevices = 64;
+
+// The scratch.  In host code this name is only a stand-in for the symbol, not
+// a device address: kernels get the address cudaGetSymbolAddress returns.
+static __device__ __align__(256) unsigned char g_scratch[kStaticScratchBytes];
+
+std::mutex g_mu;
+unsigned char* g_scratch_addr[kMaxDevices] = {};
+thread_local std::string g_static_err;
+
+#define HBX_STATIC_CUDA(expr)                                                              \
+  do {                                                                                     \
+    cudaError_t e_ = (expr);                                                               \
+    if (e_ != cudaSuccess)                                                                 \
+      ::hbx::fail(HBX_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_));       \
+  } while (0)
+
+// Device address of the scratch on the current device (looked up once).
+unsigned char* scratch_on(int device) {
+  std::lock_guard<std::mutex> lock(g_mu);
+  if (!g_scratch_addr[device]) {
+    void* p = nullptr;
+    HBX_STATIC_CUDA(cudaGetSymbolAddress(&p, g_scratch));
+    g_scratch_addr[device] = (unsigned char*)p;
+  }
+  return g_scratch_addr[device];
+}
+
+// Bump allocation of 256-byte aligned pieces of the scratch.  A first pass
+// with base == nullptr only measures.
+struct Carve {
+  unsigned char* base;
+  size_t used = 0;
+  template <class T>
+  T* take(size_t count) {
+    used = (used + 255) / 256 * 256;
+    T* p = base ? (T*)(base + used) : nullptr;
+    used += std::max<size_t>(count, 1) * sizeof(T);
+    return p;
+  }
+};
+
+template <class T>
+std::vector<T> flat(const std::vector<std::vector<T>>& v) {
+  std::vector<T> out;
+  for (auto& x : v) out.insert(out.end(), x.begin(), x.end());
+  return out;
+}
+
+std::vector<uint4> string_meta(const hbx::SideEnc& se, uint32_t n) {
+  std::vector<uint4> meta;
+  meta.reserve(se.str_off.size() * (size_t)n);
+  for (size_t slot = 0; slot < se.str_off.size(); slot++)
+    for (uint32_t i = 0; i < n; i++) {
+      const uint32_t off = se.str_off[slot][i], len = se.str_len[slot][i];
+      uint32_t pre[2] = {0, 0};
+      for (uint32_t k = 0; k < 8 && k < len; k++)
+        pre[k / 4] |= (uint32_t)se.arena[(size_t)off * 16 + k] << (8 * (k % 4));
+      meta.push_back(make_uint4(off, len, pre[0], pre[1]));
+    }
+  return meta;
+}
+
+struct Layout {
+  hbx::dev::Side L{}, R{};
+  std::vector<hbx::dev::Rule> rules;
+  std::vector<uint32_t> nb, nb_l;
+  hbx::dev::Rule* d_rules = nullptr;
+  unsigned long long* rule_base = nullptr;
+  hbx::dev::Counters* ctr = nullptr;
+  unsigned long long* seen = nullptr;
+  unsigned long long seen_slots = 0;
+  uint32_t* part_u32 = nullptr;
+  unsigned long long* part_u64 = nullptr;
+  uint32_t warp_words = 0, list_off = 0, queue_off = 0, tile_right = 128;
+};
+
+// Places every buffer; with c.base == nullptr it only measures.
+void place(Carve& c, const hbx::Encoded& E, uint64_t capacity, size_t smem_cap, Layout* Y,
+           const std::vector<uint4>& ml, const std::vector<uint4>& mr) {
+  namespace dev = hbx::dev;
+  const uint32_t nL = (uint32_t)E.L.n_rows, nR = (uint32_t)E.R.n_rows;
+  auto side = [&](const hbx::SideEnc& se, dev::Side& ds, uint32_t n, const std::vector<uint4>& m) {
+    ds.bucket = c.take<uint32_t>(n);
+    ds.eq_codes = c.take<int32_t>(se.eq_codes.size() * (size_t)n);
+    ds.comp_codes = c.take<int32_t>(se.comp_codes.size() * (size_t)n);
+    ds.arena = c.take<uint8_t>(se.arena.size());
+    ds.str_meta = c.take<uint4>(m.size());
+    ds.n_rows = n;
+  };
+  side(E.L, Y->L, nL, ml);
+  side(E.R, Y->R, nR, mr);
+  const uint32_t NS = E.n_symbols;
+  const uint32_t cap_warp_words = (uint32_t)(smem_cap / 4 / dev::kWarpsPerCta) / 4 * 4;
+  const uint32_t list_queue_words = Y->tile_right + 4 * dev::kRingEntries;
+  const uint32_t max_warp_words = cap_warp_words - list_queue_words;
+  uint32_t warp_words = 4;
+  Y->rules.assign(E.rules.size(), dev::Rule{});
+  Y->nb.assign(E.rules.size(), 0);
+  Y->nb_l.assign(E.rules.size(), 0);
+  uint32_t max_nb = 1;
+  for (size_t r = 0; r < E.rules.size(); r++) {
+    const hbx::RuleEnc& re = E.rules[r];
+    dev::Rule& d = Y->rules[r];
+    d.n_eq = (uint32_t)re.eq_slot.size();
+    d.n_sim = (uint32_t)re.sim_slot_l.size();
+    d.composite = re.composite ? 1u : 0u;
+    d.comp_index = re.composite ? (uint32_t)re.comp_index : 0u;
+    for (size_t e = 0; e < re.eq_slot.size(); e++) {
+      d.eq_slot[e] = (uint32_t)re.eq_slot[e];
+      d.radix[e] = re.radix[e];
+    }
+    uint32_t off = 0;
+    for (size_t s = 0; s < re.sim_slot_l.size(); s++) {
+      d.sim_l[s] = (uint32_t)re.sim_slot_l[s];
+      d.sim_r[s] = (uint32_t)re.sim_slot_r[s];
+      d.thr[s] = re.thr[s];
+      const uint32_t mx = std::min<uint32_t>(E.L.str_maxlen[(size_t)re.sim_slot_l[s]], hbx::kFastMaxLen);
+      const uint32_t S32 = mx ? (uint32_t)dev::row_words((int)((mx + 31) / 32)) : 0u;
+      const uint32_t words = (NS * S32 + 3) / 4 * 4;
+      if (S32 && off + words <= max_warp_words) {
+        d.peq_rows_words[s] = S32;
+        d.peq_off[s] = off;
+        off += words;
+      }
+    }
+    warp_words = std::max(warp_words, off);
+    d.domain = (uint32_t)re.domain;
+    const bool split = !re.sim_slot_l.empty() &&
+                       re.domain * dev::kWordClasses <= (uint64_t)hbx::kMaxKeyDomain * 4;
+    d.n_wclass = split ? dev::kWordClasses : 1u;
+    d.wclass_slot = split ? (uint32_t)re.sim_slot_l[0] : 0u;
+    d.domain_l = d.n_wclass * d.domain;
+    d.key_l = c.take<uint32_t>(nL);
+    d.key_r = c.take<uint32_t>(nR);
+    d.cnt_l = c.take<uint32_t>(d.domain_l);
+    d.cnt_r = c.take<uint32_t>(d.domain);
+    d.off_l = c.take<uint32_t>(d.domain_l);
+    d.off_r = c.take<uint32_t>(d.domain);
+    d.cur_l = c.take<uint32_t>(d.domain_l);
+    d.cur_r = c.take<uint32_t>(d.domain);
+    d.item_off = c.take<unsigned long long>((size_t)d.domain_l + 1);
+    d.sorted_l = c.take<uint32_t>(nL);
+    d.sorted_r = c.take<uint32_t>(nR);
+    Y->nb[r] = (d.domain + dev::kScanChunk - 1) / dev::kScanChunk;
+    Y->nb_l[r] = (d.domain_l + dev::kScanChunk - 1) / dev::kScanChunk;
+    max_nb = std::max(max_nb, std::max(Y->nb[r], Y->nb_l[r]));
+  }
+  Y->list_off = warp_words;
+  Y->queue_off = warp_words + Y->tile_right;
+  Y->warp_words = Y->queue_off + 4 * dev::kRingEntries;
+  Y->part_u32 = c.take<uint32_t>(max_nb);
+  Y->part_u64 = c.take<unsigned long long>(max_nb);
+  Y->d_rules = c.take<dev::Rule>(E.rules.size());
+  Y->rule_base = c.take<unsigned long long>(E.rules.size() + 1);
+  Y->ctr = c.take<dev::Counters>(1);
+  if (E.rules.size() > 1) {
+    unsigned long long slots = 1024;
+    while (slots < 2 * capacity) slots *= 2;
+    Y->seen_slots = slots;
+    Y->seen = c.take<unsigned long long>(slots);
+  }
+}
+
+void run_static(int device, const hbx_plan* plan, const hbx_table* left, const hbx_table* right,
+                uint64_t n_partitions, int64_t prefix_idx, hbx_pairs* out, cudaStream_t st,
+                hbx_stats* stats) {
+  namespace dev = hbx::dev;
+  int n_dev = 0;
+  HBX_STATIC_CUDA(cudaGetDeviceCount(&n_dev));
+  if (device < 0 || device >= n_dev || device >= kMaxDevices)
+    hbx::fail(HBX_ERR_INVALID_ARG, "no such CUDA device");
+  if (prefix_idx != INT_MAX && (prefix_idx < 0 || prefix_idx > INT_MAX))
+    hbx::fail(HBX_ERR_INVALID_ARG, "prefix_idx out of range");
+  if (out->capacity && (!out->l_row || !out->r_row))
+    hbx::fail(HBX_ERR_INVALID_ARG, "null output pointer");
+  const hbx::Encoded E = hbx::encode(plan->p, left->t, right->t, n_partitions, prefix_idx);
+  const uint32_t nL = (uint32_t)E.L.n_rows, nR = (uint32_t)E.R.n_rows;
+  const std::vector<uint4> ml = string_meta(E.L, nL), mr = string_meta(E.R, nR);
+
+  cudaDeviceProp prop;
+  HBX_STATIC_CUDA(cudaGetDeviceProperties(&prop, device));
+  const size_t smem_cap = std::min<size_t>(prop.sharedMemPerBlockOptin, 200 * 1024);
+  Layout Y;
+  Carve measure{nullptr};
+  place(measure, E, out->capacity, smem_cap, &Y, ml, mr);
+  if (measure.used > kStaticScratchBytes)
+    hbx::fail(HBX_ERR_INVALID_ARG,
+              "input needs " + std::to_string(measure.used) + " bytes of device scratch; the "
+              "static scratch holds " + std::to_string(kStaticScratchBytes));
+
+  int prev = 0;
+  HBX_STATIC_CUDA(cudaGetDevice(&prev));
+  HBX_STATIC_CUDA(cudaSetDevice(device));
+  struct Restore {
+    int d;
+    ~Restore() { cudaSetDevice(d); }
+  } restore{prev};
+  Carve carve{scratch_on(device)};
+  place(carve, E, out->capacity, smem_cap, &Y, ml, mr);
+
+  auto up = [&](void* dst, const void* src, size_t bytes) {
+    if (bytes) HBX_STATIC_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
+  };
+  auto up_side = [&](const hbx::SideEnc& se, const dev::Side& ds, const std::vector<uint4>& m) {
+    up((void*)ds.bucket, se.bucket.data(), se.bucket.size() * 4);
+    const std::vector<int32_t> eq = flat(se.eq_codes), comp = flat(se.comp_codes);
+    up((void*)ds.eq_codes, eq.data(), eq.size() * 4);
+    up((void*)ds.comp_codes, comp.data(), comp.size() * 4);
+    up((void*)ds.arena, se.arena.data(), se.arena.size());
+    up((void*)ds.str_meta, m.data(), m.size() * sizeof(uint4));
+    HBX_STATIC_CUDA(cudaStreamSynchronize(st));  // host vectors of this scope end here
+  };
+  up_side(E.L, Y.L, ml);
+  up_side(E.R, Y.R, mr);
+  up(Y.d_rules, Y.rules.data(), Y.rules.size() * sizeof(dev::Rule));
+
+  // counters, histograms, cursors and the duplicate set start from zero/empty
+  HBX_STATIC_CUDA(cudaMemsetAsync(Y.ctr, 0, sizeof(dev::Counters), st));
+  if (Y.seen) HBX_STATIC_CUDA(cudaMemsetAsync(Y.seen, 0xff, Y.seen_slots * 8, st));
+  const int n_sm = prop.multiProcessorCount;
+  auto grid_for = [&](uint32_t n) {
+    return (int)std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, (uint64_t)n_sm * 8));
+  };
+  for (size_t r = 0; r < Y.rules.size(); r++) {
+    const dev::Rule& d = Y.rules[r];
+    HBX_STATIC_CUDA(cudaMemsetAsync(d.cnt_l, 0, d.domain_l * 4, st));
+    HBX_STATIC_CUDA(cudaMemsetAsync(d.cnt_r, 0, d.domain * 4, st));
+    HBX_STATIC_CUDA(cudaMemsetAsync(d.cur_l, 0, d.domain_l * 4, st));
+    HBX_STATIC_CUDA(cudaMemsetAsync(d.cur_r, 0, d.domain * 4, st));
+    const uint32_t ru = (uint32_t)r;
+    if (nL) dev::k_keys_hist<<<grid_for(nL), 256, 0, st>>>(Y.L, Y.d_rules, ru, 0);
+    if (nR) dev::k_keys_hist<<<grid_for(nR), 256, 0, st>>>(Y.R, Y.d_rules, ru, 1);
+    dev::k_scan_partial_u32<<<Y.nb_l[r], 1024, 0, st>>>(d.cnt_l, d.domain_l, Y.part_u32);
+    dev::k_scan_top_u32<<<1, 1024, 0, st>>>(Y.part_u32, Y.nb_l[r]);
+    dev::k_scan_final_u32<<<Y.nb_l[r], 1024, 0, st>>>(d.cnt_l, d.domain_l, Y.part_u32, d.off_l);
+    dev::k_scan_partial_u32<<<Y.nb[r], 1024, 0, st>>>(d.cnt_r, d.domain, Y.part_u32);
+    dev::k_scan_top_u32<<<1, 1024, 0, st>>>(Y.part_u32, Y.nb[r]);
+    dev::k_scan_final_u32<<<Y.nb[r], 1024, 0, st>>>(d.cnt_r, d.domain, Y.part_u32, d.off_r);
+    dev::k_items_partial<<<Y.nb_l[r], 1024, 0, st>>>(Y.d_rules, ru, Y.tile_right, Y.part_u64,
+                                                     &Y.ctr->comparisons);
+    dev::k_scan_top_u64<<<1, 1024, 0, st>>>(Y.part_u64, Y.nb_l[r]);
+    dev::k_items_final<<<Y.nb_l[r], 1024, 0, st>>>(Y.d_rules, ru, Y.tile_right, Y.part_u64);
+    if (nL) dev::k_scatter<<<grid_for(nL), 256, 0, st>>>(Y.L, Y.d_rules, ru, 0);
+    if (nR) dev::k_scatter<<<grid_for(nR), 256, 0, st>>>(Y.R, Y.d_rules, ru, 1);
+  }
+  dev::k_rule_base<<<1, 32, 0, st>>>(Y.d_rules, (uint32_t)Y.rules.size(), Y.rule_base);
+  HBX_STATIC_CUDA(cudaGetLastError());
+
+  dev::EvalParams P{};
+  P.L = Y.L;
+  P.R = Y.R;
+  P.rules = Y.d_rules;
+  P.n_rules = (uint32_t)Y.rules.size();
+  P.n_symbols = E.n_symbols;
+  P.rule_item_base = Y.rule_base;
+  P.n_seg = 0;
+  P.tile_right = Y.tile_right;
+  P.warp_words = Y.warp_words;
+  P.list_off = Y.list_off;
+  P.queue_off = Y.queue_off;
+  P.out_l = out->l_row;
+  P.out_r = out->r_row;
+  P.capacity = out->capacity;
+  P.ctr = Y.ctr;
+  P.seen = Y.seen;
+  P.seen_mask = Y.seen ? Y.seen_slots - 1 : 0;
+  const size_t smem = (size_t)Y.warp_words * 4 * dev::kWarpsPerCta;
+  {
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lock(mu);
+    cudaFuncAttributes fa;
+    HBX_STATIC_CUDA(cudaFuncGetAttributes(&fa, dev::k_eval));
+    if ((size_t)fa.maxDynamicSharedSizeBytes < smem)
+      HBX_STATIC_CUDA(cudaFuncSetAttribute(dev::k_eval, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem));
+  }
+  int bps = 0;
+  HBX_STATIC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, dev::k_eval,
+                                                                dev::kWarpsPerCta * 32, smem));
+  dev::k_eval<<<n_sm * std::max(1, bps), dev::kWarpsPerCta * 32, smem, st>>>(P);
+  HBX_STATIC_CUDA(cudaGetLastError());
+
+  dev::Counters c{};
+  unsigned long long total_items = 0;
+  HBX_STATIC_CUDA(cudaMemcpyAsync(&c, Y.ctr, sizeof c, cudaMemcpyDeviceToHost, st));
+  HBX_STATIC_CUDA(cudaMemcpyAsync(&total_items, Y.rule_base + Y.rules.size(), 8,
+                                  cudaMemcpyDeviceToHost, st));
+  HBX_STATIC_CUDA(cudaStreamSynchronize(st));
+  if (c.items_done != total_items) hbx::fail(HBX_ERR_CUDA, "evaluation did not finish its work");
+  out->n_required = c.out_count + c.seen_overflow;
+  out->n_written = 0;
+  if (stats) {
+    *stats = hbx_stats{};
+    stats->pairs_covered = E.pairs_covered;
+    stats->pair_comparisons = c.comparisons;
+    stats->n_matches = c.out_count;
+    stats->fma_ambiguous = c.ambiguous;
+    stats->long_string_pairs = c.long_pairs;
+    stats->n_tiles = total_items;
+    stats->n_partitions_used = E.n_partitions_used;
+    stats->jw_word_ops = c.jw_word_ops;
+    stats->h2d_bytes = measure.used;
+  }
+  if (c.out_count > out->capacity || c.seen_overflow)
+    hbx::fail(HBX_ERR_CAPACITY, "output capacity below the match count");
+  out->n_written = c.out_count;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* hbx_static_last_error(void) { return g_static_err.c_str(); }
+
+hbx_status hbx_block_static(int device, const hbx_plan* plan, const hbx_table* left,
+                            const hbx_table* right, uint64_t n_partitions, int64_t prefix_idx,
+                            hbx_pairs* out, void* stream, hbx_stats* stats) {
+  if (!plan || !left || !right || !out) return HBX_ERR_INVALID_ARG;
+  try {
+    run_static(device, plan, left, right, n_partitions, prefix_idx, out, (cudaStream_t)stream,
+               stats);
+    g_static_err.clear();
+    return HBX_OK;
+  } catch (const hbx::Error& e) {
+    g_static_err = e.what();
+    return e.status;
+  } catch (const std::bad_alloc&) {
+    g_static_err = "host out of memory";
+    return HBX_ERR_OOM;
+  } catch (const std::exception& e) {
+    g_static_err = e.what();
+    return HBX_ERR_INVALID_ARG;
+  }
+}
+
+}  // extern "C"

@@ -170,6 +170,31 @@ hbx_status hbx_write_pairs(hbx_ctx* ctx, const hbx_table* left, const hbx_table*
  * exit code (0 on success). */
 int hbx_run_cli(int argc, const char* const* argv);
 
+/* ---- blocking without device allocation ----------------------------------
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc:
+ * an application whose device memory is handed out up front by another
+ * runtime or pool, a process under a fixed device-memory budget, or a
+ * latency-critical loop that cannot pay for cudaMalloc/cudaFree, which may
+ * synchronize the device.  Same result as hbx_block, but every buffer the
+ * kernels need comes from one static device array of 64 MiB inside
+ * libhbx.so (held on every GPU that loads the library until exit); this call
+ * allocates no device memory and creates no stream, event or graph.
+ *   - out holds DEVICE pointers owned by the caller; stream may be NULL;
+ *   - inputs whose encoding, join state and duplicate set exceed the 64 MiB
+ *     are refused with HBX_ERR_INVALID_ARG (hbx_static_last_error() gives the
+ *     bytes needed);
+ *   - all calls share the array: calls whose GPU work overlaps (other host
+ *     threads, unordered streams) race; each call clears what must start at
+ *     zero itself;
+ *   - the first call on a device looks up the array's address on that
+ *     device; make it before any stream capture begins.
+ * Returns when the pairs are in out (synchronous on the stream). */
+hbx_status hbx_block_static(int device, const hbx_plan* plan, const hbx_table* left,
+                            const hbx_table* right, uint64_t n_partitions, int64_t prefix_idx,
+                            hbx_pairs* out, void* stream, hbx_stats* stats);
+/* Text of the last hbx_block_static failure on the calling thread. */
+const char* hbx_static_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif
