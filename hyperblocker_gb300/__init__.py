@@ -49,7 +49,7 @@ class HbxError(RuntimeError):
 
 class Opts(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_uint32), ("use_graph", ctypes.c_int32),
-                ("tile_right", ctypes.c_int32), ("warps_per_cta", ctypes.c_int32),
+                ("tile_right", ctypes.c_int32), ("eval_variant", ctypes.c_int32),
                 ("watchdog_cycles", ctypes.c_uint64)]
 
 
@@ -143,8 +143,9 @@ class Context:
     """A CUDA device + stream for the engine (hbx_ctx)."""
 
     def __init__(self, device: int = 0, use_graph: bool = True, tile_right: int = 0,
-                 watchdog_cycles: int = 0):
-        o = Opts(ctypes.sizeof(Opts), 1 if use_graph else 0, tile_right, 0, watchdog_cycles)
+                 watchdog_cycles: int = 0, eval_variant: int = 0):
+        o = Opts(ctypes.sizeof(Opts), 1 if use_graph else 0, tile_right, eval_variant,
+                 watchdog_cycles)
         h = _VP()
         _check(lib().hbx_ctx_create(device, ctypes.byref(o), ctypes.byref(h)))
         self.h = h

@@ -13,12 +13,18 @@
 #include <algorithm>
 #include <climits>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <filesystem>
+#include <fstream>
 #include <functional>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
+
+#include <unistd.h>
 
 #include "encode.h"
 #include "hbx_core.h"
@@ -84,6 +90,7 @@ struct DBuf {
 
 struct RuleBufs {
   DBuf<uint32_t> key_l, key_r, cnt_l, cnt_r, off_l, off_r, cur_l, cur_r, sorted_l, sorted_r;
+  DBuf<dev::StrMeta> sorted_meta_r;
   DBuf<unsigned long long> item_off;
   DBuf<uint32_t> part_u32;
   DBuf<unsigned long long> part_u64;
@@ -95,7 +102,7 @@ struct SideBufs {
   DBuf<uint32_t> bucket;
   DBuf<int32_t> eq, comp;
   DBuf<uint8_t> arena;
-  DBuf<uint4> meta;
+  DBuf<dev::StrMeta> meta;
 };
 
 template <class T>
@@ -124,8 +131,9 @@ struct hbx_session {
   hbx::dev::Side side_l{}, side_r{};
   uint32_t warp_words = 4;
   uint32_t tile_right = 128;
-  uint32_t list_off = 0;
-  uint32_t queue_off = 0;
+  hbx::dev::WarpLayout wl{};
+  int variant = 0;  // evaluation kernel: 0 = k_eval, 1 = k_eval_wide
+  bool tuned = false;
   int blocks_per_sm = 1;
   size_t smem_bytes = 0;
   cudaGraphExec_t graph = nullptr;
@@ -156,6 +164,72 @@ int row_grid(uint64_t n, int n_sm) {
   return (int)std::max<uint64_t>(1, std::min<uint64_t>(g, (uint64_t)n_sm * 8));
 }
 
+// Tile shape and kernel variant of a session: right rows per work item
+// (tile_right) and the evaluation kernel (0: 3 CTAs per SM, 1: 2 CTAs per SM
+// with more registers).  Lays out each warp's shared memory (Peq tables per
+// similarity predicate, then dev::warp_layout), uploads the rule descriptors,
+// raises the kernel's shared-memory limit if needed and drops the graph.
+void configure(hbx_session* S, uint32_t tile_right, int variant) {
+  hbx_ctx* C = S->ctx;
+  const Encoded& E = S->E;
+  S->tile_right = std::min<uint32_t>(2048, std::max<uint32_t>(32, (tile_right + 31) / 32 * 32));
+  S->variant = variant ? 1 : 0;
+  const dev::EvalKernel kern = dev::eval_kernel(S->variant);
+  const uint32_t NS = E.n_symbols;
+  const size_t smem_cap = std::min<size_t>(C->smem_optin, 200 * 1024);
+  const uint32_t cap_warp_words = (uint32_t)(smem_cap / 4 / dev::kWarpsPerCta) / 4 * 4;
+  const uint32_t fixed_words = dev::warp_layout_fixed_words(S->tile_right);
+  if (fixed_words + 4 > cap_warp_words) fail(HBX_ERR_INVALID_ARG, "tile_right too large");
+  const uint32_t max_warp_words = cap_warp_words - fixed_words;
+  uint32_t warp_words = 4;
+  for (size_t r = 0; r < E.rules.size(); r++) {
+    const RuleEnc& re = E.rules[r];
+    dev::Rule& d = S->h_rules[r];
+    uint32_t off = 0;
+    for (size_t s = 0; s < re.sim_slot_l.size(); s++) {
+      const uint32_t mx = std::min<uint32_t>(E.L.str_maxlen[(size_t)re.sim_slot_l[s]], kFastMaxLen);
+      const uint32_t S32 = mx ? (uint32_t)dev::row_words((int)((mx + 31) / 32)) : 0u;
+      const uint32_t words = (NS * S32 + 3) / 4 * 4;
+      if (S32 && off + words <= max_warp_words) {
+        d.peq_rows_words[s] = S32;
+        d.peq_off[s] = off;
+        off += words;
+      } else {
+        d.peq_rows_words[s] = 0;  // evaluated by the exact per-lane path
+        d.peq_off[s] = 0;
+      }
+    }
+    warp_words = std::max(warp_words, off);
+  }
+  S->wl = dev::warp_layout(warp_words, S->tile_right);
+  S->warp_words = S->wl.warp_words;
+  // every warp region lies inside the dynamic allocation
+  S->smem_bytes = (size_t)S->warp_words * 4 * dev::kWarpsPerCta;
+  if (warp_words % 4 || S->warp_words > cap_warp_words)
+    fail(HBX_ERR_CUDA, "shared-memory layout exceeds its allocation");
+  HBX_CUDA(cudaMemcpyAsync(S->d_rules.p, S->h_rules.data(), S->h_rules.size() * sizeof(dev::Rule),
+                           cudaMemcpyHostToDevice, C->stream));
+  HBX_CUDA(cudaStreamSynchronize(C->stream));
+  {
+    // The limit belongs to the kernel, process-wide: only ever raise it, so a
+    // session needing less never lowers it under another live session.
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lock(mu);
+    cudaFuncAttributes fa;
+    HBX_CUDA(cudaFuncGetAttributes(&fa, kern));
+    if ((size_t)fa.maxDynamicSharedSizeBytes < S->smem_bytes)
+      HBX_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)S->smem_bytes));
+  }
+  int bps = 0;
+  HBX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, kThreads, S->smem_bytes));
+  S->blocks_per_sm = std::max(1, bps);
+  if (S->graph) {
+    cudaGraphExecDestroy(S->graph);
+    S->graph = nullptr;
+  }
+}
+
 void setup_session(hbx_session* S) {
   hbx_ctx* C = S->ctx;
   const Encoded& E = S->E;
@@ -166,19 +240,18 @@ void setup_session(hbx_session* S) {
     sb.eq.upload(flatten(se.eq_codes, (size_t)n), st);
     sb.comp.upload(flatten(se.comp_codes, (size_t)n), st);
     sb.arena.upload(se.arena, st);
-    // per string: {offset / 16, length, first 8 symbols (0 past the end)}
-    std::vector<uint4> meta;
+    // per string: {offset / 16, length}, first 16 symbols (0 past the end)
+    std::vector<dev::StrMeta> meta;
     meta.reserve(se.str_off.size() * (size_t)n);
     for (size_t slot = 0; slot < se.str_off.size(); slot++)
       for (uint32_t i = 0; i < n; i++) {
         const uint32_t off = se.str_off[slot][i], len = se.str_len[slot][i];
-        uint8_t pre[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        for (uint32_t k = 0; k < 8 && k < len; k++) pre[k] = se.arena[(size_t)off * 16 + k];
-        uint4 m;
-        m.x = off;
-        m.y = len;
-        m.z = (uint32_t)pre[0] | (uint32_t)pre[1] << 8 | (uint32_t)pre[2] << 16 | (uint32_t)pre[3] << 24;
-        m.w = (uint32_t)pre[4] | (uint32_t)pre[5] << 8 | (uint32_t)pre[6] << 16 | (uint32_t)pre[7] << 24;
+        uint32_t w[4] = {0, 0, 0, 0};
+        for (uint32_t k = 0; k < 16 && k < len; k++)
+          w[k / 4] |= (uint32_t)se.arena[(size_t)off * 16 + k] << (8 * (k % 4));
+        dev::StrMeta m;
+        m.loc = make_uint4(off, len, 0, 0);
+        m.head = make_uint4(w[0], w[1], w[2], w[3]);
         meta.push_back(m);
       }
     sb.meta.upload(meta, st);
@@ -193,18 +266,7 @@ void setup_session(hbx_session* S) {
   up_side(E.L, S->L, S->side_l, nL);
   up_side(E.R, S->R, S->side_r, nR);
 
-  // shared-memory Peq tables: per rule, per similarity predicate
-  const uint32_t NS = E.n_symbols;
-  const size_t smem_cap = std::min<size_t>(C->smem_optin, 200 * 1024);
-  if (C->opts.tile_right > 0) S->tile_right = (uint32_t)C->opts.tile_right;
-  S->tile_right = std::min<uint32_t>(2048, std::max<uint32_t>(32, (S->tile_right + 31) / 32 * 32));
-  const uint32_t cap_warp_words = (uint32_t)(smem_cap / 4 / dev::kWarpsPerCta) / 4 * 4;
-  // per warp: Peq tables, then a row list (tile_right words) and the scan
-  // ring (kRingEntries x 16 bytes)
-  const uint32_t list_queue_words = S->tile_right + 4 * dev::kRingEntries;
-  if (list_queue_words + 4 > cap_warp_words) fail(HBX_ERR_INVALID_ARG, "tile_right too large");
-  const uint32_t max_warp_words = cap_warp_words - list_queue_words;
-  uint32_t warp_words = 4;
+  // join state of every rule (independent of the tile shape)
   S->rb.clear();
   S->rb.resize(E.rules.size());
   S->h_rules.assign(E.rules.size(), dev::Rule{});
@@ -219,24 +281,11 @@ void setup_session(hbx_session* S) {
       d.eq_slot[e] = (uint32_t)re.eq_slot[e];
       d.radix[e] = re.radix[e];
     }
-    uint32_t off = 0;
     for (size_t s = 0; s < re.sim_slot_l.size(); s++) {
       d.sim_l[s] = (uint32_t)re.sim_slot_l[s];
       d.sim_r[s] = (uint32_t)re.sim_slot_r[s];
       d.thr[s] = re.thr[s];
-      const uint32_t mx = std::min<uint32_t>(E.L.str_maxlen[(size_t)re.sim_slot_l[s]], kFastMaxLen);
-      const uint32_t S32 = mx ? (uint32_t)dev::row_words((int)((mx + 31) / 32)) : 0u;
-      const uint32_t words = (NS * S32 + 3) / 4 * 4;
-      if (S32 && off + words <= max_warp_words) {
-        d.peq_rows_words[s] = S32;
-        d.peq_off[s] = off;
-        off += words;
-      } else {
-        d.peq_rows_words[s] = 0;  // evaluated by the exact per-lane path
-        d.peq_off[s] = 0;
-      }
     }
-    warp_words = std::max(warp_words, off);
     d.domain = (uint32_t)re.domain;
     // group left rows by the word class of the first similarity predicate's
     // string, unless that would make the left key domain too large
@@ -255,7 +304,8 @@ void setup_session(hbx_session* S) {
     b.cur_l.alloc(d.domain_l);
     b.cur_r.alloc(re.domain);
     b.sorted_l.alloc(nL);
-    b.sorted_r.alloc(nR);
+    b.sorted_r.alloc((size_t)nR + 4);
+    if (d.n_sim) b.sorted_meta_r.alloc(nR);
     b.item_off.alloc((size_t)d.domain_l + 1);
     b.nb = (uint32_t)((re.domain + dev::kScanChunk - 1) / dev::kScanChunk);
     b.nb_l = (uint32_t)((d.domain_l + dev::kScanChunk - 1) / dev::kScanChunk);
@@ -272,33 +322,14 @@ void setup_session(hbx_session* S) {
     d.item_off = b.item_off.p;
     d.sorted_l = b.sorted_l.p;
     d.sorted_r = b.sorted_r.p;
+    d.sorted_meta_r = d.n_sim ? b.sorted_meta_r.p : nullptr;
   }
-  // each warp's row list and scan ring follow its Peq tables
-  S->list_off = warp_words;
-  S->queue_off = warp_words + S->tile_right;
-  S->warp_words = S->queue_off + 4 * dev::kRingEntries;
-  S->d_rules.upload(S->h_rules, st);
+  S->d_rules.alloc(E.rules.size());
   S->d_rule_base.alloc(E.rules.size() + 1);
   S->d_ctr.alloc(1);
-  // every warp region (Peq tables + queue) lies inside the dynamic allocation
-  S->smem_bytes = (size_t)S->warp_words * 4 * dev::kWarpsPerCta;
-  if (S->queue_off % 4 || S->queue_off + 4 * dev::kRingEntries > S->warp_words ||
-      S->warp_words > cap_warp_words)
-    fail(HBX_ERR_CUDA, "shared-memory layout exceeds its allocation");
-  {
-    // The limit belongs to the kernel, process-wide: only ever raise it, so a
-    // session needing less never lowers it under another live session.
-    static std::mutex mu;
-    std::lock_guard<std::mutex> lock(mu);
-    cudaFuncAttributes fa;
-    HBX_CUDA(cudaFuncGetAttributes(&fa, dev::k_eval));
-    if ((size_t)fa.maxDynamicSharedSizeBytes < S->smem_bytes)
-      HBX_CUDA(cudaFuncSetAttribute(dev::k_eval, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)S->smem_bytes));
-  }
-  int bps = 0;
-  HBX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, dev::k_eval, kThreads, S->smem_bytes));
-  S->blocks_per_sm = std::max(1, bps);
+  const uint32_t tile = C->opts.tile_right > 0 ? (uint32_t)C->opts.tile_right : 128u;
+  const int variant = C->opts.eval_variant > 0 ? C->opts.eval_variant - 1 : 0;
+  configure(S, tile, variant);
 
   // partition boundaries of every rule's left key space, per word class
   // (plain form): entry (rule, class, p) = first left key of partition p
@@ -320,7 +351,8 @@ void setup_session(hbx_session* S) {
   HBX_CUDA(cudaEventCreate(&S->ev_eval1));
   uint64_t h2d = 0;
   for (const SideBufs* sb : {&S->L, &S->R})
-    h2d += sb->bucket.n * 4 + sb->eq.n * 4 + sb->comp.n * 4 + sb->arena.n + sb->meta.n * 16;
+    h2d += sb->bucket.n * 4 + sb->eq.n * 4 + sb->comp.n * 4 + sb->arena.n +
+           sb->meta.n * sizeof(dev::StrMeta);
   h2d += S->d_rules.n * sizeof(dev::Rule) + S->bound_idx.n * 4;
   S->stats.h2d_bytes = h2d;
   HBX_CUDA(cudaStreamSynchronize(st));
@@ -383,8 +415,10 @@ dev::EvalParams eval_params(hbx_session* S) {
   P.rule_item_base = S->d_rule_base.p;
   P.tile_right = S->tile_right;
   P.warp_words = S->warp_words;
-  P.list_off = S->list_off;
-  P.queue_off = S->queue_off;
+  P.queue_off = S->wl.queue_off;
+  P.stage_meta_off = S->wl.stage_meta_off;
+  P.stage_rows_off = S->wl.stage_rows_off;
+  P.mbar_off = S->wl.mbar_off;
   P.out_l = S->out_l.p;
   P.out_r = S->out_r.p;
   P.capacity = S->out_l.n;
@@ -400,12 +434,17 @@ uint32_t enqueue_batched(hbx_session* S, cudaStream_t st) {
   dev::EvalParams P = eval_params(S);
   P.n_seg = 0;  // every work item of every rule
   const int grid = S->ctx->n_sm * S->blocks_per_sm;
-  // External: inside stream capture a plain record would only be a capture
-  // dependency marker; this makes it an event-record node that can be timed.
-  HBX_CUDA(cudaEventRecordWithFlags(S->ev_eval0, st, cudaEventRecordExternal));
-  dev::k_eval<<<grid, kThreads, S->smem_bytes, st>>>(P);
+  // Inside stream capture a plain record would only be a capture dependency
+  // marker; the external flag makes it an event-record node that can be
+  // timed (the flag is refused outside capture).
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  HBX_CUDA(cudaStreamIsCapturing(st, &cap));
+  const unsigned rec_flags =
+      cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
+  HBX_CUDA(cudaEventRecordWithFlags(S->ev_eval0, st, rec_flags));
+  dev::eval_kernel(S->variant)<<<grid, kThreads, S->smem_bytes, st>>>(P);
   launch_check("k_eval");
-  HBX_CUDA(cudaEventRecordWithFlags(S->ev_eval1, st, cudaEventRecordExternal));
+  HBX_CUDA(cudaEventRecordWithFlags(S->ev_eval1, st, rec_flags));
   return launches + 1;
 }
 
@@ -498,7 +537,7 @@ dev::Counters run_once(hbx_session* S, hbx_mode mode, cudaStream_t st, uint32_t*
       HBX_CUDA(cudaMemsetAsync(&S->d_ctr.p->work_next, 0, sizeof(unsigned long long), st));
       const unsigned long long ctas = (n_items + dev::kWarpsPerCta - 1) / dev::kWarpsPerCta;
       const int grid = (int)std::min<unsigned long long>(ctas, (unsigned long long)max_grid);
-      dev::k_eval<<<grid, kThreads, S->smem_bytes, st>>>(P);
+      dev::eval_kernel(S->variant)<<<grid, kThreads, S->smem_bytes, st>>>(P);
       n++;
       launch_check("k_eval (plain)");
     }
@@ -509,10 +548,137 @@ dev::Counters run_once(hbx_session* S, hbx_mode mode, cudaStream_t st, uint32_t*
   return read_counters(S, st);
 }
 
+// ---- tile-shape autotuner ---------------------------------------------------
+// The first batched run of a session whose tile shape or kernel variant is
+// left to the engine (hbx_opts.tile_right == 0 or eval_variant == 0) times
+// each candidate (right rows per work item x evaluation kernel) on the
+// session's own data and keeps the fastest.  Choices are cached in a JSON
+// file (HBX_AUTOTUNE_CACHE, default $HOME/.cache/hbx_autotune.json) under a
+// signature of the device and the workload's shape, so later sessions of the
+// same shape skip the search.
+
+std::string autotune_path() {
+  if (const char* p = std::getenv("HBX_AUTOTUNE_CACHE")) return p;
+  const char* home = std::getenv("HOME");
+  return std::string(home ? home : "/tmp") + "/.cache/hbx_autotune.json";
+}
+
+std::string workload_signature(const hbx_session* S) {
+  cudaDeviceProp prop;
+  std::string sig;
+  if (cudaGetDeviceProperties(&prop, S->ctx->device) == cudaSuccess) sig = prop.name;
+  auto bucket = [](uint64_t n) {  // power-of-two bucket
+    uint32_t b = 0;
+    while ((1ull << b) < n) b++;
+    return b;
+  };
+  sig += "|L" + std::to_string(bucket(S->E.L.n_rows)) + "|R" + std::to_string(bucket(S->E.R.n_rows)) +
+         "|P" + std::to_string(bucket(S->E.n_partitions)) + "|S" + std::to_string(S->E.n_symbols);
+  for (const RuleEnc& re : S->E.rules) {
+    sig += "|e" + std::to_string(re.eq_slot.size()) + "s" + std::to_string(re.sim_slot_l.size());
+    if (!re.sim_slot_l.empty())
+      sig += "w" + std::to_string((S->E.L.str_maxlen[(size_t)re.sim_slot_l[0]] + 31) / 32) + "d" +
+             std::to_string(bucket(re.domain));
+  }
+  for (auto& ch : sig)
+    if (ch == '"' || ch == '\\') ch = '_';
+  return sig;
+}
+
+// The cache file holds one entry per line:  "<signature>": [tile_right, variant, ms],
+std::map<std::string, std::string> load_autotune_cache(const std::string& path) {
+  std::map<std::string, std::string> m;
+  std::ifstream f(path);
+  std::string line;
+  while (std::getline(f, line)) {
+    const size_t a = line.find('"'), b = line.find("\": [");
+    const size_t e = line.find(']', b == std::string::npos ? 0 : b);
+    if (a == std::string::npos || b == std::string::npos || e == std::string::npos) continue;
+    m[line.substr(a + 1, b - a - 1)] = line.substr(b + 4, e - b - 4);
+  }
+  return m;
+}
+
+void save_autotune_cache(const std::string& path, const std::map<std::string, std::string>& m) {
+  const size_t slash = path.rfind('/');
+  if (slash != std::string::npos) {
+    std::error_code ec;
+    std::filesystem::create_directories(path.substr(0, slash), ec);
+  }
+  const std::string tmp = path + ".tmp" + std::to_string((long)getpid());
+  {
+    std::ofstream f(tmp);
+    if (!f) return;  // a cache that cannot be written is not an error
+    f << "{\n";
+    size_t k = 0;
+    for (auto& kv : m) f << "  \"" << kv.first << "\": [" << kv.second << "]" << (++k < m.size() ? "," : "") << "\n";
+    f << "}\n";
+  }
+  std::rename(tmp.c_str(), path.c_str());
+}
+
+// One batched run without a graph; returns its device time in ms.
+float timed_batched_run(hbx_session* S, cudaStream_t st) {
+  HBX_CUDA(cudaEventRecord(S->ev0, st));
+  enqueue_batched(S, st);
+  HBX_CUDA(cudaEventRecord(S->ev1, st));
+  HBX_CUDA(cudaEventSynchronize(S->ev1));
+  float ms = 0;
+  HBX_CUDA(cudaEventElapsedTime(&ms, S->ev0, S->ev1));
+  return ms;
+}
+
+void autotune(hbx_session* S, cudaStream_t st) {
+  S->tuned = true;
+  const hbx_opts& o = S->ctx->opts;
+  if (o.tile_right > 0 && o.eval_variant > 0) return;
+  const std::string path = autotune_path(), sig = workload_signature(S);
+  std::map<std::string, std::string> cache = load_autotune_cache(path);
+  auto hit = cache.find(sig);
+  if (hit != cache.end()) {
+    unsigned tr = 0;
+    int v = 0;
+    float ms = 0;
+    if (std::sscanf(hit->second.c_str(), "%u, %d, %f", &tr, &v, &ms) == 3 && tr >= 32) {
+      configure(S, o.tile_right > 0 ? (uint32_t)o.tile_right : tr,
+                o.eval_variant > 0 ? o.eval_variant - 1 : v);
+      return;
+    }
+  }
+  std::vector<uint32_t> tiles = {64, 128, 256};
+  std::vector<int> variants = {0, 1};
+  if (o.tile_right > 0) tiles = {(uint32_t)o.tile_right};
+  if (o.eval_variant > 0) variants = {o.eval_variant - 1};
+  float best = 1e30f;
+  uint32_t best_tr = tiles[0];
+  int best_v = variants[0];
+  for (uint32_t tr : tiles)
+    for (int v : variants) {
+      configure(S, tr, v);
+      timed_batched_run(S, st);  // warm: caches, and the output buffer size
+      const dev::Counters c = read_counters(S, st);
+      if (c.out_count > S->out_l.n || c.seen_overflow)
+        grow_output(S, std::max<uint64_t>(c.out_count + c.seen_overflow, S->out_l.n + 1));
+      const float ms = std::min(timed_batched_run(S, st), timed_batched_run(S, st));
+      if (ms < best) {
+        best = ms;
+        best_tr = tr;
+        best_v = v;
+      }
+    }
+  configure(S, best_tr, best_v);
+  char buf[64];
+  std::snprintf(buf, sizeof buf, "%u, %d, %.4f", best_tr, best_v, best);
+  cache[sig] = buf;
+  save_autotune_cache(path, cache);
+}
+
 }  // namespace
 
 void session_run(hbx_session* S, hbx_mode mode, cudaStream_t st) {
   HBX_CUDA(cudaSetDevice(S->ctx->device));
+  if (!S->tuned && mode == HBX_MODE_BATCHED) autotune(S, st);
+
   uint32_t launches = 0;
   for (int attempt = 0; attempt < 8; attempt++) {
     HBX_CUDA(cudaEventRecord(S->ev0, st));

@@ -26,7 +26,7 @@ __global__ void k_keys_hist(Side S, const Rule* rules, uint32_t rule, int side) 
   for (uint32_t row = blockIdx.x * blockDim.x + threadIdx.x; row < S.n_rows;
        row += gridDim.x * blockDim.x) {
     uint32_t k = row_key(S, R, row);
-    if (split) k += R.domain * word_class(S.str_meta[(size_t)R.wclass_slot * S.n_rows + row].y);
+    if (split) k += R.domain * word_class(S.str_meta[(size_t)R.wclass_slot * S.n_rows + row].loc.y);
     keys[row] = k;
     atomicAdd(cnt + k, 1u);
   }
@@ -38,10 +38,14 @@ __global__ void k_scatter(Side S, const Rule* rules, uint32_t rule, int side) {
   const uint32_t* off = side ? R.off_r : R.off_l;
   uint32_t* cur = side ? R.cur_r : R.cur_l;
   uint32_t* sorted = side ? R.sorted_r : R.sorted_l;
+  StrMeta* meta_out = side ? R.sorted_meta_r : nullptr;
+  const StrMeta* meta_in = S.str_meta + (size_t)R.sim_r[0] * S.n_rows;
   for (uint32_t row = blockIdx.x * blockDim.x + threadIdx.x; row < S.n_rows;
        row += gridDim.x * blockDim.x) {
     const uint32_t k = keys[row];
-    sorted[off[k] + atomicAdd(cur + k, 1u)] = row;
+    const uint32_t pos = off[k] + atomicAdd(cur + k, 1u);
+    sorted[pos] = row;
+    if (meta_out) meta_out[pos] = meta_in[row];
   }
 }
 
@@ -407,22 +411,20 @@ __device__ __forceinline__ bool jw_decide(uint32_t m, uint32_t ls, uint32_t ll, 
 __device__ __forceinline__ int m_need_lo(uint32_t ls, uint32_t ll, uint32_t p, float thr) {
   if (p >= 10u) return 0;
   const float c = 0.1f * (float)p;
-  const float jn = (thr - c) / (1.0f - c);
-  const float mr = (3.0f * jn - 1.0f) / (1.0f / (float)ls + 1.0f / (float)ll);
+  // __fdividef errs by at most 2 ulp: a few 1e-5 matches at most, far inside
+  // the 0.05 margin below
+  const float jn = __fdividef(thr - c, 1.0f - c);
+  const float mr = __fdividef(3.0f * jn - 1.0f, __frcp_rn((float)ls) + __frcp_rn((float)ll));
   const float v = ceilf(mr - 0.05f);
   if (!(v > 0.0f)) return 0;
   return v > 1.0e6f ? 1000000 : (int)v;
 }
 
-// Slow exact similarity check of one pair (any lengths).
-__device__ __noinline__ bool sim_pass_slow(const Side& L, const Side& R, uint32_t slot_l,
-                                           uint32_t slot_r, uint32_t lrow, uint32_t rrow, float thr,
-                                           Counters* ctr) {
-  const uint4 ma = L.str_meta[(size_t)slot_l * L.n_rows + lrow];
-  const uint4 mb = R.str_meta[(size_t)slot_r * R.n_rows + rrow];
-  const uint32_t la = ma.y, lb = mb.y;
-  const uint8_t* a = L.arena + 16ull * ma.x;
-  const uint8_t* b = R.arena + 16ull * mb.x;
+// Slow exact similarity check of one pair (any lengths).  Out of line and
+// with plain pointer/scalar arguments only: passing the kernel parameters by
+// reference would copy them into local memory for the whole kernel.
+__device__ __noinline__ bool sim_pass_slow(const uint8_t* a, uint32_t la, const uint8_t* b,
+                                           uint32_t lb, float thr, Counters* ctr) {
   if (la == 0 || lb == 0) return jw_exact(0, la, lb, 0, thr, &ctr->ambiguous);
   const uint32_t mn = min(la, lb);
   if (mn > 256) atomicAdd(&ctr->long_pairs, 1ull);
@@ -499,17 +501,18 @@ struct Stage {
   const uint32_t* tab;      // Peq table of the left string (shared memory)
   const uint8_t* a;         // left string (symbols, 16-byte aligned)
   uint32_t la;
-  uint32_t a_pre0, a_pre1;  // its first 8 symbols
+  uint4 a_head;             // its first 16 symbols
   float thr;
   uint32_t slot_r;          // string slot of the right column
-  const uint32_t* list_g;   // first stage: right rows in global memory, else null
-  uint32_t* list_s;         // later stages read their rows here; survivors go here
-  uint4* q;                 // ring (kRing) of pairs to scan: {row, offset/16, length, p<<16|need}
+  uint32_t* rows;           // right rows of the input list (shared memory); survivors
+                            // are written back over consumed entries
+  const StrMeta* meta;      // first stage: the rows' staged string metadata, else null
+  uint4* q;                 // ring of pairs to scan, 2 x uint4 per entry:
+                            // {row, offset/16, length, p << 16 | need}, first 16 symbols
   uint32_t n;               // rows in the input list
   bool last;                // survivors are final matches
 };
 
-// Emits final matches of one warp step with one atomic per warp.
 // First report of a pair?  With several rules a pair can match more than one
 // of them (the reference stops at the first rule that passes,
 // global_func.cuh:161-165); a device hash set of emitted (left, right) keys
@@ -531,6 +534,7 @@ __device__ __forceinline__ bool first_report(const EvalParams& P, uint32_t lrow,
   return false;
 }
 
+// Emits final matches of one warp step with one atomic per warp.
 __device__ __forceinline__ void emit(const EvalParams& P, bool pass, uint32_t lrow, uint32_t rrow,
                                      int lane) {
   if (pass && P.seen) pass = first_report(P, lrow, rrow);
@@ -548,61 +552,69 @@ __device__ __forceinline__ void emit(const EvalParams& P, bool pass, uint32_t lr
   }
 }
 
-// Passes of one warp step: final (dedup + emit) or into the next stage's list.
-__device__ __forceinline__ void route(const EvalParams& P, const Stage& A, bool pass, uint32_t r,
-                                      uint32_t lrow, uint32_t rrow, int lane, uint32_t* lw) {
+// Passes of one warp step: final (dedup + emit) or into the next stage's list,
+// written over list entries that have already been read.
+__device__ __forceinline__ void route(const EvalParams& P, const Stage& A, bool pass, uint32_t lrow,
+                                      uint32_t rrow, int lane, uint32_t* lw) {
   if (A.last) {
     emit(P, pass, lrow, rrow, lane);
   } else {
     const unsigned pm = __ballot_sync(kFull, pass);
-    if (pass) A.list_s[*lw + __popc(pm & ((1u << lane) - 1u))] = rrow;
+    if (pass) A.rows[*lw + __popc(pm & ((1u << lane) - 1u))] = rrow;
     *lw += __popc(pm);
   }
 }
 
-// Common prefix of two 8-symbol little-endian prefixes; 8 when they agree.
-__device__ __forceinline__ uint32_t prefix8(uint32_t a0, uint32_t a1, uint32_t b0, uint32_t b1) {
-  uint32_t d = a0 ^ b0;
-  if (d) return (uint32_t)(__ffs(d) - 1) >> 3;
-  d = a1 ^ b1;
-  if (d) return 4u + ((uint32_t)(__ffs(d) - 1) >> 3);
-  return 8u;
+// Common prefix of two 16-symbol little-endian heads; 16 when they agree.
+__device__ __forceinline__ uint32_t prefix16(const uint4& a, const uint4& b) {
+  const uint32_t d[4] = {a.x ^ b.x, a.y ^ b.y, a.z ^ b.z, a.w ^ b.w};
+#pragma unroll
+  for (int k = 0; k < 4; k++)
+    if (d[k]) return 4u * k + ((uint32_t)(__ffs(d[k]) - 1) >> 3);
+  return 16u;
 }
 
 constexpr uint32_t kPrefixUnknown = 0xffu;
 constexpr uint32_t kRing = kRingEntries;  // per-warp ring of pairs waiting for a scan
 
-// Filter one batch of 32 input rows: one 16-byte metadata load per right row
-// gives its length and first 8 symbols, hence the common prefix p (when below
-// 8) and the match count the threshold needs; rows that cannot reach it are
-// decided here, the rest are appended to the ring of pairs to scan.
-// Empty right strings are decided here too.  Returns the rows appended.
+// Filter one batch of 32 input rows: one 32-byte metadata record per right row
+// gives its length and first 16 symbols, hence the common prefix p (when below
+// 16) and the match count the threshold needs; rows that cannot reach it are
+// decided here, the rest are appended to the ring of pairs to scan together
+// with their first 16 symbols.  Empty right strings are decided here too.
+// Returns the rows appended.
 __device__ __forceinline__ uint32_t filter_batch(const EvalParams& P, const Stage& A, uint32_t e0,
-                                                 uint32_t tail, uint32_t r, uint32_t lrow,
-                                                 uint32_t* lw, unsigned long long* ops) {
+                                                 uint32_t tail, uint32_t lrow, uint32_t* lw,
+                                                 unsigned long long* ops) {
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
   const uint32_t nR = P.R.n_rows;
   const uint32_t e = e0 + (uint32_t)lane;
   const bool act = e < A.n;
-  const uint32_t rrow = act ? (A.list_g ? A.list_g[e] : A.list_s[e]) : 0u;
-  const uint4 m = act ? P.R.str_meta[(size_t)A.slot_r * nR + rrow] : make_uint4(0, 0, 0, 0);
+  const uint32_t rrow = act ? A.rows[e] : 0u;
+  StrMeta m;
+  if (act) {
+    m = A.meta ? A.meta[e] : P.R.str_meta[(size_t)A.slot_r * nR + rrow];
+  } else {
+    m.loc = make_uint4(0, 0, 0, 0);
+    m.head = make_uint4(0, 0, 0, 0);
+  }
   bool pass = false, scan = false;
   uint32_t p = 0;
   int need = 0;
   if (act) {
-    const uint32_t lb = m.y;
+    const uint32_t lb = m.loc.y;
     if (lb == 0) {
       pass = jw_exact(0, A.la, 0, 0, A.thr, &P.ctr->ambiguous);
     } else {
       const uint32_t ls = min(A.la, lb), ll = max(A.la, lb);
       *ops += jw_eval_ops(ls, ll);
-      const uint32_t p8 = prefix8(A.a_pre0, A.a_pre1, m.z, m.w);
-      if (p8 == 8u && ls > 8u) {
-        scan = true;  // prefix longer than 8: measured exactly before the scan
+      const uint32_t p16 = prefix16(A.a_head, m.head);
+      if (p16 == 16u && ls > 16u) {
+        scan = true;  // prefix longer than 16: measured exactly before the scan
         p = kPrefixUnknown;
       } else {
-        p = min(p8, ls);
+        p = min(p16, ls);
         need = m_need_lo(ls, ll, p, A.thr);
         const uint32_t n_iter = min(lb, A.la + ((ls + 1u) >> 1));
         scan = need <= (int)min(n_iter, ls);  // else the threshold is out of reach
@@ -610,23 +622,27 @@ __device__ __forceinline__ uint32_t filter_batch(const EvalParams& P, const Stag
     }
   }
   const unsigned qm = __ballot_sync(kFull, scan);
-  if (scan)
-    A.q[(tail + __popc(qm & lt)) & (kRing - 1)] =
-        make_uint4(rrow, m.x, m.y, (p << 16) | (uint32_t)need);
-  route(P, A, pass, r, lrow, rrow, lane, lw);
+  if (scan) {
+    const uint32_t slot = (tail + __popc(qm & lt)) & (kRing - 1);
+    A.q[2 * slot] = make_uint4(rrow, m.loc.x, m.loc.y, (p << 16) | (uint32_t)need);
+    A.q[2 * slot + 1] = m.head;
+  }
+  route(P, A, pass, lrow, rrow, lane, lw);
   return __popc(qm);
 }
 
 // One similarity stage of one work item.  Lanes take the next queued pair as
-// soon as theirs is decided, and the queue is refilled by filter batches as
-// it drains, so lanes stay busy whatever the strings' lengths and however
-// many rows the filter drops.  Every loop turn scans one 4-character word for
-// every busy lane; a pair stops as soon as even matching every remaining
-// character stays below its bound.  Survivors go to the next stage's row
-// list (or out, in the last stage); returns their count.
+// soon as theirs is decided, and the ring is refilled by filter batches as it
+// drains, so lanes stay busy whatever the strings' lengths and however many
+// rows the filter drops.  A pair starts from the 16 symbols the ring carries
+// and loads each next 16-symbol chunk one chunk ahead, so scans do not wait on
+// memory.  Every loop turn scans one 4-symbol word for every busy lane; every
+// 16 symbols a pair stops once even matching every remaining symbol stays
+// below its bound.  Survivors go to the next stage's row list (or out, in the
+// last stage); returns their count.
 template <int W>
-__device__ __noinline__ uint32_t run_stage(const EvalParams& P, const Stage& A, uint32_t r,
-                                           uint32_t lrow, unsigned long long* ops) {
+__device__ __forceinline__ uint32_t run_stage(const EvalParams& P, const Stage& A, uint32_t lrow,
+                                           unsigned long long* ops) {
   constexpr int S = row_words(W);
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
@@ -635,7 +651,7 @@ __device__ __noinline__ uint32_t run_stage(const EvalParams& P, const Stage& A, 
   uint32_t rrow = 0, ls = 0, ll = 0, i = 0, n_iter = 0, h = 0, p = 0;
   int allowed = 0;
   const uint8_t* b = nullptr;
-  uint32_t c0 = 0, c1 = 0, c2 = 0, c3 = 0;
+  uint4 cur = make_uint4(0, 0, 0, 0), nxt = make_uint4(0, 0, 0, 0);
   uint32_t win[W], mt[W];
 #pragma unroll
   for (int k = 0; k < W; k++) win[k] = mt[k] = 0u;
@@ -644,14 +660,16 @@ __device__ __noinline__ uint32_t run_stage(const EvalParams& P, const Stage& A, 
     const uint32_t n_idle = __popc(idle);
     // refill the ring until it holds a pair for every idle lane
     while (tail - head < n_idle && in_pos < A.n && tail - head <= kRing - 32) {
-      tail += filter_batch(P, A, in_pos, tail, r, lrow, &lw, ops);
+      tail += filter_batch(P, A, in_pos, tail, lrow, &lw, ops);
       in_pos += 32;
     }
     bool fin = false, pass = false;
     const uint32_t avail = tail - head;
     const uint32_t rank = __popc(idle & lt);
     if (!busy && rank < avail) {
-      const uint4 qe = A.q[(head + rank) & (kRing - 1)];
+      const uint32_t slot = (head + rank) & (kRing - 1);
+      const uint4 qe = A.q[2 * slot];
+      cur = A.q[2 * slot + 1];
       rrow = qe.x;
       b = P.R.arena + 16ull * qe.y;
       const uint32_t lb = qe.z;
@@ -671,6 +689,7 @@ __device__ __noinline__ uint32_t run_stage(const EvalParams& P, const Stage& A, 
         allowed = (int)n_iter - need;
         i = 0;
         busy = true;
+        if (n_iter > 16u) nxt = __ldg(reinterpret_cast<const uint4*>(b + 16));
 #pragma unroll
         for (int k = 0; k < W; k++) {
           const int nb = (int)h + 1 - 32 * k;
@@ -681,17 +700,15 @@ __device__ __noinline__ uint32_t run_stage(const EvalParams& P, const Stage& A, 
     }
     head += min(n_idle, avail);
     if (busy) {
-      if ((i & 15u) == 0) {
-        const uint4 v = __ldg(reinterpret_cast<const uint4*>(b + i));
-        c0 = v.x;
-        c1 = v.y;
-        c2 = v.z;
-        c3 = v.w;
+      if ((i & 15u) == 0 && i) {
+        // chunk i/16 arrived one chunk ago; ask for the one after it
+        cur = nxt;
+        if (i + 16u < n_iter) nxt = __ldg(reinterpret_cast<const uint4*>(b + i + 16u));
       }
-      const uint32_t wd = c0;
-      c0 = c1;
-      c1 = c2;
-      c2 = c3;
+      const uint32_t wd = cur.x;
+      cur.x = cur.y;
+      cur.y = cur.z;
+      cur.z = cur.w;
 #pragma unroll
       for (int c = 0; c < 4; c++)
         bp_step<W, S>(A.tab, (wd >> (8 * c)) & 0xffu, win, mt, (i + (uint32_t)c) < h ? 1u : 0u);
@@ -705,12 +722,12 @@ __device__ __noinline__ uint32_t run_stage(const EvalParams& P, const Stage& A, 
           busy = false;
           pass = jw_decide(m, ls, ll, p, A.thr, &P.ctr->ambiguous);
         } else if ((int)(i - m) > allowed) {
-          fin = true;  // even matching every remaining character stays below
+          fin = true;  // even matching every remaining symbol stays below
           busy = false;
         }
       }
     }
-    route(P, A, fin && pass, r, lrow, rrow, lane, &lw);
+    route(P, A, fin && pass, lrow, rrow, lane, &lw);
     if (!__any_sync(kFull, busy) && head == tail && in_pos >= A.n) break;
   }
   __syncwarp();
@@ -719,37 +736,35 @@ __device__ __noinline__ uint32_t run_stage(const EvalParams& P, const Stage& A, 
 
 // Stage over a left string the fast path does not take (longer than 256
 // bytes, or no room for its table): the reference's own loops per lane.
-__device__ __noinline__ uint32_t run_stage_slow(const EvalParams& P, const Stage& A, uint32_t s_l,
-                                                uint32_t r, uint32_t lrow,
-                                                unsigned long long* ops) {
+__device__ __forceinline__ uint32_t run_stage_slow(const EvalParams& P, const Stage& A,
+                                                   unsigned long long* ops, uint32_t lrow) {
   const int lane = threadIdx.x & 31;
   uint32_t lw = 0;
   for (uint32_t e0 = 0; e0 < A.n; e0 += 32) {
     const uint32_t e = e0 + (uint32_t)lane;
     const bool act = e < A.n;
-    const uint32_t rrow = act ? (A.list_g ? A.list_g[e] : A.list_s[e]) : 0u;
+    const uint32_t rrow = act ? A.rows[e] : 0u;
     bool pass = false;
     if (act) {
-      const uint32_t lb = P.R.str_meta[(size_t)A.slot_r * P.R.n_rows + rrow].y;
-      if (lb && A.la) *ops += jw_eval_ops(min(A.la, lb), max(A.la, lb));
-      pass = sim_pass_slow(P.L, P.R, s_l, A.slot_r, lrow, rrow, A.thr, P.ctr);
+      const uint4 mb = P.R.str_meta[(size_t)A.slot_r * P.R.n_rows + rrow].loc;
+      if (mb.y && A.la) *ops += jw_eval_ops(min(A.la, mb.y), max(A.la, mb.y));
+      pass = sim_pass_slow(A.a, A.la, P.R.arena + 16ull * mb.x, mb.y, A.thr, P.ctr);
     }
     __syncwarp();
-    route(P, A, pass, r, lrow, rrow, lane, &lw);
+    route(P, A, pass, lrow, rrow, lane, &lw);
   }
   __syncwarp();
   return lw;
 }
 
 __device__ __forceinline__ uint32_t stage_dispatch(uint32_t W, const EvalParams& P, const Stage& A,
-                                                   uint32_t r, uint32_t lrow,
-                                                   unsigned long long* ops) {
+                                                   uint32_t lrow, unsigned long long* ops) {
   switch (W) {
-    case 1: return run_stage<1>(P, A, r, lrow, ops);
-    case 2: return run_stage<2>(P, A, r, lrow, ops);
-    case 3: return run_stage<3>(P, A, r, lrow, ops);
-    case 4: return run_stage<4>(P, A, r, lrow, ops);
-    default: return run_stage<8>(P, A, r, lrow, ops);
+    case 1: return run_stage<1>(P, A, lrow, ops);
+    case 2: return run_stage<2>(P, A, lrow, ops);
+    case 3: return run_stage<3>(P, A, lrow, ops);
+    case 4: return run_stage<4>(P, A, lrow, ops);
+    default: return run_stage<8>(P, A, lrow, ops);
   }
 }
 
@@ -764,13 +779,68 @@ __device__ __forceinline__ unsigned long long seg_item(const EvalParams& P, unsi
   return ~0ull;
 }
 
-__global__ void __launch_bounds__(kWarpsPerCta * 32, 3) k_eval(EvalParams P) {
+// ---- bulk copies (TMA) into shared memory, completed on an mbarrier --------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile(
+      "{\n\t.reg .b64 st;\n\t"
+      "mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(smem_u32(bar)),
+      "r"(bytes)
+      : "memory");
+}
+
+// Global -> shared bulk copy: both addresses 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Waits for the phase with the given parity, at most kMaxWaitSpins tries
+// (each try suspends the thread for a while).  false = gave up.
+constexpr uint32_t kMaxWaitSpins = 1u << 22;
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (uint32_t k = 0; k < kMaxWaitSpins; k++)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+// The evaluation kernel body, instantiated twice below with different
+// register budgets (see k_eval / k_eval_wide).
+__device__ __forceinline__ void eval_body(const EvalParams& P) {
   extern __shared__ __align__(16) uint32_t smem[];
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   uint32_t* region = smem + (size_t)warp * P.warp_words;
-  uint32_t* list_s = region + P.list_off;
   uint4* q = reinterpret_cast<uint4*>(region + P.queue_off);
+  StrMeta* st_meta = reinterpret_cast<StrMeta*>(region + P.stage_meta_off);
+  uint32_t* st_rows = region + P.stage_rows_off;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(region + P.mbar_off);
+  if (lane == 0) mbar_init(bar);
+  __syncwarp();
+  uint32_t phase = 0;
   unsigned long long n_work = 0;  // length of this launch's work list
   if (P.n_seg == 0) {
     n_work = P.rule_item_base[P.n_rules];
@@ -821,44 +891,85 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, 3) k_eval(EvalParams P) {
         emit(P, idx < rb1, lrow, rrow, lane);
       }
     } else {
+      // stage the item's right rows and their string metadata (two contiguous,
+      // 16-byte aligned blocks) with bulk copies while the Peq table is built
+      const uint32_t a0 = rb0 & ~3u;
+      if (lane == 0) {
+        const uint32_t mbytes = (rb1 - rb0) * (uint32_t)sizeof(StrMeta);
+        const uint32_t rbytes = ((rb1 - a0) * 4u + 15u) & ~15u;
+        // the previous item's reads of these buffers are done (__syncwarp);
+        // order them before the asynchronous writes
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(bar, mbytes + rbytes);
+        bulk_g2s(st_meta, R.sorted_meta_r + rb0, mbytes, bar);
+        bulk_g2s(st_rows, R.sorted_r + a0, rbytes, bar);
+      }
+      bool staged = false;
       Stage A;
-      A.list_g = R.sorted_r + rb0;
-      A.list_s = list_s;
+      A.rows = st_rows + (rb0 - a0);
+      A.meta = st_meta;
       A.q = q;
       A.n = rb1 - rb0;
       for (uint32_t s = 0; s < R.n_sim && A.n > 0; s++) {
         const uint32_t sl = R.sim_l[s];
-        const uint4 am = P.L.str_meta[(size_t)sl * P.L.n_rows + lrow];
-        A.la = am.y;
-        A.a = P.L.arena + 16ull * am.x;
-        A.a_pre0 = am.z;
-        A.a_pre1 = am.w;
+        const StrMeta am = P.L.str_meta[(size_t)sl * P.L.n_rows + lrow];
+        A.la = am.loc.y;
+        A.a = P.L.arena + 16ull * am.loc.x;
+        A.a_head = am.head;
         A.thr = R.thr[s];
         A.slot_r = R.sim_r[s];
         A.last = s + 1 == R.n_sim;
         const uint32_t W = (A.la + 31u) >> 5;
         const bool fast =
             A.la > 0 && A.la <= 256 && R.peq_rows_words[s] >= (uint32_t)row_words((int)W);
+        uint32_t* tab = region + R.peq_off[s];
+        if (fast) build_peq(tab, (uint32_t)row_words((int)W), P.n_symbols, A.a, A.la, lane);
+        if (!staged) {
+          staged = true;
+          const bool ok = mbar_wait(bar, phase);
+          phase ^= 1u;
+          if (!__all_sync(kFull, ok)) {
+            // the copy never completed: report, wait (bounded) for it, stop
+            if (lane == 0) atomicAdd(&P.ctr->watchdog_trips, 1ull);
+            mbar_wait(bar, phase ^ 1u);
+            goto out;
+          }
+        }
         uint32_t n_next;
         if (fast) {
-          uint32_t* tab = region + R.peq_off[s];
-          build_peq(tab, (uint32_t)row_words((int)W), P.n_symbols, A.a, A.la, lane);
           A.tab = tab;
-          n_next = stage_dispatch(W, P, A, r, lrow, &ops);
+          n_next = stage_dispatch(W, P, A, lrow, &ops);
         } else {
-          n_next = run_stage_slow(P, A, sl, r, lrow, &ops);
+          n_next = run_stage_slow(P, A, &ops, lrow);
         }
-        A.list_g = nullptr;
+        A.meta = nullptr;  // later stages: survivors kept in A.rows
         A.n = n_next;
       }
+      if (!staged) {  // no stage ran: still consume the phase of this item's copies
+        const bool ok = mbar_wait(bar, phase);
+        phase ^= 1u;
+        if (!__all_sync(kFull, ok)) {
+          if (lane == 0) atomicAdd(&P.ctr->watchdog_trips, 1ull);
+          goto out;
+        }
+      }
+      __syncwarp();
     }
     done++;
   }
+out:
   if (lane == 0 && done) atomicAdd(&P.ctr->items_done, done);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) ops += __shfl_down_sync(kFull, ops, o);
   if (lane == 0 && ops) atomicAdd(&P.ctr->jw_word_ops, ops);
 }
+
+// Dense variant: 3 CTAs (24 warps) per SM, at most 85 registers per thread.
+__global__ void __launch_bounds__(kWarpsPerCta * 32, 3) k_eval(EvalParams P) { eval_body(P); }
+
+// Wide variant: 2 CTAs (16 warps) per SM, up to 128 registers per thread, so
+// the longer-string scan variants keep their state in registers.
+__global__ void __launch_bounds__(kWarpsPerCta * 32, 2) k_eval_wide(EvalParams P) { eval_body(P); }
 
 }  // namespace dev
 }  // namespace hbx

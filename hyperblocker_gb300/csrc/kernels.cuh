@@ -46,14 +46,20 @@ constexpr int kWarpsPerCta = 8;
 __host__ __device__ constexpr int row_words(int w) { return w <= 1 ? 1 : w <= 2 ? 2 : w <= 4 ? 4 : 8; }
 constexpr float kDecisionMargin = 1e-4f;  // |approx JW - thr| below this -> exact path
 
+// Metadata of one string: where it is, how long, and its first 16 symbols
+// (0 past the end), so that one 32-byte load gives the length, the common
+// prefix with another string (up to 16) and the first chunk of a scan.
+struct __align__(16) StrMeta {
+  uint4 loc;   // {offset / 16, length, 0, 0}
+  uint4 head;  // symbols 0-3, 4-7, 8-11, 12-15 (little endian)
+};
+
 struct Side {
   const uint32_t* bucket;
   const int32_t* eq_codes;    // [n_eq_slots][n_rows]
   const int32_t* comp_codes;  // [n_comp][n_rows]
   const uint8_t* arena;       // symbol strings, 16-byte aligned, zero padded
-  // [n_str_slots][n_rows]: {offset / 16, length, symbols 0-3, symbols 4-7}
-  // (symbols past the end of the string are 0)
-  const uint4* str_meta;
+  const StrMeta* str_meta;    // [n_str_slots][n_rows]
   uint32_t n_rows;
 };
 
@@ -83,12 +89,42 @@ struct Rule {
   uint32_t* cur_r;
   unsigned long long* item_off;  // [domain_l + 1]
   uint32_t* sorted_l;
-  uint32_t* sorted_r;
+  uint32_t* sorted_r;  // [n_rows + 4]: the tail pads 16-byte bulk copies
+  // right-row string metadata of the first similarity predicate in sorted_r
+  // order, so that a work item's metadata is one contiguous, 16-byte-aligned
+  // block for a bulk copy into shared memory (null without similarities)
+  StrMeta* sorted_meta_r;
 };
 
 constexpr uint32_t kWordClasses = 5;
 constexpr uint32_t kMaxSegments = 8;
 constexpr uint32_t kRingEntries = 64;
+
+// Shared memory of one warp of k_eval, in 32-bit words: the Peq tables
+// (peq_words, a multiple of 4), then the scan ring (kRingEntries x 32 bytes),
+// the staged item metadata (tile_right x 32 bytes), the staged item rows
+// (tile_right + 8: a 16-byte-aligned copy starts up to 3 rows early and rounds
+// up; the same words then hold the rows that survive each stage) and one
+// mbarrier.  Every offset is a multiple of 4 words (16 bytes) when tile_right
+// is a multiple of 32.
+struct WarpLayout {
+  uint32_t queue_off, stage_meta_off, stage_rows_off, mbar_off, warp_words;
+};
+
+inline WarpLayout warp_layout(uint32_t peq_words, uint32_t tile_right) {
+  WarpLayout w;
+  w.queue_off = peq_words;
+  w.stage_meta_off = w.queue_off + 8 * kRingEntries;
+  w.stage_rows_off = w.stage_meta_off + 8 * tile_right;
+  w.mbar_off = w.stage_rows_off + tile_right + 8;
+  w.warp_words = w.mbar_off + 4;
+  return w;
+}
+
+// Words of a warp's layout that do not depend on the Peq tables.
+inline uint32_t warp_layout_fixed_words(uint32_t tile_right) {
+  return warp_layout(0, tile_right).warp_words;
+}
 
 __host__ __device__ inline uint32_t word_class(uint32_t len) {
   const uint32_t w = (len + 31u) >> 5;
@@ -120,9 +156,11 @@ struct EvalParams {
   unsigned long long seg_begin[kMaxSegments];
   unsigned long long seg_end[kMaxSegments];
   uint32_t tile_right;  // TR
-  uint32_t warp_words;  // shared-memory words per warp: Peq tables, row list, scan ring
-  uint32_t list_off;    // word offset of the warp's row list (tile_right words)
-  uint32_t queue_off;   // word offset of the warp's scan ring (kRingEntries x uint4)
+  uint32_t warp_words;      // shared-memory words per warp (see warp_layout)
+  uint32_t queue_off;       // word offset of the warp's scan ring
+  uint32_t stage_meta_off;  // word offset of the staged item metadata
+  uint32_t stage_rows_off;  // word offset of the staged item rows / survivor list
+  uint32_t mbar_off;        // word offset of the warp's mbarrier (8-byte aligned)
   uint32_t* out_l;
   uint32_t* out_r;
   unsigned long long capacity;
@@ -147,7 +185,11 @@ __global__ void k_items_final(const Rule* rules, uint32_t rule, uint32_t tile_ri
                               const unsigned long long* partial);
 __global__ void k_rule_base(const Rule* rules, uint32_t n_rules, unsigned long long* base);
 // ------------------------------------------------------------------ evaluation
-__global__ void k_eval(EvalParams P);
+__global__ void k_eval(EvalParams P);       // 3 CTAs per SM (register-limited)
+__global__ void k_eval_wide(EvalParams P);  // 2 CTAs per SM (more registers)
+
+using EvalKernel = void (*)(EvalParams);
+inline EvalKernel eval_kernel(int wide) { return wide ? k_eval_wide : k_eval; }
 
 constexpr uint32_t kScanChunk = 4096;  // elements per CTA in the scans (1024 threads x 4)
 

@@ -91,16 +91,19 @@ std::vector<T> flat(const std::vector<std::vector<T>>& v) {
   return out;
 }
 
-std::vector<uint4> string_meta(const hbx::SideEnc& se, uint32_t n) {
-  std::vector<uint4> meta;
+std::vector<hbx::dev::StrMeta> string_meta(const hbx::SideEnc& se, uint32_t n) {
+  std::vector<hbx::dev::StrMeta> meta;
   meta.reserve(se.str_off.size() * (size_t)n);
   for (size_t slot = 0; slot < se.str_off.size(); slot++)
     for (uint32_t i = 0; i < n; i++) {
       const uint32_t off = se.str_off[slot][i], len = se.str_len[slot][i];
-      uint32_t pre[2] = {0, 0};
-      for (uint32_t k = 0; k < 8 && k < len; k++)
-        pre[k / 4] |= (uint32_t)se.arena[(size_t)off * 16 + k] << (8 * (k % 4));
-      meta.push_back(make_uint4(off, len, pre[0], pre[1]));
+      uint32_t w[4] = {0, 0, 0, 0};
+      for (uint32_t k = 0; k < 16 && k < len; k++)
+        w[k / 4] |= (uint32_t)se.arena[(size_t)off * 16 + k] << (8 * (k % 4));
+      hbx::dev::StrMeta m;
+      m.loc = make_uint4(off, len, 0, 0);
+      m.head = make_uint4(w[0], w[1], w[2], w[3]);
+      meta.push_back(m);
     }
   return meta;
 }
@@ -116,28 +119,29 @@ struct Layout {
   unsigned long long seen_slots = 0;
   uint32_t* part_u32 = nullptr;
   unsigned long long* part_u64 = nullptr;
-  uint32_t warp_words = 0, list_off = 0, queue_off = 0, tile_right = 128;
+  hbx::dev::WarpLayout wl{};
+  uint32_t tile_right = 128;
 };
 
 // Places every buffer; with c.base == nullptr it only measures.
 void place(Carve& c, const hbx::Encoded& E, uint64_t capacity, size_t smem_cap, Layout* Y,
-           const std::vector<uint4>& ml, const std::vector<uint4>& mr) {
+           const std::vector<hbx::dev::StrMeta>& ml, const std::vector<hbx::dev::StrMeta>& mr) {
   namespace dev = hbx::dev;
   const uint32_t nL = (uint32_t)E.L.n_rows, nR = (uint32_t)E.R.n_rows;
-  auto side = [&](const hbx::SideEnc& se, dev::Side& ds, uint32_t n, const std::vector<uint4>& m) {
+  auto side = [&](const hbx::SideEnc& se, dev::Side& ds, uint32_t n,
+                  const std::vector<dev::StrMeta>& m) {
     ds.bucket = c.take<uint32_t>(n);
     ds.eq_codes = c.take<int32_t>(se.eq_codes.size() * (size_t)n);
     ds.comp_codes = c.take<int32_t>(se.comp_codes.size() * (size_t)n);
     ds.arena = c.take<uint8_t>(se.arena.size());
-    ds.str_meta = c.take<uint4>(m.size());
+    ds.str_meta = c.take<dev::StrMeta>(m.size());
     ds.n_rows = n;
   };
   side(E.L, Y->L, nL, ml);
   side(E.R, Y->R, nR, mr);
   const uint32_t NS = E.n_symbols;
   const uint32_t cap_warp_words = (uint32_t)(smem_cap / 4 / dev::kWarpsPerCta) / 4 * 4;
-  const uint32_t list_queue_words = Y->tile_right + 4 * dev::kRingEntries;
-  const uint32_t max_warp_words = cap_warp_words - list_queue_words;
+  const uint32_t max_warp_words = cap_warp_words - dev::warp_layout_fixed_words(Y->tile_right);
   uint32_t warp_words = 4;
   Y->rules.assign(E.rules.size(), dev::Rule{});
   Y->nb.assign(E.rules.size(), 0);
@@ -185,14 +189,13 @@ void place(Carve& c, const hbx::Encoded& E, uint64_t capacity, size_t smem_cap, 
     d.cur_r = c.take<uint32_t>(d.domain);
     d.item_off = c.take<unsigned long long>((size_t)d.domain_l + 1);
     d.sorted_l = c.take<uint32_t>(nL);
-    d.sorted_r = c.take<uint32_t>(nR);
+    d.sorted_r = c.take<uint32_t>((size_t)nR + 4);
+    d.sorted_meta_r = d.n_sim ? c.take<dev::StrMeta>(nR) : nullptr;
     Y->nb[r] = (d.domain + dev::kScanChunk - 1) / dev::kScanChunk;
     Y->nb_l[r] = (d.domain_l + dev::kScanChunk - 1) / dev::kScanChunk;
     max_nb = std::max(max_nb, std::max(Y->nb[r], Y->nb_l[r]));
   }
-  Y->list_off = warp_words;
-  Y->queue_off = warp_words + Y->tile_right;
-  Y->warp_words = Y->queue_off + 4 * dev::kRingEntries;
+  Y->wl = dev::warp_layout(warp_words, Y->tile_right);
   Y->part_u32 = c.take<uint32_t>(max_nb);
   Y->part_u64 = c.take<unsigned long long>(max_nb);
   Y->d_rules = c.take<dev::Rule>(E.rules.size());
@@ -220,7 +223,7 @@ void run_static(int device, const hbx_plan* plan, const hbx_table* left, const h
     hbx::fail(HBX_ERR_INVALID_ARG, "null output pointer");
   const hbx::Encoded E = hbx::encode(plan->p, left->t, right->t, n_partitions, prefix_idx);
   const uint32_t nL = (uint32_t)E.L.n_rows, nR = (uint32_t)E.R.n_rows;
-  const std::vector<uint4> ml = string_meta(E.L, nL), mr = string_meta(E.R, nR);
+  const std::vector<hbx::dev::StrMeta> ml = string_meta(E.L, nL), mr = string_meta(E.R, nR);
 
   cudaDeviceProp prop;
   HBX_STATIC_CUDA(cudaGetDeviceProperties(&prop, device));
@@ -246,13 +249,14 @@ void run_static(int device, const hbx_plan* plan, const hbx_table* left, const h
   auto up = [&](void* dst, const void* src, size_t bytes) {
     if (bytes) HBX_STATIC_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
   };
-  auto up_side = [&](const hbx::SideEnc& se, const dev::Side& ds, const std::vector<uint4>& m) {
+  auto up_side = [&](const hbx::SideEnc& se, const dev::Side& ds,
+                     const std::vector<dev::StrMeta>& m) {
     up((void*)ds.bucket, se.bucket.data(), se.bucket.size() * 4);
     const std::vector<int32_t> eq = flat(se.eq_codes), comp = flat(se.comp_codes);
     up((void*)ds.eq_codes, eq.data(), eq.size() * 4);
     up((void*)ds.comp_codes, comp.data(), comp.size() * 4);
     up((void*)ds.arena, se.arena.data(), se.arena.size());
-    up((void*)ds.str_meta, m.data(), m.size() * sizeof(uint4));
+    up((void*)ds.str_meta, m.data(), m.size() * sizeof(dev::StrMeta));
     HBX_STATIC_CUDA(cudaStreamSynchronize(st));  // host vectors of this scope end here
   };
   up_side(E.L, Y.L, ml);
@@ -300,16 +304,18 @@ void run_static(int device, const hbx_plan* plan, const hbx_table* left, const h
   P.rule_item_base = Y.rule_base;
   P.n_seg = 0;
   P.tile_right = Y.tile_right;
-  P.warp_words = Y.warp_words;
-  P.list_off = Y.list_off;
-  P.queue_off = Y.queue_off;
+  P.warp_words = Y.wl.warp_words;
+  P.queue_off = Y.wl.queue_off;
+  P.stage_meta_off = Y.wl.stage_meta_off;
+  P.stage_rows_off = Y.wl.stage_rows_off;
+  P.mbar_off = Y.wl.mbar_off;
   P.out_l = out->l_row;
   P.out_r = out->r_row;
   P.capacity = out->capacity;
   P.ctr = Y.ctr;
   P.seen = Y.seen;
   P.seen_mask = Y.seen ? Y.seen_slots - 1 : 0;
-  const size_t smem = (size_t)Y.warp_words * 4 * dev::kWarpsPerCta;
+  const size_t smem = (size_t)Y.wl.warp_words * 4 * dev::kWarpsPerCta;
   {
     static std::mutex mu;
     std::lock_guard<std::mutex> lock(mu);

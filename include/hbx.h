@@ -69,8 +69,9 @@ typedef struct hbx_server hbx_server;
 typedef struct hbx_opts {
   uint32_t struct_size;      /* sizeof(hbx_opts) */
   int32_t use_graph;         /* batched mode replays a CUDA graph (default 1) */
-  int32_t tile_right;        /* right rows per tile, 0 = autotuned/default */
-  int32_t warps_per_cta;     /* left rows per tile, 0 = autotuned/default */
+  int32_t tile_right;        /* right rows per work item, 0 = autotuned */
+  int32_t eval_variant;      /* evaluation kernel: 1 = 3 CTAs/SM, 2 = 2 CTAs/SM with more
+                                registers, 0 = autotuned */
   uint64_t watchdog_cycles;  /* per-CTA SM-cycle budget of the persistent loop, 0 = none */
 } hbx_opts;
 

@@ -16,6 +16,11 @@ if ROOT not in sys.path:
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and the built libhbx.so")
+    # the tile-shape autotuner's cache goes to a private file during tests
+    import tempfile
+
+    os.environ.setdefault("HBX_AUTOTUNE_CACHE",
+                          os.path.join(tempfile.mkdtemp(prefix="hbx_tests_"), "autotune.json"))
 
 
 @pytest.fixture(scope="session")

@@ -165,3 +165,32 @@ def test_cli_drop_in(built, golden, tmp_path):
     r = subprocess.run(cmd + ["-hbx_mode=plain"], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     assert len(open(out, "rb").read().splitlines()) == 2 * len(lines)  # append mode
+
+
+@pytest.mark.parametrize("tile", [32, 64, 256])
+@pytest.mark.parametrize("variant", [1, 2])
+def test_tile_shapes_and_kernel_variants_agree(built, tile, variant):
+    """Every tile shape and both evaluation kernels give the oracle's pairs."""
+    cl, cr = _util.random_tables(500 + tile, 80, 400, b"abcdefgh ,", 150)
+    docs = [synth.rule_yaml([3], [(1, 0.7)]), synth.rule_yaml([4], [(2, 0.6), (1, 0.5)])]
+    want = api.run_block(api.CTable(cl), api.CTable(cr), _oracle_plan(docs), 2)
+    c = hb.Context(0, tile_right=tile, eval_variant=variant)
+    for mode in MODES:
+        got, st = _engine_pairs(c, docs, cl, cr, 2, _util.INT_MAX, mode)
+        assert np.array_equal(got, want.pairs), (tile, variant, mode)
+    c.close()
+
+
+def test_autotuner_choice_is_cached_and_exact(built, tmp_path, monkeypatch):
+    cache = tmp_path / "tune.json"
+    monkeypatch.setenv("HBX_AUTOTUNE_CACHE", str(cache))
+    cl, cr = _util.random_tables(77, 200, 600, b"abcdefgh ,", 90)
+    docs = [synth.rule_yaml([3], [(1, 0.7)])]
+    want = api.run_block(api.CTable(cl), api.CTable(cr), _oracle_plan(docs), 1)
+    for _ in range(2):  # first run tunes and writes the cache, second reads it
+        c = hb.Context(0)
+        got, _ = _engine_pairs(c, docs, cl, cr, 1)
+        assert np.array_equal(got, want.pairs)
+        c.close()
+    text = cache.read_text()
+    assert text.startswith("{") and "|L" in text
