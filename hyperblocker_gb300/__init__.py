@@ -50,6 +50,7 @@ class HbxError(RuntimeError):
 class Opts(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_uint32), ("use_graph", ctypes.c_int32),
                 ("tile_right", ctypes.c_int32), ("eval_variant", ctypes.c_int32),
+                ("pred_order", ctypes.c_int32), ("ingest", ctypes.c_int32),
                 ("watchdog_cycles", ctypes.c_uint64)]
 
 
@@ -72,7 +73,8 @@ class Stats(ctypes.Structure):
                 ("n_partitions_used", ctypes.c_uint32), ("n_launches", ctypes.c_uint32),
                 ("ms_last_run", ctypes.c_double), ("ms_join", ctypes.c_double),
                 ("ms_eval", ctypes.c_double), ("jw_word_ops", ctypes.c_uint64),
-                ("h2d_bytes", ctypes.c_uint64)]
+                ("h2d_bytes", ctypes.c_uint64), ("ms_create", ctypes.c_double),
+                ("ingest_on_device", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
     def as_dict(self) -> Dict[str, float]:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -143,9 +145,10 @@ class Context:
     """A CUDA device + stream for the engine (hbx_ctx)."""
 
     def __init__(self, device: int = 0, use_graph: bool = True, tile_right: int = 0,
-                 watchdog_cycles: int = 0, eval_variant: int = 0):
+                 watchdog_cycles: int = 0, eval_variant: int = 0, pred_order: int = 0,
+                 ingest: int = 0):
         o = Opts(ctypes.sizeof(Opts), 1 if use_graph else 0, tile_right, eval_variant,
-                 watchdog_cycles)
+                 pred_order, ingest, watchdog_cycles)
         h = _VP()
         _check(lib().hbx_ctx_create(device, ctypes.byref(o), ctypes.byref(h)))
         self.h = h
@@ -305,8 +308,16 @@ class Session:
 
 
 def block(ctx: Context, plan: Plan, left: Table, right: Table, n_partitions: int = 1,
-          prefix_idx: int = INT_MAX, mode="batched", capacity: int = 1 << 16):
-    """Host tables -> (pairs (n, 2) uint32 of (left row, right row), stats)."""
+          prefix_idx: int = INT_MAX, mode="batched", capacity: Optional[int] = None):
+    """Host tables -> (pairs (n, 2) uint32 of (left row, right row), stats).
+
+    ``hbx_block`` writes nothing when the output buffer is too small (it
+    reports the size needed and the call is repeated), so without an explicit
+    ``capacity`` the buffer is sized from the largest result seen on this
+    context, with a quarter of headroom.
+    """
+    if capacity is None:
+        capacity = getattr(ctx, "_capacity_hint", 1 << 16)
     while True:
         ol = np.empty(max(capacity, 1), dtype=np.uint32)
         orr = np.empty(max(capacity, 1), dtype=np.uint32)
@@ -316,9 +327,12 @@ def block(ctx: Context, plan: Plan, left: Table, right: Table, n_partitions: int
                              ctypes.byref(p), ctypes.byref(s))
         if st == ERR_CAPACITY:
             capacity = int(p.n_required)
+            ctx._capacity_hint = max(getattr(ctx, "_capacity_hint", 0), capacity + capacity // 4)
             continue
         _check(st, ctx.h)
         n = int(p.n_written)
+        if n + n // 4 > getattr(ctx, "_capacity_hint", 1 << 16):
+            ctx._capacity_hint = n + n // 4
         return np.stack([ol[:n], orr[:n]], axis=1), s
 
 

@@ -120,6 +120,7 @@ hbx_status hbx_table_from_csv(hbx_ctx* ctx, const char* path, char sep, hbx_tabl
   if (!path || !out) return HBX_ERR_INVALID_ARG;
   *out = nullptr;
   auto t = std::make_unique<hbx_table>();
+  t->uid = hbx::next_table_uid();
   hbx_status s = guard_host(ctx, [&] { t->t = hbx::table_from_csv(path, sep ? sep : ','); });
   if (s == HBX_OK) *out = t.release();
   return s;
@@ -129,6 +130,7 @@ hbx_status hbx_table_ingest(hbx_ctx* ctx, const hbx_columns* cols, hbx_table** o
   if (!cols || !out) return HBX_ERR_INVALID_ARG;
   *out = nullptr;
   auto t = std::make_unique<hbx_table>();
+  t->uid = hbx::next_table_uid();
   hbx_status s = guard_host(ctx, [&] { t->t = hbx::table_from_columns(cols); });
   if (s == HBX_OK) *out = t.release();
   return s;
@@ -139,6 +141,7 @@ int32_t hbx_table_n_cols(const hbx_table* t) { return t ? t->t.n_cols() : -1; }
 
 hbx_status hbx_table_destroy(hbx_table* t) {
   if (!t) return HBX_ERR_INVALID_ARG;
+  hbx::unpin_table(t);
   delete t;
   return HBX_OK;
 }

@@ -7,6 +7,7 @@
 // the default parameters the reference uses (no trimming, CR dropped, no
 // quoted line breaks, automatic unquoting, UTF-8 BOM skipped) directly into
 // column-major byte arenas instead of a vector<vector<string>>.
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -109,6 +110,7 @@ Table table_from_buffer(const char* data, size_t n, char sep) {
     col.off = std::move(rb.cells_off[(size_t)c]);
     t.cols.push_back(std::move(col));
   }
+  finish_table(&t);
   return t;
 }
 
@@ -144,7 +146,18 @@ Table table_from_columns(const hbx_columns* cols) {
     }
     t.cols.push_back(std::move(col));
   }
+  finish_table(&t);
   return t;
+}
+
+void finish_table(Table* t) {
+  for (Column& c : t->cols)
+    c.has_nul = !c.bytes.empty() && std::memchr(c.bytes.data(), 0, c.bytes.size()) != nullptr;
+}
+
+uint64_t next_table_uid() {
+  static std::atomic<uint64_t> next{1};
+  return next.fetch_add(1);
 }
 
 }  // namespace hbx

@@ -1,0 +1,121 @@
+// device_buffers.h -- owned device buffers of a session.
+//
+// Sessions allocate a few dozen buffers and free them when they end; a
+// one-shot hbx_block call creates and destroys a session every time.  So the
+// buffers come from the context's stream-ordered memory pool (its release
+// threshold is unlimited, so freed memory stays with the pool and the next
+// session's allocations do not reach the driver).  The pool is chosen by a
+// PoolScope on the calling thread for the duration of one C-ABI call; outside
+// any scope a buffer falls back to cudaMalloc.  A buffer remembers where it
+// came from and returns there.
+//
+// Ordering: allocations are ordered on the scope's stream.  Every entry point
+// synchronizes that stream before it returns, and a session frees its buffers
+// only from hbx_session_destroy, when none of its work is in flight.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "hbx_core.h"
+#include "kernels.cuh"
+
+#define HBX_CUDA(expr)                                                                        \
+  do {                                                                                        \
+    cudaError_t e_ = (expr);                                                                  \
+    if (e_ != cudaSuccess)                                                                    \
+      ::hbx::fail(e_ == cudaErrorMemoryAllocation ? HBX_ERR_OOM : HBX_ERR_CUDA,               \
+                  std::string(#expr) + ": " + cudaGetErrorString(e_));                        \
+  } while (0)
+
+namespace hbx {
+
+struct DevPool {
+  cudaMemPool_t pool = nullptr;
+  cudaStream_t stream = nullptr;
+};
+
+// The pool of the C-ABI call running on this thread (null: cudaMalloc).
+inline const DevPool*& current_pool() {
+  thread_local const DevPool* p = nullptr;
+  return p;
+}
+
+struct PoolScope {
+  const DevPool* prev;
+  DevPool mine;
+  PoolScope(cudaMemPool_t pool, cudaStream_t stream) : prev(current_pool()) {
+    mine.pool = pool;
+    mine.stream = stream;
+    current_pool() = pool ? &mine : nullptr;
+  }
+  ~PoolScope() { current_pool() = prev; }
+  PoolScope(const PoolScope&) = delete;
+  PoolScope& operator=(const PoolScope&) = delete;
+};
+
+template <class T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DevPool from{};  // pool and stream of the allocation (pool null: cudaMalloc)
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  DBuf(DBuf&& o) noexcept : p(o.p), n(o.n), from(o.from) {
+    o.p = nullptr;
+    o.n = 0;
+  }
+  DBuf& operator=(DBuf&& o) noexcept {
+    if (this != &o) {
+      reset();
+      p = o.p;
+      n = o.n;
+      from = o.from;
+      o.p = nullptr;
+      o.n = 0;
+    }
+    return *this;
+  }
+  ~DBuf() { reset(); }
+  void reset() {
+    if (p) {
+      if (from.pool)
+        cudaFreeAsync(p, from.stream);
+      else
+        cudaFree(p);
+    }
+    p = nullptr;
+    n = 0;
+  }
+  void alloc(size_t count) {
+    reset();
+    if (count == 0) count = 1;
+    const DevPool* dp = current_pool();
+    if (dp) {
+      HBX_CUDA(cudaMallocFromPoolAsync((void**)&p, count * sizeof(T), dp->pool, dp->stream));
+      from = *dp;
+    } else {
+      HBX_CUDA(cudaMalloc((void**)&p, count * sizeof(T)));
+      from = DevPool{};
+    }
+    n = count;
+  }
+  void upload(const std::vector<T>& v, cudaStream_t s) {
+    alloc(v.size());
+    if (!v.empty())
+      HBX_CUDA(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+  }
+};
+
+// Device copy of one encoded table.
+struct SideBufs {
+  DBuf<uint32_t> bucket;
+  DBuf<int32_t> eq, comp;
+  DBuf<uint8_t> arena;
+  DBuf<dev::StrMeta> meta;
+};
+
+}  // namespace hbx

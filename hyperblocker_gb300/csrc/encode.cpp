@@ -69,39 +69,28 @@ void check_col(const Table& t, int col, const char* side, const char* what) {
 
 }  // namespace
 
-Encoded encode(const Plan& plan, const Table& left, const Table& right, uint64_t n_partitions,
-               int64_t prefix_idx) {
+Encoded encode_schema(const Plan& plan, const Table& left, const Table& right,
+                      uint64_t n_partitions, int64_t prefix_idx) {
   if (n_partitions == 0) fail(HBX_ERR_INVALID_ARG, "n_partitions must be >= 1");
   if (n_partitions > (1ull << 20)) fail(HBX_ERR_UNSUPPORTED, "n_partitions above 2^20");
   if (left.n_rows > (int64_t)UINT32_MAX - 1 || right.n_rows > (int64_t)UINT32_MAX - 1)
     fail(HBX_ERR_UNSUPPORTED, "more than 2^32 - 2 rows in a table");
   Encoded E;
   E.n_partitions = n_partitions;
+  E.prefix_idx = prefix_idx;
   E.L.n_rows = left.n_rows;
   E.R.n_rows = right.n_rows;
 
-  // ---- partition buckets (data_mngr.h:150-202)
-  int part_col = -1;
-  if (!plan.pred_type.empty() && plan.pred_type[0] == 'e') part_col = plan.pred_index[0];
+  // ---- partition key (data_mngr.h:150-202)
+  if (!plan.pred_type.empty() && plan.pred_type[0] == 'e') E.part_col = plan.pred_index[0];
   if (left.n_cols() == 0 || right.n_cols() == 0) fail(HBX_ERR_UNSUPPORTED, "table without columns");
-  if (part_col >= 0) {
-    check_col(left, part_col, "left", "the partition key");
-    check_col(right, part_col, "right", "the partition key");
+  if (E.part_col >= 0) {
+    check_col(left, E.part_col, "left", "the partition key");
+    check_col(right, E.part_col, "right", "the partition key");
   }
   if (prefix_idx != INT_MAX) {
     check_col(left, (int)prefix_idx, "left", "prefix_hash_pred_idx");
     check_col(right, (int)prefix_idx, "right", "prefix_hash_pred_idx");
-  }
-  compute_buckets(left, part_col, n_partitions, prefix_idx, &E.L.bucket);
-  compute_buckets(right, part_col, n_partitions, prefix_idx, &E.R.bucket);
-  {
-    std::vector<uint64_t> hl(n_partitions, 0), hr(n_partitions, 0);
-    for (uint32_t b : E.L.bucket) hl[b]++;
-    for (uint32_t b : E.R.bucket) hr[b]++;
-    for (uint64_t p = 0; p < n_partitions; p++) {
-      E.pairs_covered += hl[p] * hr[p];
-      if (hl[p] && hr[p]) E.n_partitions_used++;
-    }
   }
 
   // ---- columns the rules use; output ids are column 0 of each table
@@ -116,15 +105,68 @@ Encoded encode(const Plan& plan, const Table& left, const Table& right, uint64_t
     }
   }
 
-  // ---- equality slots with joint dictionaries
+  // ---- equality slots (one joint dictionary each) and string slots
   auto eq_slot_of = [&](int cl, int crr) {
     for (size_t s = 0; s < E.eq_slots.size(); s++)
       if (E.eq_slots[s].first == cl && E.eq_slots[s].second == crr) return (int)s;
     E.eq_slots.emplace_back(cl, crr);
     return (int)E.eq_slots.size() - 1;
   };
+  auto str_slot_of = [&](SideEnc& S, int col) {
+    for (size_t s = 0; s < S.str_col.size(); s++)
+      if (S.str_col[s] == col) return (int)s;
+    S.str_col.push_back(col);
+    return (int)S.str_col.size() - 1;
+  };
   for (auto& cr : plan.compiled)
     for (auto& p : cr.eqs) eq_slot_of(p.col_l, p.col_r);
+  for (auto& cr : plan.compiled)
+    for (auto& p : cr.sims) {
+      str_slot_of(E.L, p.col_l);
+      str_slot_of(E.R, p.col_r);
+    }
+  for (auto& cr : plan.compiled) {
+    RuleEnc re;
+    for (auto& p : cr.eqs) re.eq_slot.push_back(eq_slot_of(p.col_l, p.col_r));
+    for (auto& p : cr.sims) {
+      re.sim_slot_l.push_back(str_slot_of(E.L, p.col_l));
+      re.sim_slot_r.push_back(str_slot_of(E.R, p.col_r));
+      re.thr.push_back(p.thr);
+    }
+    E.rules.push_back(std::move(re));
+  }
+  return E;
+}
+
+void encode_rows(const Table& left, const Table& right, Encoded* Ep) {
+  Encoded& E = *Ep;
+  const uint64_t n_partitions = E.n_partitions;
+  for (SideEnc* S : {&E.L, &E.R}) {  // everything below is (re)built from scratch
+    S->comp_codes.clear();
+    S->arena.clear();
+    S->str_off.clear();
+    S->str_len.clear();
+    S->str_maxlen.clear();
+  }
+  compute_buckets(left, E.part_col, n_partitions, E.prefix_idx, &E.L.bucket);
+  compute_buckets(right, E.part_col, n_partitions, E.prefix_idx, &E.R.bucket);
+  {
+    std::vector<uint64_t> hl(n_partitions, 0), hr(n_partitions, 0);
+    for (uint32_t b : E.L.bucket) hl[b]++;
+    for (uint32_t b : E.R.bucket) hr[b]++;
+    E.pairs_covered = 0;
+    E.n_partitions_used = 0;
+    for (uint64_t p = 0; p < n_partitions; p++) {
+      E.pairs_covered += hl[p] * hr[p];
+      if (hl[p] && hr[p]) E.n_partitions_used++;
+    }
+  }
+
+  // ---- joint dictionaries: two cells are equal (equalities_kernel,
+  // device_func.cuh:39-52, compares up to the first NUL) iff their codes are
+  E.L.eq_codes.clear();
+  E.R.eq_codes.clear();
+  E.eq_card.clear();
   for (auto& slot : E.eq_slots) {
     std::unordered_map<std::string_view, int32_t> dict;
     dict.reserve((size_t)(left.n_rows + right.n_rows) / 4 + 16);
@@ -143,18 +185,7 @@ Encoded encode(const Plan& plan, const Table& left, const Table& right, uint64_t
     E.eq_card.push_back((uint32_t)std::max<size_t>(dict.size(), 1));
   }
 
-  // ---- string slots and the symbol alphabet
-  auto str_slot_of = [&](SideEnc& S, int col) {
-    for (size_t s = 0; s < S.str_col.size(); s++)
-      if (S.str_col[s] == col) return (int)s;
-    S.str_col.push_back(col);
-    return (int)S.str_col.size() - 1;
-  };
-  for (auto& cr : plan.compiled)
-    for (auto& p : cr.sims) {
-      str_slot_of(E.L, p.col_l);
-      str_slot_of(E.R, p.col_r);
-    }
+  // ---- the symbol alphabet of the string slots
   uint64_t freq[256] = {0};
   auto count_side = [&](const Table& t, const SideEnc& S) {
     for (int col : S.str_col) {
@@ -204,16 +235,16 @@ Encoded encode(const Plan& plan, const Table& left, const Table& right, uint64_t
   };
   pack_side(left, E.L);
   pack_side(right, E.R);
+}
 
-  // ---- rules: slots, thresholds and join-key domains
-  for (auto& cr : plan.compiled) {
-    RuleEnc re;
-    for (auto& p : cr.eqs) re.eq_slot.push_back(eq_slot_of(p.col_l, p.col_r));
-    for (auto& p : cr.sims) {
-      re.sim_slot_l.push_back(str_slot_of(E.L, p.col_l));
-      re.sim_slot_r.push_back(str_slot_of(E.R, p.col_r));
-      re.thr.push_back(p.thr);
-    }
+bool finish_rules(Encoded* Ep, bool allow_composite) {
+  Encoded& E = *Ep;
+  const uint64_t n_partitions = E.n_partitions;
+  for (RuleEnc& re : E.rules) {
+    re.radix.clear();
+    re.part_key_begin.clear();
+    re.composite = false;
+    re.comp_index = -1;
     // mixed-radix domain
     unsigned __int128 M = 1;
     for (int s : re.eq_slot) {
@@ -224,41 +255,49 @@ Encoded encode(const Plan& plan, const Table& left, const Table& right, uint64_t
     if (D <= kMaxKeyDomain) {
       re.domain = (uint64_t)D;
       for (uint64_t p = 0; p <= n_partitions; p++) re.part_key_begin.push_back(p * (uint64_t)M);
-    } else {
-      // dense ids of the (bucket, codes...) tuples that occur, grouped by bucket
-      re.composite = true;
-      re.comp_index = (int)E.L.comp_codes.size();
-      std::unordered_map<std::string, int32_t> ids;
-      std::vector<uint32_t> id_bucket;
-      std::string key;
-      auto tuple_id = [&](const SideEnc& S, int64_t i) {
-        key.clear();
-        uint32_t b = S.bucket[(size_t)i];
-        key.append((const char*)&b, 4);
-        for (int s : re.eq_slot) key.append((const char*)&S.eq_codes[(size_t)s][(size_t)i], 4);
-        auto it = ids.emplace(key, (int32_t)ids.size());
-        if (it.second) id_bucket.push_back(b);
-        return it.first->second;
-      };
-      std::vector<int32_t> tl((size_t)E.L.n_rows), tr((size_t)E.R.n_rows);
-      for (int64_t i = 0; i < E.L.n_rows; i++) tl[(size_t)i] = tuple_id(E.L, i);
-      for (int64_t i = 0; i < E.R.n_rows; i++) tr[(size_t)i] = tuple_id(E.R, i);
-      std::vector<uint64_t> start(n_partitions + 1, 0);
-      for (uint32_t b : id_bucket) start[b + 1]++;
-      for (uint64_t p = 0; p < n_partitions; p++) start[p + 1] += start[p];
-      std::vector<int32_t> remap(id_bucket.size());
-      std::vector<uint64_t> cur(start.begin(), start.end() - 1);
-      for (size_t k = 0; k < id_bucket.size(); k++) remap[k] = (int32_t)cur[id_bucket[k]]++;
-      for (auto& v : tl) v = remap[(size_t)v];
-      for (auto& v : tr) v = remap[(size_t)v];
-      E.L.comp_codes.push_back(std::move(tl));
-      E.R.comp_codes.push_back(std::move(tr));
-      re.domain = std::max<uint64_t>(id_bucket.size(), 1);
-      re.part_key_begin = start;
-      if (re.domain > (1ull << 31)) fail(HBX_ERR_UNSUPPORTED, "join key domain too large");
+      continue;
     }
-    E.rules.push_back(std::move(re));
+    if (!allow_composite) return false;
+    // dense ids of the (bucket, codes...) tuples that occur, grouped by bucket
+    re.composite = true;
+    re.comp_index = (int)E.L.comp_codes.size();
+    std::unordered_map<std::string, int32_t> ids;
+    std::vector<uint32_t> id_bucket;
+    std::string key;
+    auto tuple_id = [&](const SideEnc& S, int64_t i) {
+      key.clear();
+      uint32_t b = S.bucket[(size_t)i];
+      key.append((const char*)&b, 4);
+      for (int s : re.eq_slot) key.append((const char*)&S.eq_codes[(size_t)s][(size_t)i], 4);
+      auto it = ids.emplace(key, (int32_t)ids.size());
+      if (it.second) id_bucket.push_back(b);
+      return it.first->second;
+    };
+    std::vector<int32_t> tl((size_t)E.L.n_rows), tr((size_t)E.R.n_rows);
+    for (int64_t i = 0; i < E.L.n_rows; i++) tl[(size_t)i] = tuple_id(E.L, i);
+    for (int64_t i = 0; i < E.R.n_rows; i++) tr[(size_t)i] = tuple_id(E.R, i);
+    std::vector<uint64_t> start(n_partitions + 1, 0);
+    for (uint32_t b : id_bucket) start[b + 1]++;
+    for (uint64_t p = 0; p < n_partitions; p++) start[p + 1] += start[p];
+    std::vector<int32_t> remap(id_bucket.size());
+    std::vector<uint64_t> cur(start.begin(), start.end() - 1);
+    for (size_t k = 0; k < id_bucket.size(); k++) remap[k] = (int32_t)cur[id_bucket[k]]++;
+    for (auto& v : tl) v = remap[(size_t)v];
+    for (auto& v : tr) v = remap[(size_t)v];
+    E.L.comp_codes.push_back(std::move(tl));
+    E.R.comp_codes.push_back(std::move(tr));
+    re.domain = std::max<uint64_t>(id_bucket.size(), 1);
+    re.part_key_begin = start;
+    if (re.domain > (1ull << 31)) fail(HBX_ERR_UNSUPPORTED, "join key domain too large");
   }
+  return true;
+}
+
+Encoded encode(const Plan& plan, const Table& left, const Table& right, uint64_t n_partitions,
+               int64_t prefix_idx) {
+  Encoded E = encode_schema(plan, left, right, n_partitions, prefix_idx);
+  encode_rows(left, right, &E);
+  finish_rules(&E, true);
   return E;
 }
 

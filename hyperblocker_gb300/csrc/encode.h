@@ -39,6 +39,8 @@ struct RuleEnc {
 
 struct Encoded {
   uint64_t n_partitions = 1;
+  int part_col = -1;             // column hashed for the partition bucket, -1 = none
+  int64_t prefix_idx = 2147483647;  // column of the first-character hash (INT_MAX = none)
   SideEnc L, R;
   std::vector<std::pair<int, int>> eq_slots;  // (left col, right col)
   std::vector<uint32_t> eq_card;
@@ -49,7 +51,20 @@ struct Encoded {
   uint32_t n_partitions_used = 0;
 };
 
-// Builds the encoding; throws hbx::Error on inputs the reference cannot run.
+// Slots and rules of a plan over two tables, without per-row data: checks the
+// columns, gives each (left column, right column) equality pair a joint
+// dictionary slot and each similarity column a string slot.  Throws
+// hbx::Error on inputs the reference cannot run.
+Encoded encode_schema(const Plan& plan, const Table& left, const Table& right,
+                      uint64_t n_partitions, int64_t prefix_idx);
+// Host encoding of every row: buckets, dictionary codes, symbols, arenas.
+void encode_rows(const Table& left, const Table& right, Encoded* E);
+// Join-key domains from the dictionary sizes.  A rule whose mixed-radix
+// domain exceeds kMaxKeyDomain gets dense composite ids, which are built from
+// the host codes of encode_rows; with allow_composite false such a rule makes
+// this return false instead.
+bool finish_rules(Encoded* E, bool allow_composite);
+// The whole host encoding (schema, rows, domains).
 Encoded encode(const Plan& plan, const Table& left, const Table& right, uint64_t n_partitions,
                int64_t prefix_idx);
 

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <climits>
 #include <cstdio>
 #include <cstdlib>
@@ -26,67 +27,23 @@
 
 #include <unistd.h>
 
+#include "device_buffers.h"
 #include "encode.h"
 #include "hbx_core.h"
+#include "ingest.h"
 #include "kernels.cuh"
-
-#define HBX_CUDA(expr)                                                                        \
-  do {                                                                                        \
-    cudaError_t e_ = (expr);                                                                  \
-    if (e_ != cudaSuccess)                                                                    \
-      ::hbx::fail(e_ == cudaErrorMemoryAllocation ? HBX_ERR_OOM : HBX_ERR_CUDA,               \
-                  std::string(#expr) + ": " + cudaGetErrorString(e_));                        \
-  } while (0)
 
 struct hbx_ctx {
   int device = 0;
   int n_sm = 0;
   size_t smem_optin = 0;
   cudaStream_t stream = nullptr;
+  cudaMemPool_t pool = nullptr;  // device memory of this context's sessions
   hbx_opts opts{};
   std::string err;
 };
 
 namespace hbx {
-
-template <class T>
-struct DBuf {
-  T* p = nullptr;
-  size_t n = 0;
-  DBuf() = default;
-  DBuf(const DBuf&) = delete;
-  DBuf& operator=(const DBuf&) = delete;
-  DBuf(DBuf&& o) noexcept : p(o.p), n(o.n) {
-    o.p = nullptr;
-    o.n = 0;
-  }
-  DBuf& operator=(DBuf&& o) noexcept {
-    if (this != &o) {
-      reset();
-      p = o.p;
-      n = o.n;
-      o.p = nullptr;
-      o.n = 0;
-    }
-    return *this;
-  }
-  ~DBuf() { reset(); }
-  void reset() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    n = 0;
-  }
-  void alloc(size_t count) {
-    reset();
-    if (count == 0) count = 1;
-    HBX_CUDA(cudaMalloc((void**)&p, count * sizeof(T)));
-    n = count;
-  }
-  void upload(const std::vector<T>& v, cudaStream_t s) {
-    alloc(v.size());
-    if (!v.empty()) HBX_CUDA(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
-  }
-};
 
 struct RuleBufs {
   DBuf<uint32_t> key_l, key_r, cnt_l, cnt_r, off_l, off_r, cur_l, cur_r, sorted_l, sorted_r;
@@ -96,13 +53,6 @@ struct RuleBufs {
   DBuf<unsigned long long> part_u64;
   uint32_t nb = 0;    // scan CTAs over the join key domain
   uint32_t nb_l = 0;  // scan CTAs over the left key domain (word classes x keys)
-};
-
-struct SideBufs {
-  DBuf<uint32_t> bucket;
-  DBuf<int32_t> eq, comp;
-  DBuf<uint8_t> arena;
-  DBuf<dev::StrMeta> meta;
 };
 
 template <class T>
@@ -134,6 +84,7 @@ struct hbx_session {
   hbx::dev::WarpLayout wl{};
   int variant = 0;  // evaluation kernel: 0 = k_eval, 1 = k_eval_wide
   bool tuned = false;
+  bool one_shot = false;  // runs once (hbx_block): no graph is captured
   int blocks_per_sm = 1;
   size_t smem_bytes = 0;
   cudaGraphExec_t graph = nullptr;
@@ -230,12 +181,12 @@ void configure(hbx_session* S, uint32_t tile_right, int variant) {
   }
 }
 
-void setup_session(hbx_session* S) {
-  hbx_ctx* C = S->ctx;
+// Uploads the host encoding of both tables (the host ingest path).
+uint64_t upload_host_encoding(hbx_session* S) {
   const Encoded& E = S->E;
-  cudaStream_t st = C->stream;
+  cudaStream_t st = S->ctx->stream;
   const uint32_t nL = (uint32_t)E.L.n_rows, nR = (uint32_t)E.R.n_rows;
-  auto up_side = [&](const SideEnc& se, SideBufs& sb, dev::Side& ds, uint32_t n) {
+  auto up_side = [&](const SideEnc& se, SideBufs& sb, uint32_t n) {
     sb.bucket.upload(se.bucket, st);
     sb.eq.upload(flatten(se.eq_codes, (size_t)n), st);
     sb.comp.upload(flatten(se.comp_codes, (size_t)n), st);
@@ -256,6 +207,23 @@ void setup_session(hbx_session* S) {
       }
     sb.meta.upload(meta, st);
     HBX_CUDA(cudaStreamSynchronize(st));  // the host vector dies at scope end
+  };
+  up_side(E.L, S->L, nL);
+  up_side(E.R, S->R, nR);
+  uint64_t h2d = 0;
+  for (const SideBufs* sb : {&S->L, &S->R})
+    h2d += sb->bucket.n * 4 + sb->eq.n * 4 + sb->comp.n * 4 + sb->arena.n +
+           sb->meta.n * sizeof(dev::StrMeta);
+  return h2d;
+}
+
+// Device state of a session whose side buffers hold the encoded tables.
+void setup_session(hbx_session* S, uint64_t h2d_tables) {
+  hbx_ctx* C = S->ctx;
+  const Encoded& E = S->E;
+  cudaStream_t st = C->stream;
+  const uint32_t nL = (uint32_t)E.L.n_rows, nR = (uint32_t)E.R.n_rows;
+  auto bind = [](const SideBufs& sb, dev::Side& ds, uint32_t n) {
     ds.bucket = sb.bucket.p;
     ds.eq_codes = sb.eq.p;
     ds.comp_codes = sb.comp.p;
@@ -263,8 +231,8 @@ void setup_session(hbx_session* S) {
     ds.str_meta = sb.meta.p;
     ds.n_rows = n;
   };
-  up_side(E.L, S->L, S->side_l, nL);
-  up_side(E.R, S->R, S->side_r, nR);
+  bind(S->L, S->side_l, nL);
+  bind(S->R, S->side_r, nR);
 
   // join state of every rule (independent of the tile shape)
   S->rb.clear();
@@ -349,10 +317,7 @@ void setup_session(hbx_session* S) {
   HBX_CUDA(cudaEventCreate(&S->ev1));
   HBX_CUDA(cudaEventCreate(&S->ev_eval0));
   HBX_CUDA(cudaEventCreate(&S->ev_eval1));
-  uint64_t h2d = 0;
-  for (const SideBufs* sb : {&S->L, &S->R})
-    h2d += sb->bucket.n * 4 + sb->eq.n * 4 + sb->comp.n * 4 + sb->arena.n +
-           sb->meta.n * sizeof(dev::StrMeta);
+  uint64_t h2d = h2d_tables;
   h2d += S->d_rules.n * sizeof(dev::Rule) + S->bound_idx.n * 4;
   S->stats.h2d_bytes = h2d;
   HBX_CUDA(cudaStreamSynchronize(st));
@@ -473,7 +438,7 @@ dev::Counters read_counters(hbx_session* S, cudaStream_t st) {
 
 // One run into the session's own output buffers; returns the counters.
 dev::Counters run_once(hbx_session* S, hbx_mode mode, cudaStream_t st, uint32_t* launches) {
-  const bool use_graph = S->ctx->opts.use_graph != 0;
+  const bool use_graph = S->ctx->opts.use_graph != 0 && !S->one_shot;
   if (mode == HBX_MODE_BATCHED) {
     if (use_graph) {
       if (!S->graph) {
@@ -586,7 +551,7 @@ std::string workload_signature(const hbx_session* S) {
 }
 
 // The cache file holds one entry per line:  "<signature>": [tile_right, variant, ms],
-std::map<std::string, std::string> load_autotune_cache(const std::string& path) {
+std::map<std::string, std::string> read_autotune_file(const std::string& path) {
   std::map<std::string, std::string> m;
   std::ifstream f(path);
   std::string line;
@@ -599,7 +564,28 @@ std::map<std::string, std::string> load_autotune_cache(const std::string& path) 
   return m;
 }
 
+// The file is read once per process and path; later lookups use the copy in
+// memory, which every new choice updates before it is written back.
+std::mutex g_tune_mu;
+std::map<std::string, std::map<std::string, std::string>> g_tune_mem;  // path -> entries
+
+std::map<std::string, std::string> load_autotune_cache(const std::string& path) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  auto it = g_tune_mem.find(path);
+  if (it == g_tune_mem.end()) it = g_tune_mem.emplace(path, read_autotune_file(path)).first;
+  return it->second;
+}
+
+void write_autotune_file(const std::string& path, const std::map<std::string, std::string>& m);
+
 void save_autotune_cache(const std::string& path, const std::map<std::string, std::string>& m) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  std::map<std::string, std::string>& mem = g_tune_mem[path];
+  for (auto& kv : m) mem[kv.first] = kv.second;
+  write_autotune_file(path, mem);
+}
+
+void write_autotune_file(const std::string& path, const std::map<std::string, std::string>& m) {
   const size_t slash = path.rfind('/');
   if (slash != std::string::npos) {
     std::error_code ec;
@@ -675,6 +661,58 @@ void autotune(hbx_session* S, cudaStream_t st) {
 
 }  // namespace
 
+// Encodes the tables (on the device unless hbx_opts.ingest asks for the host
+// encoder, or only the host encoder is exact for the input) and builds the
+// session's device state.  The similarity predicates of each rule run in the
+// order the planner measures for this pair of tables (hbx_opts.pred_order),
+// memoised on the plan.
+void create_session(hbx_session* S, const hbx_plan* plan, const hbx_table* left,
+                    const hbx_table* right, uint64_t n_partitions, int64_t prefix_idx) {
+  hbx_ctx* C = S->ctx;
+  const auto t0 = std::chrono::steady_clock::now();
+  PoolScope scope(C->pool, C->stream);
+  Plan ordered;
+  const Plan* use = &plan->p;
+  if (C->opts.pred_order == 0) {
+    hbx_plan* mp = const_cast<hbx_plan*>(plan);
+    const std::pair<uint64_t, uint64_t> key(left->uid, right->uid);
+    std::vector<CompiledRule> order;
+    bool have = false;
+    {
+      std::lock_guard<std::mutex> lock(mp->order_mu);
+      auto it = mp->order_cache.find(key);
+      if (it != mp->order_cache.end()) {
+        order = it->second;
+        have = true;
+      }
+    }
+    ordered = plan->p;
+    if (have) {
+      ordered.compiled = std::move(order);
+    } else {
+      order_predicates(&ordered, left->t, right->t);
+      std::lock_guard<std::mutex> lock(mp->order_mu);
+      mp->order_cache[key] = ordered.compiled;
+    }
+    use = &ordered;
+  }
+  S->E = encode_schema(*use, left->t, right->t, n_partitions, prefix_idx);
+  bool on_device = false;
+  uint64_t h2d = 0;
+  std::string why;
+  if (C->opts.ingest == 0)
+    on_device = device_encode(left, right, &S->E, &S->L, &S->R, C->n_sm, C->stream, &h2d, &why);
+  if (!on_device) {
+    encode_rows(left->t, right->t, &S->E);
+    finish_rules(&S->E, true);
+    h2d = upload_host_encoding(S);
+  }
+  setup_session(S, h2d);
+  S->stats.ingest_on_device = on_device ? 1u : 0u;
+  S->stats.ms_create =
+      std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
 void session_run(hbx_session* S, hbx_mode mode, cudaStream_t st) {
   HBX_CUDA(cudaSetDevice(S->ctx->device));
   if (!S->tuned && mode == HBX_MODE_BATCHED) autotune(S, st);
@@ -747,6 +785,9 @@ hbx_status hbx_ctx_create(int device, const hbx_opts* opts, hbx_ctx** out) {
   ctx->opts.use_graph = 1;
   if (opts) {
     if (opts->struct_size != sizeof(hbx_opts)) return HBX_ERR_INVALID_ARG;
+    if (opts->pred_order < 0 || opts->pred_order > 1) return HBX_ERR_INVALID_ARG;
+    if (opts->eval_variant < 0 || opts->eval_variant > 2) return HBX_ERR_INVALID_ARG;
+    if (opts->ingest < 0 || opts->ingest > 1) return HBX_ERR_INVALID_ARG;
     ctx->opts = *opts;
   }
   hbx_status s = guard(ctx.get(), [&] {
@@ -760,6 +801,13 @@ hbx_status hbx_ctx_create(int device, const hbx_opts* opts, hbx_ctx** out) {
     ctx->n_sm = prop.multiProcessorCount;
     ctx->smem_optin = prop.sharedMemPerBlockOptin;
     HBX_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    HBX_CUDA(cudaMemPoolCreate(&ctx->pool, &props));
+    uint64_t keep = UINT64_MAX;  // freed blocks stay in the pool for the next session
+    HBX_CUDA(cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep));
   });
   if (s != HBX_OK) return s;
   *out = ctx.release();
@@ -768,6 +816,9 @@ hbx_status hbx_ctx_create(int device, const hbx_opts* opts, hbx_ctx** out) {
 
 hbx_status hbx_ctx_destroy(hbx_ctx* ctx) {
   if (!ctx) return HBX_ERR_INVALID_ARG;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return HBX_OK;
@@ -794,8 +845,7 @@ hbx_status hbx_session_create(hbx_ctx* ctx, const hbx_plan* plan, const hbx_tabl
     if (prefix_idx != INT_MAX && (prefix_idx < 0 || prefix_idx > INT_MAX))
       hbx::fail(HBX_ERR_INVALID_ARG, "prefix_idx out of range");
     HBX_CUDA(cudaSetDevice(ctx->device));
-    S->E = hbx::encode(plan->p, left->t, right->t, n_partitions, prefix_idx);
-    hbx::setup_session(S.get());
+    hbx::create_session(S.get(), plan, left, right, n_partitions, prefix_idx);
   });
   if (st != HBX_OK) return st;
   *out = S.release();
@@ -807,6 +857,7 @@ hbx_status hbx_session_run(hbx_session* s, hbx_mode mode, hbx_pairs* out, void* 
   if (mode != HBX_MODE_PLAIN && mode != HBX_MODE_BATCHED) return HBX_ERR_INVALID_ARG;
   return guard(s->ctx, [&] {
     cudaStream_t st = stream ? (cudaStream_t)stream : s->ctx->stream;
+    hbx::PoolScope scope(s->ctx->pool, st);
     hbx::session_run(s, mode, st);
     const uint64_t n = s->stats.n_matches;
     out->n_required = n;
@@ -839,10 +890,17 @@ hbx_status hbx_block(hbx_ctx* ctx, const hbx_plan* plan, const hbx_table* left,
                      const hbx_table* right, uint64_t n_partitions, int64_t prefix_idx,
                      hbx_mode mode, hbx_pairs* out, hbx_stats* stats) {
   if (!ctx || !out) return HBX_ERR_INVALID_ARG;
-  hbx_session* s = nullptr;
-  hbx_status st = hbx_session_create(ctx, plan, left, right, n_partitions, prefix_idx, &s);
-  if (st != HBX_OK) return st;
-  st = guard(ctx, [&] {
+  if (!plan || !left || !right) return HBX_ERR_INVALID_ARG;
+  auto S = std::make_unique<hbx_session>();
+  S->ctx = ctx;
+  S->one_shot = true;
+  hbx_session* s = S.get();
+  hbx_status st = guard(ctx, [&] {
+    if (prefix_idx != INT_MAX && (prefix_idx < 0 || prefix_idx > INT_MAX))
+      hbx::fail(HBX_ERR_INVALID_ARG, "prefix_idx out of range");
+    HBX_CUDA(cudaSetDevice(ctx->device));
+    hbx::PoolScope scope(ctx->pool, ctx->stream);
+    hbx::create_session(s, plan, left, right, n_partitions, prefix_idx);
     hbx::session_run(s, mode, ctx->stream);
     const uint64_t n = s->stats.n_matches;
     out->n_required = n;
@@ -857,7 +915,7 @@ hbx_status hbx_block(hbx_ctx* ctx, const hbx_plan* plan, const hbx_table* left,
     }
     out->n_written = n;
   });
-  hbx_session_destroy(s);
+  S.reset();
   return st;
 }
 

@@ -2,6 +2,8 @@
 #pragma once
 
 #include <cstdint>
+#include <map>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <utility>
@@ -30,6 +32,7 @@ constexpr int kFastMaxLen = 256;  // bit-parallel JW for left strings up to this
 struct Column {
   std::vector<char> bytes;
   std::vector<int64_t> off;  // n_rows + 1
+  bool has_nul = false;      // some cell holds a NUL byte (cells compare up to it)
   const char* ptr(int64_t i) const { return bytes.data() + off[(size_t)i]; }
   int64_t len(int64_t i) const { return off[(size_t)i + 1] - off[(size_t)i]; }
 };
@@ -88,7 +91,25 @@ void order_predicates(Plan* plan, const Table& left, const Table& right);
 
 struct hbx_plan {
   hbx::Plan p;
+  // Evaluation order measured for a (left table, right table) pair, by table
+  // uid.  Tables never change after creation, so an entry stays valid.
+  std::mutex order_mu;
+  std::map<std::pair<uint64_t, uint64_t>, std::vector<hbx::CompiledRule>> order_cache;
 };
 struct hbx_table {
   hbx::Table t;
+  uint64_t uid = 0;  // unique per table created in this process
+  // page-locked column buffers (pin_table), released by hbx_table_destroy
+  std::mutex pin_mu;
+  bool pin_tried = false;
+  std::vector<void*> pinned;
 };
+
+namespace hbx {
+// Sets has_nul of every column (after a table is built).
+void finish_table(Table* t);
+// Unlocks what pin_table locked (engine side; no CUDA call when nothing is).
+void unpin_table(hbx_table* t);
+// Next table uid.
+uint64_t next_table_uid();
+}  // namespace hbx

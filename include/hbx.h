@@ -72,6 +72,11 @@ typedef struct hbx_opts {
   int32_t tile_right;        /* right rows per work item, 0 = autotuned */
   int32_t eval_variant;      /* evaluation kernel: 1 = 3 CTAs/SM, 2 = 2 CTAs/SM with more
                                 registers, 0 = autotuned */
+  int32_t pred_order;        /* similarity predicates of a rule run in: 0 = order of measured
+                                selectivity and cost (default), 1 = the order the rule gives */
+  int32_t ingest;            /* tables are encoded: 0 = on the device (default; the host
+                                encoder still takes the inputs only it encodes exactly),
+                                1 = on the host */
   uint64_t watchdog_cycles;  /* per-CTA SM-cycle budget of the persistent loop, 0 = none */
 } hbx_opts;
 
@@ -107,6 +112,9 @@ typedef struct hbx_stats {
   double ms_eval;             /* device time of the pair-evaluation kernel(s) */
   uint64_t jw_word_ops;       /* algorithmic 64-bit word operations of the JW phase */
   uint64_t h2d_bytes;         /* bytes uploaded when the session was created */
+  double ms_create;           /* host wall time of the session's creation */
+  uint32_t ingest_on_device;  /* 1 when the tables were encoded on the device */
+  uint32_t reserved;
 } hbx_stats;
 
 /* ---- context ------------------------------------------------------------ */
