@@ -35,7 +35,7 @@ EXE_PATH = os.path.join(HERE, "_build", "run_hyperblocker_exec")
 INT_MAX = 2147483647
 
 OK, ERR_INVALID_ARG, ERR_CUDA, ERR_OOM, ERR_CAPACITY, ERR_WATCHDOG, ERR_PARSE, ERR_IO, \
-    ERR_UNSUPPORTED = range(9)
+    ERR_UNSUPPORTED, ERR_TIMEOUT = range(10)
 MODE_PLAIN, MODE_BATCHED = 0, 1
 _MODES = {"plain": MODE_PLAIN, "batched": MODE_BATCHED}
 
@@ -80,6 +80,31 @@ class Stats(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class ServeOpts(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_uint32), ("max_inflight", ctypes.c_int32),
+                ("max_batch_rows", ctypes.c_int64), ("budget_bytes", ctypes.c_uint64),
+                ("tile_right", ctypes.c_int32), ("eval_variant", ctypes.c_int32)]
+
+
+class ServeResult(ctypes.Structure):
+    _fields_ = [("req_id", ctypes.c_uint64), ("status", ctypes.c_int32), ("plan", ctypes.c_int32),
+                ("n_pairs", ctypes.c_uint64), ("l_row", ctypes.POINTER(ctypes.c_uint32)),
+                ("r_row", ctypes.POINTER(ctypes.c_uint32)), ("pair_comparisons", ctypes.c_uint64),
+                ("ms_queued", ctypes.c_double), ("ms_total", ctypes.c_double),
+                ("batch_requests", ctypes.c_uint32), ("batch_id", ctypes.c_uint32)]
+
+
+class ServeStats(ctypes.Structure):
+    _fields_ = [("requests_done", ctypes.c_uint64), ("batches", ctypes.c_uint64),
+                ("rows", ctypes.c_uint64), ("pair_comparisons", ctypes.c_uint64),
+                ("n_pairs", ctypes.c_uint64), ("ms_device", ctypes.c_double),
+                ("budget_bytes", ctypes.c_uint64), ("peak_bytes", ctypes.c_uint64),
+                ("resident_bytes", ctypes.c_uint64)]
+
+    def as_dict(self) -> Dict[str, float]:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 # Every function include/hbx.h declares: name -> (restype, argtypes).
 _VP = ctypes.c_void_p
 SIGNATURES = {
@@ -114,6 +139,13 @@ SIGNATURES = {
                                         ctypes.c_int64, ctypes.POINTER(Pairs), _VP,
                                         ctypes.POINTER(Stats)]),
     "hbx_static_last_error": (ctypes.c_char_p, []),
+    "hbx_serve_open": (ctypes.c_int, [_VP, ctypes.POINTER(_VP), ctypes.c_int32, _VP,
+                                      ctypes.POINTER(ServeOpts), ctypes.POINTER(_VP)]),
+    "hbx_serve_submit": (ctypes.c_int, [_VP, ctypes.c_uint64, ctypes.c_int32, ctypes.POINTER(Columns)]),
+    "hbx_serve_poll": (ctypes.c_int, [_VP, ctypes.c_int32, ctypes.POINTER(ServeResult)]),
+    "hbx_serve_get_stats": (ctypes.c_int, [_VP, ctypes.POINTER(ServeStats)]),
+    "hbx_serve_close": (ctypes.c_int, [_VP]),
+    "hbx_serve_last_error": (ctypes.c_char_p, [_VP]),
 }
 
 _lib: Optional[ctypes.CDLL] = None
@@ -227,24 +259,10 @@ class Table:
         return cls(h)
 
     @classmethod
-    def from_columns(cls, cols: Sequence[Sequence[bytes]], ctx: Optional[Context] = None) -> "Table":
-        n_cols = len(cols)
-        n_rows = len(cols[0]) if n_cols else 0
-        datas, offs = [], []
-        for col in cols:
-            if len(col) != n_rows:
-                raise ValueError("columns differ in length")
-            blob = b"".join(col)
-            off = np.zeros(n_rows + 1, dtype=np.int64)
-            if n_rows:
-                off[1:] = np.cumsum([len(x) for x in col])
-            datas.append(ctypes.create_string_buffer(blob, max(len(blob), 1)))
-            offs.append(off)
-        data_arr = (ctypes.c_char_p * max(n_cols, 1))(*[ctypes.cast(d, ctypes.c_char_p) for d in datas])
-        off_arr = (ctypes.POINTER(ctypes.c_int64) * max(n_cols, 1))(
-            *[o.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)) for o in offs])
-        cs = Columns(n_rows, n_cols, ctypes.cast(data_arr, ctypes.POINTER(ctypes.c_char_p)),
-                     ctypes.cast(off_arr, ctypes.POINTER(ctypes.POINTER(ctypes.c_int64))))
+    def from_columns(cls, cols, ctx: Optional[Context] = None) -> "Table":
+        """Column-major cells: each column a sequence of bytes, or a
+        (blob uint8 array, int64 offsets) pair; the engine copies them."""
+        cs, keep = _columns_struct(cols)
         h = _VP()
         c = ctx.h if ctx else None
         _check(lib().hbx_table_ingest(c, ctypes.byref(cs), ctypes.byref(h)), c)
@@ -262,6 +280,108 @@ class Table:
         if getattr(self, "h", None):
             lib().hbx_table_destroy(self.h)
             self.h = None
+
+
+def _columns_struct(cols):
+    """hbx_columns over column-major cells: each column is a sequence of bytes
+    or a (blob uint8 array, int64 offsets) pair.  Returns (struct, keepalive)."""
+    n_cols = len(cols)
+    datas, offs = [], []
+    n_rows = None
+    for col in cols:
+        if isinstance(col, tuple):
+            blob = np.ascontiguousarray(col[0], dtype=np.uint8)
+            off = np.ascontiguousarray(col[1], dtype=np.int64)
+            if blob.size == 0:
+                blob = np.zeros(1, dtype=np.uint8)
+        else:
+            joined = b"".join(col)
+            blob = np.frombuffer(joined, dtype=np.uint8) if joined else np.zeros(1, np.uint8)
+            off = np.zeros(len(col) + 1, dtype=np.int64)
+            if len(col):
+                off[1:] = np.cumsum([len(x) for x in col])
+        rows = len(off) - 1
+        if n_rows is not None and rows != n_rows:
+            raise ValueError("columns differ in length")
+        n_rows = rows
+        datas.append(blob)
+        offs.append(off)
+    data_arr = (ctypes.c_char_p * max(n_cols, 1))(
+        *[ctypes.cast(d.ctypes.data, ctypes.c_char_p) for d in datas])
+    off_arr = (ctypes.POINTER(ctypes.c_int64) * max(n_cols, 1))(
+        *[o.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)) for o in offs])
+    cs = Columns(n_rows or 0, n_cols, ctypes.cast(data_arr, ctypes.POINTER(ctypes.c_char_p)),
+                 ctypes.cast(off_arr, ctypes.POINTER(ctypes.POINTER(ctypes.c_int64))))
+    return cs, (datas, offs, data_arr, off_arr)
+
+
+class Server:
+    """Resident right table answering requests of left records (hbx_serve_*).
+
+    ``plans[k]`` is request plan k.  ``submit`` copies the records and returns
+    at once; ``poll`` returns finished requests as dicts with the request id,
+    its (left row, right row) pairs sorted, and its timings.
+    """
+
+    def __init__(self, ctx: Context, plans: Sequence["Plan"], right: "Table",
+                 max_inflight: int = 0, max_batch_rows: int = 0, budget_bytes: int = 0,
+                 tile_right: int = 0, eval_variant: int = 0):
+        o = ServeOpts(ctypes.sizeof(ServeOpts), max_inflight, max_batch_rows, budget_bytes,
+                      tile_right, eval_variant)
+        arr = (_VP * len(plans))(*[p.h for p in plans])
+        h = _VP()
+        _check(lib().hbx_serve_open(ctx.h, arr, len(plans), right.h, ctypes.byref(o),
+                                    ctypes.byref(h)), ctx.h)
+        self.h = h
+        self.ctx = ctx
+        self._keep = (list(plans), right)
+
+    def _err(self, st: int) -> None:
+        if st != OK:
+            msg = lib().hbx_serve_last_error(self.h)
+            raise HbxError(st, (msg or b"").decode(errors="replace"))
+
+    def submit(self, req_id: int, plan: int, cols) -> None:
+        cs, keep = _columns_struct(cols)
+        self._err(lib().hbx_serve_submit(self.h, req_id, plan, ctypes.byref(cs)))
+
+    def poll(self, timeout_ms: int = -1) -> Optional[dict]:
+        r = ServeResult()
+        st = lib().hbx_serve_poll(self.h, timeout_ms, ctypes.byref(r))
+        if st == ERR_TIMEOUT:
+            return None
+        self._err(st)
+        n = int(r.n_pairs)
+        pairs = np.zeros((n, 2), dtype=np.uint32)
+        if n:
+            pairs[:, 0] = np.ctypeslib.as_array(r.l_row, shape=(n,))
+            pairs[:, 1] = np.ctypeslib.as_array(r.r_row, shape=(n,))
+        return {"id": int(r.req_id), "status": int(r.status), "plan": int(r.plan), "pairs": pairs,
+                "comparisons": int(r.pair_comparisons), "ms_queued": r.ms_queued,
+                "ms_total": r.ms_total, "batch_requests": int(r.batch_requests),
+                "batch_id": int(r.batch_id)}
+
+    def stats(self) -> ServeStats:
+        s = ServeStats()
+        self._err(lib().hbx_serve_get_stats(self.h, ctypes.byref(s)))
+        return s
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            lib().hbx_serve_close(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 def _mode(mode) -> int:

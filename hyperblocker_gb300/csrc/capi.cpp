@@ -66,6 +66,7 @@ const char* hbx_status_string(hbx_status s) {
     case HBX_ERR_PARSE: return "parse error";
     case HBX_ERR_IO: return "I/O error";
     case HBX_ERR_UNSUPPORTED: return "unsupported input";
+    case HBX_ERR_TIMEOUT: return "timed out";
   }
   return "unknown status";
 }

@@ -1,0 +1,18 @@
+// context.h -- the hbx_ctx of the C ABI (device, stream, memory pool).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "../../include/hbx.h"
+
+struct hbx_ctx {
+  int device = 0;
+  int n_sm = 0;
+  size_t smem_optin = 0;
+  cudaStream_t stream = nullptr;
+  cudaMemPool_t pool = nullptr;  // device memory of this context's sessions and servers
+  hbx_opts opts{};
+  std::string err;
+};

@@ -102,6 +102,8 @@ struct DBuf {
       from = DevPool{};
     }
     n = count;
+    // the kernels' bulk copies and vector loads need 16-byte aligned bases
+    if ((uintptr_t)p & 15) fail(HBX_ERR_CUDA, "device allocation not 16-byte aligned");
   }
   void upload(const std::vector<T>& v, cudaStream_t s) {
     alloc(v.size());
@@ -109,6 +111,10 @@ struct DBuf {
       HBX_CUDA(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
   }
 };
+
+// Raises (never lowers) an evaluation kernel's dynamic shared-memory limit
+// to bytes; the limit is process-wide, shared by every session and server.
+void raise_smem_limit(dev::EvalKernel kern, size_t bytes);
 
 // Device copy of one encoded table.
 struct SideBufs {

@@ -27,21 +27,13 @@
 
 #include <unistd.h>
 
+#include "context.h"
 #include "device_buffers.h"
 #include "encode.h"
 #include "hbx_core.h"
 #include "ingest.h"
 #include "kernels.cuh"
 
-struct hbx_ctx {
-  int device = 0;
-  int n_sm = 0;
-  size_t smem_optin = 0;
-  cudaStream_t stream = nullptr;
-  cudaMemPool_t pool = nullptr;  // device memory of this context's sessions
-  hbx_opts opts{};
-  std::string err;
-};
 
 namespace hbx {
 
@@ -100,6 +92,17 @@ struct hbx_session {
 };
 
 namespace hbx {
+
+void raise_smem_limit(dev::EvalKernel kern, size_t bytes) {
+  // The limit belongs to the kernel, process-wide: only ever raise it, so a
+  // session needing less never lowers it under another live session.
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lock(mu);
+  cudaFuncAttributes fa;
+  HBX_CUDA(cudaFuncGetAttributes(&fa, kern));
+  if ((size_t)fa.maxDynamicSharedSizeBytes < bytes)
+    HBX_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+}
 
 namespace {
 
@@ -161,17 +164,7 @@ void configure(hbx_session* S, uint32_t tile_right, int variant) {
   HBX_CUDA(cudaMemcpyAsync(S->d_rules.p, S->h_rules.data(), S->h_rules.size() * sizeof(dev::Rule),
                            cudaMemcpyHostToDevice, C->stream));
   HBX_CUDA(cudaStreamSynchronize(C->stream));
-  {
-    // The limit belongs to the kernel, process-wide: only ever raise it, so a
-    // session needing less never lowers it under another live session.
-    static std::mutex mu;
-    std::lock_guard<std::mutex> lock(mu);
-    cudaFuncAttributes fa;
-    HBX_CUDA(cudaFuncGetAttributes(&fa, kern));
-    if ((size_t)fa.maxDynamicSharedSizeBytes < S->smem_bytes)
-      HBX_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)S->smem_bytes));
-  }
+  raise_smem_limit(kern, S->smem_bytes);
   int bps = 0;
   HBX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, kThreads, S->smem_bytes));
   S->blocks_per_sm = std::max(1, bps);

@@ -36,30 +36,7 @@
 namespace hbx {
 namespace ing {
 
-constexpr unsigned long long kEmpty = ~0ull;
 constexpr uint32_t kSharedHist = 4096;  // partitions counted in shared memory
-constexpr uint32_t kFlagCollision = 1, kFlagTableFull = 2;
-
-// summary words (u64)
-enum : uint32_t { kSumPairs = 0, kSumUsed = 1, kSumFlags = 2, kSumSymbols = 3, kSumFixed = 4 };
-
-struct ColDev {
-  const uint8_t* bytes;
-  const int64_t* off;  // n + 1
-  uint32_t has_nul;
-};
-
-// Byte range of cell i, its length cut at the first NUL when the column has
-// NUL bytes.
-__device__ __forceinline__ uint32_t cell_len(const ColDev& c, uint32_t i, int64_t* start) {
-  const int64_t a = c.off[i];
-  const uint32_t n = (uint32_t)(c.off[i + 1] - a);
-  *start = a;
-  if (c.has_nul)
-    for (uint32_t k = 0; k < n; k++)
-      if (c.bytes[a + k] == 0) return k;
-  return n;
-}
 
 __global__ void k_buckets(ColDev part, uint32_t use_part, ColDev pre, uint32_t use_pre,
                           unsigned long long n_part, uint32_t n, uint32_t* bucket,
@@ -282,9 +259,7 @@ __global__ void k_pack(ColDev c, uint32_t n, const uint32_t* off16, const uint8_
 
 }  // namespace ing
 
-namespace {
-
-int grid_for(uint64_t n, int n_sm, int per_sm = 8) {
+int grid_for(uint64_t n, int n_sm, int per_sm) {
   const uint64_t g = (n + 255) / 256;
   return (int)std::max<uint64_t>(1, std::min<uint64_t>(g, (uint64_t)n_sm * per_sm));
 }
@@ -294,7 +269,6 @@ void check_launch(const char* what) {
   if (e != cudaSuccess) fail(HBX_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-// Exclusive scan of n u32 values (n >= 1) with the join's scan kernels.
 void scan_u32(const uint32_t* in, uint32_t n, uint32_t* out, cudaStream_t st) {
   const uint32_t nb = (n + dev::kScanChunk - 1) / dev::kScanChunk;
   DBuf<uint32_t> part;
@@ -304,6 +278,8 @@ void scan_u32(const uint32_t* in, uint32_t n, uint32_t* out, cudaStream_t st) {
   dev::k_scan_final_u32<<<nb, 1024, 0, st>>>(in, n, part.p, out);
   check_launch("ingest scan");
 }
+
+namespace {
 
 struct DevCol {
   DBuf<uint8_t> bytes;

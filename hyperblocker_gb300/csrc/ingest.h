@@ -11,6 +11,59 @@
 
 namespace hbx {
 
+// ---- kernels shared by the session ingest and the serving loop ------------
+namespace ing {
+
+constexpr unsigned long long kEmpty = ~0ull;  // free slot of a dictionary table
+constexpr uint32_t kFlagCollision = 1, kFlagTableFull = 2;
+// words of an ingest summary (u64): pairs covered, used partitions, flags,
+// alphabet size, then call-specific words
+enum : uint32_t { kSumPairs = 0, kSumUsed = 1, kSumFlags = 2, kSumSymbols = 3, kSumFixed = 4 };
+
+// One device column: cell bytes and int64 offsets (n + 1), as a host Column.
+struct ColDev {
+  const uint8_t* bytes;
+  const int64_t* off;
+  uint32_t has_nul;
+};
+
+// Length of cell i, cut at its first NUL when the column has NUL bytes
+// (the reference compares cells as C strings); *start = its first byte.
+__device__ __forceinline__ uint32_t cell_len(const ColDev& c, uint32_t i, int64_t* start) {
+  const int64_t a = c.off[i];
+  const uint32_t n = (uint32_t)(c.off[i + 1] - a);
+  *start = a;
+  if (c.has_nul)
+    for (uint32_t k = 0; k < n; k++)
+      if (c.bytes[a + k] == 0) return k;
+  return n;
+}
+
+__global__ void k_dict_insert(ColDev c, uint32_t n, uint32_t gid_base, unsigned long long* keys,
+                              uint32_t* rep, uint32_t mask, uint32_t* row_slot,
+                              unsigned long long* sum);
+__global__ void k_occupied(const unsigned long long* keys, uint32_t cap, uint32_t* occ);
+__global__ void k_dict_assign(ColDev c, uint32_t n, uint32_t gid_base, const uint32_t* row_slot,
+                              const uint32_t* code, const uint32_t* rep, ColDev cl, ColDev cr,
+                              uint32_t n_left, int32_t* out, unsigned long long* sum);
+__global__ void k_scan_total(const uint32_t* scan, const uint32_t* in, uint32_t n,
+                             unsigned long long extra, unsigned long long* dst);
+__global__ void k_byte_hist(ColDev c, uint32_t n, unsigned long long* hist);
+__global__ void k_symbol_map(const unsigned long long* hist, uint8_t* sym, unsigned long long* sum);
+__global__ void k_units(ColDev c, uint32_t n, uint32_t* units);
+__global__ void k_pack(ColDev c, uint32_t n, const uint32_t* off16, const uint8_t* sym_g,
+                       uint8_t* arena, dev::StrMeta* meta, unsigned long long* maxlen);
+
+}  // namespace ing
+
+// Blocks for n items of 256 threads, at most per_sm per SM.
+int grid_for(uint64_t n, int n_sm, int per_sm = 8);
+// Fails with HBX_ERR_CUDA if the last launch failed.
+void check_launch(const char* what);
+// Exclusive scan of n >= 1 u32 values into out (the join's scan kernels);
+// its scratch comes from the current pool.
+void scan_u32(const uint32_t* in, uint32_t n, uint32_t* out, cudaStream_t st);
+
 // Encodes both tables for one plan on the device, writing the side buffers
 // directly: partition buckets with the reference's std::hash
 // (data_mngr.h:150-202), one joint dictionary per equality slot, the

@@ -48,7 +48,8 @@ typedef enum hbx_status {
   HBX_ERR_WATCHDOG = 5,   /* a device loop exceeded its time budget and stopped */
   HBX_ERR_PARSE = 6,      /* malformed CSV or YAML rule */
   HBX_ERR_IO = 7,         /* file could not be read or written */
-  HBX_ERR_UNSUPPORTED = 8 /* input the engine refuses (undefined in the reference) */
+  HBX_ERR_UNSUPPORTED = 8, /* input the engine refuses (undefined in the reference) */
+  HBX_ERR_TIMEOUT = 9      /* hbx_serve_poll: no result became ready within the timeout */
 } hbx_status;
 
 typedef enum hbx_mode {
@@ -178,6 +179,76 @@ hbx_status hbx_write_pairs(hbx_ctx* ctx, const hbx_table* left, const hbx_table*
  * -prefix_hash_pred_idx], plus -hbx_mode=plain|batched.  Returns a process
  * exit code (0 on success). */
 int hbx_run_cli(int argc, const char* const* argv);
+
+/* ---- serving -------------------------------------------------------------
+ * No counterpart in the reference, which runs one batch job per process.  A
+ * server keeps one right table resident on the device and answers requests
+ * as they arrive: each request is a batch of left records and the index of
+ * one of the server's plans; its result is every (left record, right row)
+ * pair that some rule of that plan accepts (equalities, then similarities,
+ * as in hbx_block), over all pairs (one partition).
+ *
+ * A worker thread admits queued requests in arrival order while the device
+ * memory they need fits the budget, encodes each admitted group of requests
+ * as one batch and evaluates every (request, rule) pair of the batch in one
+ * persistent launch; up to max_inflight batches are on the device at once,
+ * so requests that arrive while others run are admitted as soon as a batch
+ * slot and memory free up (continuous batching).  A request's result does
+ * not depend on what it was batched with.
+ *
+ * hbx_serve_submit and hbx_serve_poll may be called from any threads; one
+ * thread at a time should poll.  The server uses its context's device and
+ * memory pool; destroy the server before the context. */
+typedef struct hbx_serve_opts {
+  uint32_t struct_size;     /* sizeof(hbx_serve_opts) */
+  int32_t max_inflight;     /* batches on the device at once, 0 = 2 */
+  int64_t max_batch_rows;   /* left rows per batch, 0 = 131072 */
+  uint64_t budget_bytes;    /* device memory for batches in flight, 0 = half of the free memory */
+  int32_t tile_right;       /* right rows per work item, 0 = 128 */
+  int32_t eval_variant;     /* evaluation kernel as hbx_opts, 0 = 2 CTAs/SM */
+} hbx_serve_opts;
+
+typedef struct hbx_serve_result {
+  uint64_t req_id;
+  hbx_status status;
+  int32_t plan;
+  uint64_t n_pairs;
+  const uint32_t* l_row;     /* row of the request's records; valid until the next poll */
+  const uint32_t* r_row;     /* row of the resident table */
+  uint64_t pair_comparisons; /* (rule, left, right) triples whose equalities hold */
+  double ms_queued;          /* submit -> admitted into a batch */
+  double ms_total;           /* submit -> result ready */
+  uint32_t batch_requests;   /* requests in the batch this one ran in */
+  uint32_t batch_id;
+} hbx_serve_result;
+
+typedef struct hbx_serve_stats {
+  uint64_t requests_done;
+  uint64_t batches;
+  uint64_t rows;              /* left records evaluated */
+  uint64_t pair_comparisons;
+  uint64_t n_pairs;
+  double ms_device;           /* summed device time of the batches (CUDA events) */
+  uint64_t budget_bytes;
+  uint64_t peak_bytes;        /* largest device memory held by batches in flight */
+  uint64_t resident_bytes;    /* device memory of the resident table and its joins */
+} hbx_serve_stats;
+
+/* plans[k] is request plan k; every plan's column indices refer to the
+ * request records (left) and the resident table (right). */
+hbx_status hbx_serve_open(hbx_ctx* ctx, const hbx_plan* const* plans, int32_t n_plans,
+                          const hbx_table* right, const hbx_serve_opts* opts, hbx_server** out);
+/* Copies the records and queues the request; returns at once.  A request
+ * that alone exceeds the budget is refused with HBX_ERR_CAPACITY. */
+hbx_status hbx_serve_submit(hbx_server* s, uint64_t req_id, int32_t plan, const hbx_columns* left);
+/* Waits up to timeout_ms (< 0: no limit) for a finished request and returns
+ * it; HBX_ERR_TIMEOUT when none finished in time.  out->status is the
+ * request's own outcome. */
+hbx_status hbx_serve_poll(hbx_server* s, int32_t timeout_ms, hbx_serve_result* out);
+hbx_status hbx_serve_get_stats(const hbx_server* s, hbx_serve_stats* out);
+/* Finishes the queued and running requests, then frees the server. */
+hbx_status hbx_serve_close(hbx_server* s);
+const char* hbx_serve_last_error(const hbx_server* s);
 
 /* ---- blocking without device allocation ----------------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc:

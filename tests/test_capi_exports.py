@@ -25,5 +25,5 @@ def test_every_declared_symbol_is_exported(built):
 
 def test_status_strings(built):
     L = hb.lib()
-    for s in range(9):
-        assert L.hbx_status_string(s)
+    for s in range(10):
+        assert L.hbx_status_string(s) != b"unknown status"
