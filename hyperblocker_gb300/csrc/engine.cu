@@ -196,6 +196,7 @@ uint64_t upload_host_encoding(hbx_session* S) {
         dev::StrMeta m;
         m.loc = make_uint4(off, len, 0, 0);
         m.head = make_uint4(w[0], w[1], w[2], w[3]);
+        dev::make_sig(se.arena.data() + (size_t)off * 16, len, m.sig);
         meta.push_back(m);
       }
     sb.meta.upload(meta, st);
@@ -376,6 +377,7 @@ dev::EvalParams eval_params(hbx_session* S) {
   P.queue_off = S->wl.queue_off;
   P.stage_meta_off = S->wl.stage_meta_off;
   P.stage_rows_off = S->wl.stage_rows_off;
+  P.sig_off = S->wl.sig_off;
   P.mbar_off = S->wl.mbar_off;
   P.out_l = S->out_l.p;
   P.out_r = S->out_r.p;

@@ -215,14 +215,16 @@ __global__ void k_units(ColDev c, uint32_t n, uint32_t* units) {
 }
 
 // One warp per string: symbols into the arena at unit off16[i], metadata
-// {offset / 16, length, 0, 0} + the first 16 symbols; the longest length
-// goes to *maxlen.
+// {offset / 16, length, 0, 0} + the first 16 symbols + the count signature
+// (dev::StrMeta); the longest length goes to *maxlen.  256 threads per block.
 __global__ void k_pack(ColDev c, uint32_t n, const uint32_t* off16, const uint8_t* sym_g,
                        uint8_t* arena, dev::StrMeta* meta, unsigned long long* maxlen) {
   __shared__ uint8_t sym[256];
+  __shared__ uint32_t s_cnt[8][dev::kSigBuckets];
   for (uint32_t k = threadIdx.x; k < 256; k += blockDim.x) sym[k] = sym_g[k];
   __syncthreads();
   const uint32_t lane = threadIdx.x & 31;
+  uint32_t* cnt = s_cnt[threadIdx.x >> 5];
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   uint32_t mx = 0;
   for (uint32_t i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {
@@ -239,20 +241,46 @@ __global__ void k_pack(ColDev c, uint32_t n, const uint32_t* off16, const uint8_
       }
     }
     const uint64_t pos = (uint64_t)off16[i] * 16;
-    for (uint32_t j = lane; j < len; j += 32) arena[pos + j] = sym[c.bytes[a + j]];
+    cnt[lane] = 0;
+    __syncwarp();
+    for (uint32_t base = 0; base < len; base += 32) {
+      const uint32_t j = base + lane;
+      const uint32_t v = j < len ? sym[c.bytes[a + j]] : 0u;
+      if (j < len) arena[pos + j] = (uint8_t)v;
+      // one add per (bucket, chunk): the lowest lane of each bucket group
+      const uint32_t b = v ? dev::sig_bucket(v) : 0xffffffffu;
+      const unsigned grp = __match_any_sync(0xffffffffu, b);
+      if (v && lane == (uint32_t)(__ffs(grp) - 1)) cnt[b] += (uint32_t)__popc(grp);
+      __syncwarp();
+    }
+    __syncwarp();
+    uint32_t sw = 0;  // signature word `lane` (lanes 0-7)
+    if (lane < 8) {
+      if (len > dev::kSigMaxLen) {
+        sw = 0xffffffffu;
+      } else {
+        for (int k = 0; k < 4; k++) sw |= cnt[4 * lane + k] << (8 * k);
+      }
+    }
     const uint32_t s = (lane < 16 && lane < len) ? sym[c.bytes[a + lane]] : 0u;
     uint32_t v = s << (8 * (lane & 3));
     v |= __shfl_xor_sync(0xffffffffu, v, 1);
     v |= __shfl_xor_sync(0xffffffffu, v, 2);
     const uint32_t w0 = __shfl_sync(0xffffffffu, v, 0), w1 = __shfl_sync(0xffffffffu, v, 4);
     const uint32_t w2 = __shfl_sync(0xffffffffu, v, 8), w3 = __shfl_sync(0xffffffffu, v, 12);
+    uint32_t g[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) g[k] = __shfl_sync(0xffffffffu, sw, k);
     if (lane == 0) {
       dev::StrMeta m;
       m.loc = make_uint4(off16[i], len, 0u, 0u);
       m.head = make_uint4(w0, w1, w2, w3);
+      m.sig[0] = make_uint4(g[0], g[1], g[2], g[3]);
+      m.sig[1] = make_uint4(g[4], g[5], g[6], g[7]);
       meta[i] = m;
       mx = max(mx, len);
     }
+    __syncwarp();
   }
   if (lane == 0 && mx) atomicMax(maxlen, (unsigned long long)mx);
 }

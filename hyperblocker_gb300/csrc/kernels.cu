@@ -507,6 +507,7 @@ struct Stage {
   uint32_t* rows;           // right rows of the input list (shared memory); survivors
                             // are written back over consumed entries
   const StrMeta* meta;      // first stage: the rows' staged string metadata, else null
+  const uint4* a_sig;       // count signature of the left string (shared memory)
   uint4* q;                 // ring of pairs to scan, 2 x uint4 per entry:
                             // {row, offset/16, length, p << 16 | need}, first 16 symbols
   uint32_t n;               // rows in the input list
@@ -565,6 +566,23 @@ __device__ __forceinline__ void route(const EvalParams& P, const Stage& A, bool 
   }
 }
 
+// Upper bound on the Jaro matches of two strings from their count signatures
+// (dev::StrMeta): sum over buckets of the smaller count.
+__device__ __forceinline__ uint32_t sig_bound(const uint4& a0, const uint4& a1, const uint4& b0,
+                                              const uint4& b1) {
+  constexpr unsigned kOnes = 0x01010101u;
+  uint32_t s = 0;
+  s = __dp4a(__vminu4(a0.x, b0.x), kOnes, s);
+  s = __dp4a(__vminu4(a0.y, b0.y), kOnes, s);
+  s = __dp4a(__vminu4(a0.z, b0.z), kOnes, s);
+  s = __dp4a(__vminu4(a0.w, b0.w), kOnes, s);
+  s = __dp4a(__vminu4(a1.x, b1.x), kOnes, s);
+  s = __dp4a(__vminu4(a1.y, b1.y), kOnes, s);
+  s = __dp4a(__vminu4(a1.z, b1.z), kOnes, s);
+  s = __dp4a(__vminu4(a1.w, b1.w), kOnes, s);
+  return s;
+}
+
 // Common prefix of two 16-symbol little-endian heads; 16 when they agree.
 __device__ __forceinline__ uint32_t prefix16(const uint4& a, const uint4& b) {
   const uint32_t d[4] = {a.x ^ b.x, a.y ^ b.y, a.z ^ b.z, a.w ^ b.w};
@@ -592,9 +610,12 @@ __device__ __forceinline__ uint32_t filter_batch(const EvalParams& P, const Stag
   const uint32_t e = e0 + (uint32_t)lane;
   const bool act = e < A.n;
   const uint32_t rrow = act ? A.rows[e] : 0u;
+  const StrMeta* mp = nullptr;
   StrMeta m;
   if (act) {
-    m = A.meta ? A.meta[e] : P.R.str_meta[(size_t)A.slot_r * nR + rrow];
+    mp = A.meta ? A.meta + e : P.R.str_meta + (size_t)A.slot_r * nR + rrow;
+    m.loc = mp->loc;
+    m.head = mp->head;
   } else {
     m.loc = make_uint4(0, 0, 0, 0);
     m.head = make_uint4(0, 0, 0, 0);
@@ -618,6 +639,11 @@ __device__ __forceinline__ uint32_t filter_batch(const EvalParams& P, const Stag
         need = m_need_lo(ls, ll, p, A.thr);
         const uint32_t n_iter = min(lb, A.la + ((ls + 1u) >> 1));
         scan = need <= (int)min(n_iter, ls);  // else the threshold is out of reach
+        // the count signatures bound the matches from above: below the need,
+        // the pair cannot pass
+        if (scan && need > 0 &&
+            (int)sig_bound(A.a_sig[0], A.a_sig[1], mp->sig[0], mp->sig[1]) < need)
+          scan = false;
       }
     }
   }
@@ -837,6 +863,7 @@ __device__ __forceinline__ void eval_body(const EvalParams& P) {
   uint4* q = reinterpret_cast<uint4*>(region + P.queue_off);
   StrMeta* st_meta = reinterpret_cast<StrMeta*>(region + P.stage_meta_off);
   uint32_t* st_rows = region + P.stage_rows_off;
+  uint4* l_sig = reinterpret_cast<uint4*>(region + P.sig_off);
   uint64_t* bar = reinterpret_cast<uint64_t*>(region + P.mbar_off);
   if (lane == 0) mbar_init(bar);
   __syncwarp();
@@ -912,10 +939,14 @@ __device__ __forceinline__ void eval_body(const EvalParams& P) {
       A.n = rb1 - rb0;
       for (uint32_t s = 0; s < R.n_sim && A.n > 0; s++) {
         const uint32_t sl = R.sim_l[s];
-        const StrMeta am = P.L.str_meta[(size_t)sl * P.L.n_rows + lrow];
-        A.la = am.loc.y;
-        A.a = P.L.arena + 16ull * am.loc.x;
-        A.a_head = am.head;
+        const StrMeta* amp = P.L.str_meta + (size_t)sl * P.L.n_rows + lrow;
+        const uint4 aloc = amp->loc;
+        A.la = aloc.y;
+        A.a = P.L.arena + 16ull * aloc.x;
+        A.a_head = amp->head;
+        if (lane < 2) l_sig[lane] = amp->sig[lane];
+        __syncwarp();
+        A.a_sig = l_sig;
         A.thr = R.thr[s];
         A.slot_r = R.sim_r[s];
         A.last = s + 1 == R.n_sim;

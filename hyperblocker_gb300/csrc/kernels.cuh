@@ -46,13 +46,45 @@ constexpr int kWarpsPerCta = 8;
 __host__ __device__ constexpr int row_words(int w) { return w <= 1 ? 1 : w <= 2 ? 2 : w <= 4 ? 4 : 8; }
 constexpr float kDecisionMargin = 1e-4f;  // |approx JW - thr| below this -> exact path
 
-// Metadata of one string: where it is, how long, and its first 16 symbols
-// (0 past the end), so that one 32-byte load gives the length, the common
-// prefix with another string (up to 16) and the first chunk of a scan.
+// Count signature of a string: byte k (of 32) counts the string's symbols in
+// bucket k, where the 31 most frequent symbols have a bucket each and the
+// rest share the last one.  For any two strings a, b the Jaro match count
+// (any matching between equal symbols) is at most
+//     sum_k min(sig_a[k], sig_b[k]),
+// and pooling symbols into one bucket only raises that sum, so the bound is
+// exact.  A string longer than kSigMaxLen bytes, whose counts might not fit a
+// byte, gets 0xff in every bucket: min() then takes the other side's count,
+// which still bounds the matches from above.
+constexpr uint32_t kSigBuckets = 32;
+constexpr uint32_t kSigMaxLen = 255;
+__host__ __device__ inline uint32_t sig_bucket(uint32_t sym) {  // sym >= 1
+  return sym >= kSigBuckets ? kSigBuckets - 1 : sym - 1;
+}
+
+// Metadata of one string: where it is, how long, its first 16 symbols (0 past
+// the end) and its count signature, so that one 64-byte record gives the
+// length, the common prefix with another string (up to 16), the first chunk
+// of a scan and an upper bound on the matches with any other string.
 struct __align__(16) StrMeta {
-  uint4 loc;   // {offset / 16, length, 0, 0}
-  uint4 head;  // symbols 0-3, 4-7, 8-11, 12-15 (little endian)
+  uint4 loc;     // {offset / 16, length, 0, 0}
+  uint4 head;    // symbols 0-3, 4-7, 8-11, 12-15 (little endian)
+  uint4 sig[2];  // bucket counts 0-15, 16-31, one byte each (little endian)
 };
+
+// Host form of the signature of a string of symbols.
+inline void make_sig(const uint8_t* s, uint32_t len, uint4 out[2]) {
+  uint32_t w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  if (len > kSigMaxLen) {
+    for (int k = 0; k < 8; k++) w[k] = 0xffffffffu;
+  } else {
+    uint32_t c[kSigBuckets] = {0};
+    for (uint32_t i = 0; i < len; i++)
+      if (s[i]) c[sig_bucket(s[i])]++;
+    for (uint32_t k = 0; k < kSigBuckets; k++) w[k / 4] |= c[k] << (8 * (k % 4));
+  }
+  out[0] = make_uint4(w[0], w[1], w[2], w[3]);
+  out[1] = make_uint4(w[4], w[5], w[6], w[7]);
+}
 
 struct Side {
   const uint32_t* bucket;
@@ -102,21 +134,23 @@ constexpr uint32_t kRingEntries = 64;
 
 // Shared memory of one warp of k_eval, in 32-bit words: the Peq tables
 // (peq_words, a multiple of 4), then the scan ring (kRingEntries x 32 bytes),
-// the staged item metadata (tile_right x 32 bytes), the staged item rows
+// the staged item metadata (tile_right StrMeta records), the staged item rows
 // (tile_right + 8: a 16-byte-aligned copy starts up to 3 rows early and rounds
-// up; the same words then hold the rows that survive each stage) and one
-// mbarrier.  Every offset is a multiple of 4 words (16 bytes) when tile_right
-// is a multiple of 32.
+// up; the same words then hold the rows that survive each stage), the count
+// signature of the stage's left string (8 words) and one mbarrier.  Every
+// offset is a multiple of 4 words (16 bytes) when tile_right is a multiple of
+// 32.
 struct WarpLayout {
-  uint32_t queue_off, stage_meta_off, stage_rows_off, mbar_off, warp_words;
+  uint32_t queue_off, stage_meta_off, stage_rows_off, sig_off, mbar_off, warp_words;
 };
 
 inline WarpLayout warp_layout(uint32_t peq_words, uint32_t tile_right) {
   WarpLayout w;
   w.queue_off = peq_words;
   w.stage_meta_off = w.queue_off + 8 * kRingEntries;
-  w.stage_rows_off = w.stage_meta_off + 8 * tile_right;
-  w.mbar_off = w.stage_rows_off + tile_right + 8;
+  w.stage_rows_off = w.stage_meta_off + (uint32_t)(sizeof(StrMeta) / 4) * tile_right;
+  w.sig_off = w.stage_rows_off + tile_right + 8;
+  w.mbar_off = w.sig_off + 8;
   w.warp_words = w.mbar_off + 4;
   return w;
 }
@@ -160,6 +194,7 @@ struct EvalParams {
   uint32_t queue_off;       // word offset of the warp's scan ring
   uint32_t stage_meta_off;  // word offset of the staged item metadata
   uint32_t stage_rows_off;  // word offset of the staged item rows / survivor list
+  uint32_t sig_off;         // word offset of the left string's count signature
   uint32_t mbar_off;        // word offset of the warp's mbarrier (8-byte aligned)
   uint32_t* out_l;
   uint32_t* out_r;

@@ -780,6 +780,7 @@ void launch_eval(hbx_server* S, Slot& B) {
   P.queue_off = S->wl.queue_off;
   P.stage_meta_off = S->wl.stage_meta_off;
   P.stage_rows_off = S->wl.stage_rows_off;
+  P.sig_off = S->wl.sig_off;
   P.mbar_off = S->wl.mbar_off;
   P.out_l = B.out_l.p;
   P.out_r = B.out_r.p;

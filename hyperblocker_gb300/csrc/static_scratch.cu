@@ -103,6 +103,7 @@ std::vector<hbx::dev::StrMeta> string_meta(const hbx::SideEnc& se, uint32_t n) {
       hbx::dev::StrMeta m;
       m.loc = make_uint4(off, len, 0, 0);
       m.head = make_uint4(w[0], w[1], w[2], w[3]);
+      hbx::dev::make_sig(se.arena.data() + (size_t)off * 16, len, m.sig);
       meta.push_back(m);
     }
   return meta;
@@ -308,6 +309,7 @@ void run_static(int device, const hbx_plan* plan, const hbx_table* left, const h
   P.queue_off = Y.wl.queue_off;
   P.stage_meta_off = Y.wl.stage_meta_off;
   P.stage_rows_off = Y.wl.stage_rows_off;
+  P.sig_off = Y.wl.sig_off;
   P.mbar_off = Y.wl.mbar_off;
   P.out_l = out->l_row;
   P.out_r = out->r_row;
