@@ -154,13 +154,29 @@ struct RuleT {
   DBuf<dev::StrMeta> sorted_meta_r;
 };
 
+// A request: its records, and its progress through the batches.  Records
+// are dispatched in row chunks; the result is delivered when the last chunk
+// has come back.
 struct Request {
   uint64_t id = 0;
   int32_t plan = 0;
   Table rows;
   uint32_t n = 0;
-  uint64_t est = 0;
   Clock::time_point t_submit, t_admit;
+  bool admitted = false;
+  uint32_t next = 0;         // first row not dispatched yet
+  uint32_t outstanding = 0;  // chunks in batches that have not come back
+  std::vector<std::pair<uint32_t, uint32_t>> pairs;
+  uint64_t comparisons = 0;
+  uint32_t batch_requests = 0, batch_id = 0;
+  hbx_status status = HBX_OK;
+};
+
+// Rows [r0, r1) of one request inside a batch.
+struct Entry {
+  Request* r = nullptr;
+  uint32_t r0 = 0, r1 = 0;
+  uint32_t n() const { return r1 - r0; }
 };
 
 struct Result {
@@ -178,7 +194,7 @@ struct Inst {
   DBuf<unsigned long long> item_off, part_u64;
   DBuf<uint32_t> part_u32;
   uint32_t nb_l = 0;
-  uint32_t req = 0;  // request index within the batch
+  uint32_t req = 0;  // entry index within the batch
 };
 
 struct Pinned {
@@ -205,8 +221,8 @@ struct Slot {
   cudaEvent_t ev_start = nullptr, ev_eval = nullptr, ev_out = nullptr;
   int state = 0;  // 0 idle, 1 evaluating, 2 copying pairs back
   uint32_t batch_id = 0;
-  std::vector<std::unique_ptr<Request>> reqs;
-  std::vector<uint32_t> base;  // first batch row of each request (+ total)
+  std::vector<Entry> ents;
+  std::vector<uint32_t> base;  // first batch row of each entry (+ total)
   uint64_t est = 0;
   uint32_t n_rows = 0;
   std::vector<DevColumn> cols;  // per needed left column
@@ -228,7 +244,7 @@ struct Slot {
     if (st) cudaStreamDestroy(st);
   }
   void release() {
-    reqs.clear();
+    ents.clear();
     base.clear();
     cols.clear();
     L = SideBufs{};
@@ -281,7 +297,7 @@ struct hbx_server {
   // queue and results
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
-  std::deque<std::unique_ptr<Request>> queue;
+  std::vector<std::unique_ptr<Request>> active;  // submitted, result not delivered yet
   std::deque<Result> done;
   Result current;
   bool stopping = false;
@@ -598,13 +614,18 @@ void open_server(hbx_server* S, const hbx_plan* const* plans, int32_t n_plans, c
   S->st.resident_bytes = S->resident_bytes;
 }
 
-// Device memory a request needs while its batch is in flight (upper bound).
-uint64_t estimate(const hbx_server* S, const Table& t, int32_t plan) {
-  const uint64_t n = (uint64_t)t.n_rows;
+// Device memory rows [r0, r1) of a request need while their batch is in
+// flight (upper bound).
+uint64_t estimate(const hbx_server* S, const Table& t, int32_t plan, uint32_t r0, uint32_t r1) {
+  const uint64_t n = r1 - r0;
   uint64_t b = 0;
-  for (int c : S->left_cols) b += t.cols[(size_t)c].bytes.size() + 8 * (n + 1);
-  for (int c : S->lstr) b += t.cols[(size_t)c].bytes.size() + 15 * n + 16 + 40 * n;  // arena, meta, scan
-  b += 4 * n * S->pairs.size();
+  auto bytes = [&](int c) {
+    const Column& col = t.cols[(size_t)c];
+    return (uint64_t)(col.off[r1] - col.off[r0]);
+  };
+  for (int c : S->left_cols) b += bytes(c) + 8 * (n + 1) + 16;
+  for (int c : S->lstr) b += bytes(c) + 15 * n + 16 + 40 * n;  // arena, metadata, scan
+  b += sizeof(dev::StrMeta) * n * S->lstr.size() + 4 * n * S->pairs.size();
   for (int r : S->plan_rules[(size_t)plan]) {
     const dev::Rule& d = S->rules[(size_t)r]->d;
     b += 12ull * n + 20ull * d.domain_l + 64 + 8 * ((d.domain_l + dev::kScanChunk - 1) / dev::kScanChunk + 1);
@@ -617,9 +638,9 @@ void launch_batch(hbx_server* S, Slot& B) {
   hbx_ctx* C = S->ctx;
   cudaStream_t st = B.st;
   PoolScope scope(C->pool, st);
-  const size_t nq = B.reqs.size();
+  const size_t nq = B.ents.size();
   B.base.assign(nq + 1, 0);
-  for (size_t q = 0; q < nq; q++) B.base[q + 1] = B.base[q] + B.reqs[q]->n;
+  for (size_t q = 0; q < nq; q++) B.base[q + 1] = B.base[q] + B.ents[q].n();
   const uint32_t N = B.base[nq];
   B.n_rows = N;
   HBX_CUDA(cudaEventRecord(B.ev_start, st));
@@ -629,7 +650,10 @@ void launch_batch(hbx_server* S, Slot& B) {
   std::vector<uint64_t> bytes_c(nc, 0), boff(nc), ooff(nc);
   uint64_t total = 0;
   for (size_t k = 0; k < nc; k++) {
-    for (auto& r : B.reqs) bytes_c[k] += r->rows.cols[(size_t)S->left_cols[k]].bytes.size();
+    for (auto& e : B.ents) {
+      const Column& col = e.r->rows.cols[(size_t)S->left_cols[k]];
+      bytes_c[k] += (uint64_t)(col.off[e.r1] - col.off[e.r0]);
+    }
     boff[k] = total;
     total += (bytes_c[k] + 15) / 16 * 16;
   }
@@ -648,12 +672,13 @@ void launch_batch(hbx_server* S, Slot& B) {
     off[0] = 0;
     uint32_t row = 0;
     bool nul = false;
-    for (auto& r : B.reqs) {
-      const Column& col = r->rows.cols[(size_t)c];
-      if (!col.bytes.empty()) std::memcpy(h + boff[k] + pos, col.bytes.data(), col.bytes.size());
-      for (uint32_t i = 0; i < r->n; i++) off[row + i + 1] = (int64_t)pos + col.off[i + 1];
-      pos += col.bytes.size();
-      row += r->n;
+    for (auto& e : B.ents) {
+      const Column& col = e.r->rows.cols[(size_t)c];
+      const int64_t a = col.off[e.r0], len = col.off[e.r1] - a;
+      if (len) std::memcpy(h + boff[k] + pos, col.bytes.data() + a, (size_t)len);
+      for (uint32_t i = 0; i < e.n(); i++) off[row + i + 1] = (int64_t)pos + col.off[e.r0 + i + 1] - a;
+      pos += (uint64_t)len;
+      row += e.n();
       nul = nul || col.has_nul;
     }
     DevColumn& d = B.cols[k];
@@ -698,12 +723,12 @@ void launch_batch(hbx_server* S, Slot& B) {
   B.inst.clear();
   B.h_rules.clear();
   for (size_t q = 0; q < nq; q++)
-    for (int r : S->plan_rules[(size_t)B.reqs[q]->plan]) {
+    for (int r : S->plan_rules[(size_t)B.ents[q].r->plan]) {
       const dev::Rule& t = S->rules[(size_t)r]->d;
       B.inst.emplace_back();
       Inst& I = B.inst.back();
       I.req = (uint32_t)q;
-      const uint32_t n = B.reqs[q]->n;
+      const uint32_t n = B.ents[q].n();
       I.key_l.alloc(std::max<uint32_t>(n, 1));
       I.cnt_l.alloc(t.domain_l);
       I.off_l.alloc(t.domain_l);
@@ -736,7 +761,7 @@ void launch_batch(hbx_server* S, Slot& B) {
   for (uint32_t i = 0; i < ni; i++) {
     const Inst& I = B.inst[i];
     const dev::Rule& t = B.h_rules[i];
-    const uint32_t row0 = B.base[I.req], n = B.reqs[I.req]->n;
+    const uint32_t row0 = B.base[I.req], n = B.ents[I.req].n();
     if (n) k_keys<<<grid_for(n, C->n_sm), 256, 0, st>>>(B.d_rules.p, i, B.side_l, row0, n, I.key_l.p);
     dev::k_scan_partial_u32<<<I.nb_l, 1024, 0, st>>>(I.cnt_l.p, t.domain_l, I.part_u32.p);
     dev::k_scan_top_u32<<<1, 1024, 0, st>>>(I.part_u32.p, I.nb_l);
@@ -801,23 +826,56 @@ void launch_eval(hbx_server* S, Slot& B) {
   B.state = 1;
 }
 
-void finish_requests(hbx_server* S, Slot& B, hbx_status status, const std::string& why) {
+// Delivers a request whose rows have all come back (caller holds the lock).
+void deliver(hbx_server* S, Request* r, Clock::time_point now) {
+  std::sort(r->pairs.begin(), r->pairs.end());
+  Result res;
+  res.id = r->id;
+  res.plan = r->plan;
+  res.status = r->status;
+  if (r->status == HBX_OK) {
+    res.l.reserve(r->pairs.size());
+    res.r.reserve(r->pairs.size());
+    for (auto& pr : r->pairs) {
+      res.l.push_back(pr.first);
+      res.r.push_back(pr.second);
+    }
+  }
+  res.comparisons = r->comparisons;
+  res.ms_queued = r->admitted ? ms_between(r->t_submit, r->t_admit) : 0.0;
+  res.ms_total = ms_between(r->t_submit, now);
+  res.batch_requests = r->batch_requests;
+  res.batch_id = r->batch_id;
+  S->done.push_back(std::move(res));
+  S->st.requests_done++;
+  for (size_t k = 0; k < S->active.size(); k++)
+    if (S->active[k].get() == r) {
+      S->active.erase(S->active.begin() + (long)k);
+      break;
+    }
+  S->cv_done.notify_all();
+}
+
+// A batch failed: its requests fail (their other chunks are not dispatched).
+void fail_batch(hbx_server* S, Slot& B, hbx_status status, const std::string& why) {
   const auto now = Clock::now();
   std::lock_guard<std::mutex> lock(S->mu);
-  for (auto& r : B.reqs) {
-    Result res;
-    res.id = r->id;
-    res.plan = r->plan;
-    res.status = status;
-    res.ms_queued = ms_between(r->t_submit, r->t_admit);
-    res.ms_total = ms_between(r->t_submit, now);
-    res.batch_requests = (uint32_t)B.reqs.size();
-    res.batch_id = B.batch_id;
-    S->done.push_back(std::move(res));
+  S->err = why;
+  for (auto& e : B.ents) {
+    Request* r = e.r;
+    r->status = status;
+    r->next = r->n;
+    r->outstanding--;
   }
-  if (status != HBX_OK) S->err = why;
+  for (auto& e : B.ents)
+    if (e.r->outstanding == 0) {
+      Request* r = e.r;
+      e.r = nullptr;
+      bool live = false;
+      for (auto& a : S->active) live = live || a.get() == r;
+      if (live) deliver(S, r, now);
+    }
   S->in_use -= B.est;
-  S->cv_done.notify_all();
 }
 
 // Advances one batch; returns true when something happened.
@@ -871,61 +929,48 @@ bool progress(hbx_server* S, Slot& B) {
     HBX_CUDA(cudaEventElapsedTime(&ms, B.ev_start, B.ev_eval));
     const uint64_t n = B.capacity;
     const uint32_t* ho = (const uint32_t*)B.h_out.p;
-    const size_t nq = B.reqs.size();
-    std::vector<std::vector<std::pair<uint32_t, uint32_t>>> per(nq);
+    const size_t nq = B.ents.size();
+    const uint8_t* h = (const uint8_t*)B.h_ctr.p;
+    const auto now = Clock::now();
+    std::lock_guard<std::mutex> lock(S->mu);
     for (uint64_t k = 0; k < n; k++) {
       const uint32_t l = ho[k];
       const size_t q = (size_t)(std::upper_bound(B.base.begin(), B.base.end(), l) - B.base.begin()) - 1;
-      per[q].emplace_back(l - B.base[q], ho[n + k]);
+      const Entry& e = B.ents[q];
+      e.r->pairs.emplace_back(l - B.base[q] + e.r0, ho[n + k]);
     }
-    const uint8_t* h = (const uint8_t*)B.h_ctr.p;
-    std::vector<uint64_t> cmp(nq, 0);
     uint64_t cmp_all = 0;
     for (size_t i = 0; i < B.inst.size(); i++) {
       uint64_t v;
       std::memcpy(&v, h + sizeof(dev::Counters) + 8 + 8 * i, 8);
-      cmp[B.inst[i].req] += v;
+      B.ents[B.inst[i].req].r->comparisons += v;
       cmp_all += v;
     }
-    const auto now = Clock::now();
-    {
-      std::lock_guard<std::mutex> lock(S->mu);
-      for (size_t q = 0; q < nq; q++) {
-        std::sort(per[q].begin(), per[q].end());
-        Result res;
-        res.id = B.reqs[q]->id;
-        res.plan = B.reqs[q]->plan;
-        res.l.reserve(per[q].size());
-        res.r.reserve(per[q].size());
-        for (auto& pr : per[q]) {
-          res.l.push_back(pr.first);
-          res.r.push_back(pr.second);
-        }
-        res.comparisons = cmp[q];
-        res.ms_queued = ms_between(B.reqs[q]->t_submit, B.reqs[q]->t_admit);
-        res.ms_total = ms_between(B.reqs[q]->t_submit, now);
-        res.batch_requests = (uint32_t)nq;
-        res.batch_id = B.batch_id;
-        S->done.push_back(std::move(res));
-      }
-      S->st.requests_done += nq;
-      S->st.batches++;
-      S->st.rows += B.n_rows;
-      S->st.pair_comparisons += cmp_all;
-      S->st.n_pairs += n;
-      S->st.ms_device += ms;
-      S->in_use -= B.est;
-      S->cv_done.notify_all();
+    for (auto& e : B.ents) {
+      Request* r = e.r;
+      r->batch_requests = std::max<uint32_t>(r->batch_requests, (uint32_t)nq);
+      r->batch_id = B.batch_id;
+      r->outstanding--;
+      if (r->outstanding == 0 && r->next == r->n) deliver(S, r, now);
     }
+    S->st.batches++;
+    S->st.rows += B.n_rows;
+    S->st.pair_comparisons += cmp_all;
+    S->st.n_pairs += n;
+    S->st.ms_device += ms;
+    S->in_use -= B.est;
     B.release();
     return true;
   }
   return false;
 }
 
+// Requests waiting longer than this go ahead of shorter ones.
+constexpr double kAgingMs = 200.0;
+
 void worker_loop(hbx_server* S) {
   cudaSetDevice(S->ctx->device);
-  const uint64_t max_rows = S->opts.max_batch_rows > 0 ? (uint64_t)S->opts.max_batch_rows : 131072u;
+  const uint64_t max_rows = S->opts.max_batch_rows > 0 ? (uint64_t)S->opts.max_batch_rows : 4096u;
   for (;;) {
     bool progressed = false;
     for (auto& sp : S->slots) {
@@ -935,7 +980,7 @@ void worker_loop(hbx_server* S) {
         progressed |= progress(S, B);
       } catch (const Error& e) {
         cudaStreamSynchronize(B.st);
-        finish_requests(S, B, e.status, e.what());
+        fail_batch(S, B, e.status, e.what());
         B.release();
         progressed = true;
       }
@@ -946,22 +991,41 @@ void worker_loop(hbx_server* S) {
         idle = sp.get();
         break;
       }
-    std::vector<std::unique_ptr<Request>> take;
+    std::vector<Entry> ents;
     uint64_t est = 0;
     {
       std::unique_lock<std::mutex> lock(S->mu);
-      if (idle && !S->queue.empty()) {
-        uint64_t rows = 0;
+      if (idle) {
+        // shortest remaining work first (rows not yet dispatched), except that
+        // requests waiting past kAgingMs go first, oldest first
         const auto now = Clock::now();
-        while (!S->queue.empty()) {
-          Request* r = S->queue.front().get();
-          if (!take.empty() && rows + r->n > max_rows) break;
-          if (S->in_use + est + r->est > S->budget && !(S->in_use == 0 && take.empty())) break;
-          rows += r->n;
-          est += r->est;
-          r->t_admit = now;
-          take.push_back(std::move(S->queue.front()));
-          S->queue.pop_front();
+        std::vector<Request*> cand;
+        for (auto& r : S->active)
+          if (r->next < r->n) cand.push_back(r.get());
+        std::sort(cand.begin(), cand.end(), [&](const Request* x, const Request* y) {
+          const bool ax = ms_between(x->t_submit, now) > kAgingMs;
+          const bool ay = ms_between(y->t_submit, now) > kAgingMs;
+          if (ax != ay) return ax;
+          if (ax) return x->t_submit < y->t_submit;
+          const uint32_t rx = x->n - x->next, ry = y->n - y->next;
+          if (rx != ry) return rx < ry;
+          return x->t_submit < y->t_submit;
+        });
+        uint64_t rows = 0;
+        for (Request* r : cand) {
+          const uint32_t take = (uint32_t)std::min<uint64_t>(r->n - r->next, max_rows - rows);
+          if (take == 0) break;
+          const uint64_t e = estimate(S, r->rows, r->plan, r->next, r->next + take);
+          if (S->in_use + est + e > S->budget && !(S->in_use == 0 && ents.empty())) break;
+          ents.push_back(Entry{r, r->next, r->next + take});
+          r->next += take;
+          r->outstanding++;
+          if (!r->admitted) {
+            r->admitted = true;
+            r->t_admit = now;
+          }
+          rows += take;
+          est += e;
         }
         S->in_use += est;
         S->peak = std::max(S->peak, S->in_use);
@@ -969,15 +1033,15 @@ void worker_loop(hbx_server* S) {
       }
       bool busy = false;
       for (auto& sp : S->slots) busy = busy || sp->state != 0;
-      if (take.empty() && !busy) {
-        if (S->stopping && S->queue.empty()) return;
+      if (ents.empty() && !busy) {
+        if (S->stopping && S->active.empty()) return;
         if (!progressed) S->cv_work.wait_for(lock, std::chrono::milliseconds(2));
         continue;
       }
     }
-    if (!take.empty()) {
+    if (!ents.empty()) {
       Slot& B = *idle;
-      B.reqs = std::move(take);
+      B.ents = std::move(ents);
       B.est = est;
       B.batch_id = S->next_batch++;
       try {
@@ -985,7 +1049,7 @@ void worker_loop(hbx_server* S) {
         launch_eval(S, B);
       } catch (const Error& e) {
         cudaStreamSynchronize(B.st);
-        finish_requests(S, B, e.status, e.what());
+        fail_batch(S, B, e.status, e.what());
         B.release();
       }
       progressed = true;
@@ -1037,6 +1101,7 @@ hbx_status hbx_serve_submit(hbx_server* s, uint64_t req_id, int32_t plan, const 
   r->id = req_id;
   r->plan = plan;
   r->t_submit = Clock::now();
+  uint64_t need = 0;
   try {
     if (plan < 0 || plan >= (int32_t)s->plan_rules.size()) fail(HBX_ERR_INVALID_ARG, "no such plan");
     r->rows = table_from_columns(left);
@@ -1044,7 +1109,9 @@ hbx_status hbx_serve_submit(hbx_server* s, uint64_t req_id, int32_t plan, const 
       fail(HBX_ERR_INVALID_ARG, "the request has fewer columns than its plans read");
     if (r->rows.n_rows > (int64_t)(1u << 30)) fail(HBX_ERR_UNSUPPORTED, "request above 2^30 rows");
     r->n = (uint32_t)r->rows.n_rows;
-    r->est = estimate(s, r->rows, plan);
+    // the largest chunk the request can be dispatched in must fit the budget
+    const uint64_t max_rows = s->opts.max_batch_rows > 0 ? (uint64_t)s->opts.max_batch_rows : 4096u;
+    need = estimate(s, r->rows, plan, 0, (uint32_t)std::min<uint64_t>(r->n, max_rows));
   } catch (const Error& e) {
     std::lock_guard<std::mutex> lock(s->mu);
     s->err = e.what();
@@ -1055,13 +1122,18 @@ hbx_status hbx_serve_submit(hbx_server* s, uint64_t req_id, int32_t plan, const 
     s->err = "the server is closing";
     return HBX_ERR_INVALID_ARG;
   }
-  if (r->est > s->budget) {
-    s->err = "request needs " + std::to_string(r->est) + " bytes of device memory; the budget is " +
+  if (need > s->budget) {
+    s->err = "request needs " + std::to_string(need) + " bytes of device memory; the budget is " +
              std::to_string(s->budget);
     return HBX_ERR_CAPACITY;
   }
-  s->queue.push_back(std::move(r));
-  s->cv_work.notify_one();
+  Request* raw = r.get();
+  s->active.push_back(std::move(r));
+  if (raw->n == 0) {
+    deliver(s, raw, Clock::now());  // nothing to evaluate
+  } else {
+    s->cv_work.notify_one();
+  }
   return HBX_OK;
 }
 

@@ -188,13 +188,15 @@ int hbx_run_cli(int argc, const char* const* argv);
  * pair that some rule of that plan accepts (equalities, then similarities,
  * as in hbx_block), over all pairs (one partition).
  *
- * A worker thread admits queued requests in arrival order while the device
- * memory they need fits the budget, encodes each admitted group of requests
- * as one batch and evaluates every (request, rule) pair of the batch in one
- * persistent launch; up to max_inflight batches are on the device at once,
- * so requests that arrive while others run are admitted as soon as a batch
- * slot and memory free up (continuous batching).  A request's result does
- * not depend on what it was batched with.
+ * A worker thread forms batches of up to max_batch_rows records from the
+ * queued requests while the device memory they need fits the budget: a
+ * request is dispatched in row chunks, requests with the fewest records left
+ * go first (requests waiting over 200 ms go ahead of them), and each batch
+ * evaluates every (chunk, rule) pair in one persistent launch.  Up to
+ * max_inflight batches are on the device at once, so requests that arrive
+ * while others run are admitted as soon as a batch slot and memory free up
+ * (continuous batching).  A request's result does not depend on what it was
+ * batched with or how it was chunked.
  *
  * hbx_serve_submit and hbx_serve_poll may be called from any threads; one
  * thread at a time should poll.  The server uses its context's device and
@@ -202,7 +204,7 @@ int hbx_run_cli(int argc, const char* const* argv);
 typedef struct hbx_serve_opts {
   uint32_t struct_size;     /* sizeof(hbx_serve_opts) */
   int32_t max_inflight;     /* batches on the device at once, 0 = 2 */
-  int64_t max_batch_rows;   /* left rows per batch, 0 = 131072 */
+  int64_t max_batch_rows;   /* left records per batch, 0 = 4096 */
   uint64_t budget_bytes;    /* device memory for batches in flight, 0 = half of the free memory */
   int32_t tile_right;       /* right rows per work item, 0 = 128 */
   int32_t eval_variant;     /* evaluation kernel as hbx_opts, 0 = 2 CTAs/SM */
@@ -239,7 +241,8 @@ typedef struct hbx_serve_stats {
 hbx_status hbx_serve_open(hbx_ctx* ctx, const hbx_plan* const* plans, int32_t n_plans,
                           const hbx_table* right, const hbx_serve_opts* opts, hbx_server** out);
 /* Copies the records and queues the request; returns at once.  A request
- * that alone exceeds the budget is refused with HBX_ERR_CAPACITY. */
+ * whose first chunk alone exceeds the budget is refused with
+ * HBX_ERR_CAPACITY. */
 hbx_status hbx_serve_submit(hbx_server* s, uint64_t req_id, int32_t plan, const hbx_columns* left);
 /* Waits up to timeout_ms (< 0: no limit) for a finished request and returns
  * it; HBX_ERR_TIMEOUT when none finished in time.  out->status is the
