@@ -23,6 +23,11 @@ Jaro-Winkler pair evaluation and compaction of the matching pairs.
   the ``roofline`` block for the conventions), ``cpu_baseline``: the oracle
   (the reference's brute-force algorithm restated in C++) on all host cores.
 
+At N=1 two more workloads are measured and reported in the same line:
+``c3`` (1M x 1M rows, 8 rules, 64 Zipf-sized partitions: batched vs plain)
+and ``serving`` (10M resident right rows, a Poisson trace of left-record
+requests: p50/p99/p999 latency and pair-comparisons/s); ``--sections`` picks.
+
 ``--impl reference`` times that CPU implementation alone and prints the same
 line with ``"impl": "reference"``.  With N > 1 GPUs (torchrun) every rank runs
 an independent replica (weak scaling); the path needs no collective.
@@ -180,6 +185,130 @@ def cpu_baseline(paths, n_partitions, target_s=15.0, steps=1, warmup=0, step_fra
                       f"{sum(cmps)} pair-comparisons in {sum(secs):.2f} s)"}
 
 
+def bench_c3(args, ctx, dev):
+    """C3: 1M x 1M rows, 8 rules, 64 Zipf-sized partitions; batched vs plain.
+
+    One untimed batched step (it also runs the tile autotuner and sizes the
+    output), then args.c3_steps timed steps of each form, CUDA events around
+    each step on the launching stream; the inputs (about 200 MB a side) are
+    larger than L2."""
+    import torch
+
+    import hyperblocker_gb300 as hb
+    from hyperblocker_gb300 import synth_big
+
+    n = args.c3_rows
+    w = synth_big.c3(n, n, max(1, n // 50))
+    plan = hb.Plan.from_yaml(w.rules, ctx)
+    L = hb.Table.from_columns(w.left.cols, ctx)
+    R = hb.Table.from_columns(w.right.cols, ctx)
+    sess = hb.Session(ctx, plan, L, R, w.n_partitions)
+    stream = torch.cuda.Stream(device=dev)
+    m = sess.count("batched", stream.cuda_stream)
+    cap = max(1, m)
+    out_l = torch.empty(cap, dtype=torch.int32, device=dev)
+    out_r = torch.empty(cap, dtype=torch.int32, device=dev)
+    res = {}
+    for mode in ("batched", "plain"):
+        sess.run_device(mode, out_l.data_ptr(), out_r.data_ptr(), cap, stream.cuda_stream)  # warm
+        ms, ms_eval, ops = [], [], []
+        for _ in range(args.c3_steps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                e0.record(stream)
+                sess.run_device(mode, out_l.data_ptr(), out_r.data_ptr(), cap, stream.cuda_stream)
+                e1.record(stream)
+            e1.synchronize()
+            st = sess.stats()
+            ms.append(e0.elapsed_time(e1))
+            ms_eval.append(st.ms_eval)
+            ops.append(st.jw_word_ops)
+        res[mode] = {"value": st.pair_comparisons / (statistics.mean(ms) / 1000.0),
+                     "ms_per_step": statistics.mean(ms), "ms_eval": statistics.mean(ms_eval),
+                     "launches_per_step": int(st.n_launches)}
+    st = sess.stats()
+    out = {"workload": f"c3: {n:,} x {n:,} synthetic rows (+1 header row each), 8 rules (1-2 "
+                       "equalities, 1-3 JW predicates, thresholds U[0.80,0.95]), 64 partitions "
+                       "keyed by a Zipf(1.3) column", "steps": args.c3_steps,
+           "pair_comparisons_per_step": int(st.pair_comparisons),
+           "pairs_covered_per_step": int(st.pairs_covered),
+           "matches_per_step": int(m), "unit": UNIT,
+           "batched": res["batched"], "plain": res["plain"],
+           "batched_vs_plain": res["batched"]["value"] / res["plain"]["value"],
+           "jw_word_ops_per_step": int(statistics.mean(ops)),
+           "alu_tops_eval": statistics.mean(ops) / (res["batched"]["ms_eval"] / 1000.0) / 1e12}
+    sess.close()
+    return out
+
+
+def bench_serving(args, ctx):
+    """C4: a resident right table of args.serve_rows rows; args.serve_requests
+    requests of log-uniform 1-50k left records arriving Poisson at
+    args.serve_rate per second, each naming one of 4 rules.  Requests are
+    submitted at their arrival times from this thread and their results
+    polled; latency = submit -> result ready (host clock)."""
+    import numpy as np
+
+    import hyperblocker_gb300 as hb
+    from hyperblocker_gb300 import synth_big
+
+    right = synth_big.c4_right(args.serve_rows)
+    reqs = synth_big.c4_requests(right, args.serve_requests, rate=args.serve_rate, seed=1)
+    plans = [hb.Plan.from_yaml([d], ctx) for d in synth_big.SERVE_RULES]
+    R = hb.Table.from_columns(right.cols, ctx)
+    del right
+    t = time.perf_counter()
+    srv = hb.Server(ctx, plans, R)
+    t_open = time.perf_counter() - t
+    for k in range(len(plans)):  # warm: one small request per plan
+        srv.submit(1 << 40 | k, k, reqs[0].cols)
+    for _ in range(len(plans)):
+        srv.poll(-1)
+    s0 = srv.stats()
+    n = len(reqs)
+    got, sent = {}, 0
+    t0 = time.perf_counter()
+    while len(got) < n:
+        now = time.perf_counter() - t0
+        while sent < n and reqs[sent].t_arrival <= now:
+            srv.submit(sent, reqs[sent].rule, reqs[sent].cols)
+            sent += 1
+        r = srv.poll(0 if sent < n else 50)
+        while r is not None:
+            got[r["id"]] = r
+            r = srv.poll(0)
+        if sent < n:
+            dt = reqs[sent].t_arrival - (time.perf_counter() - t0)
+            if dt > 0:
+                time.sleep(min(dt, 0.0005))
+    wall = time.perf_counter() - t0
+    s1 = srv.stats()
+    srv.close()
+    lat = np.array([got[i]["ms_total"] for i in range(n)])
+    size = np.array([reqs[i].n_rows for i in range(n)])
+    mid = lat[(size >= 5000) & (size <= 20000)]
+    cmp = sum(got[i]["comparisons"] for i in range(n))
+    bad = sum(1 for i in range(n) if got[i]["status"] != hb.OK)
+    pct = lambda a, q: float(np.percentile(a, q)) if len(a) else None
+    return {"workload": f"c4: {args.serve_rows:,} resident right rows; {n} requests of "
+                        "log-uniform 1-50,000 left records, Poisson arrivals at "
+                        f"{args.serve_rate:g}/s, one of 4 rules (year and venue equalities, "
+                        "1-2 JW predicates) each", "requests": n, "failed": bad,
+            "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99), "p999_ms": pct(lat, 99.9),
+            "max_ms": float(lat.max()),
+            "p50_ms_5k_20k_rows": pct(mid, 50), "p99_ms_5k_20k_rows": pct(mid, 99),
+            "requests_5k_20k_rows": int(len(mid)),
+            "pair_comparisons_per_s": cmp / wall, "unit": UNIT,
+            "records_per_s": float(size.sum()) / wall, "trace_s": float(reqs[-1].t_arrival),
+            "wall_s": wall, "device_busy_frac": (s1.ms_device - s0.ms_device) / 1000.0 / wall,
+            "batches": int(s1.batches - s0.batches),
+            "mean_batch_requests": float(np.mean([got[i]["batch_requests"] for i in range(n)])),
+            "open_s": t_open, "resident_bytes": int(s1.resident_bytes),
+            "latency": "submit -> result ready, host clock; requests submitted at their "
+                       "arrival times"}
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
@@ -313,6 +442,8 @@ def run_engine(args, rank, world, local_rank):
             "frac": achieved / peak_tops,
             "traffic": _traffic_per_launch(),
             "ops_per_launch": ops, "ms_per_launch": ms_eval,
+            "tile_right": int(sess.stats().tile_right),
+            "eval_variant": int(sess.stats().eval_variant),
             "peak_source": f"nominal: {n_sm} SMs x 128 INT32 lanes / 2 per 64-bit op x "
                            f"{sm_max:.0f} MHz (sm_max_mhz of MEASURED_PEAKS.json); "
                            "MEASURED_PEAKS.json has no integer-pipe figure",
@@ -321,6 +452,11 @@ def run_engine(args, rank, world, local_rank):
         cb = None
         if world == 1 and not args.no_cpu_baseline:
             cb = cpu_baseline(paths, w.n_partitions)
+        extra = {}
+        if world == 1 and "c3" in args.sections:
+            extra["c3"] = bench_c3(args, ctx, dev)
+        if world == 1 and "serve" in args.sections:
+            extra["serving"] = bench_serving(args, ctx)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -345,6 +481,7 @@ def run_engine(args, rank, world, local_rank):
         if cb:
             line["cpu_baseline"] = {"value": cb["value"], "unit": UNIT, "cores": cb["cores"],
                                     "kind": "port", "sample": cb["sample"]}
+        line.update(extra)
         print(json.dumps(line), flush=True)
     sess.close()
     ctx.close()
@@ -361,7 +498,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--sections", default="c3,serve",
+                    help="extra measurements at N=1, comma separated: c3 (1M x 1M batching "
+                         "workload), serve (resident-table serving trace); '' for none")
+    ap.add_argument("--c3-rows", type=int, default=1_000_000)
+    ap.add_argument("--c3-steps", type=int, default=2)
+    ap.add_argument("--serve-rows", type=int, default=10_000_000)
+    ap.add_argument("--serve-requests", type=int, default=800)
+    ap.add_argument("--serve-rate", type=float, default=200.0)
     args = ap.parse_args()
+    args.sections = [x for x in args.sections.split(",") if x]
     if args.warmup < 3:
         args.warmup = 3
     rank = _env_int("RANK", 0)

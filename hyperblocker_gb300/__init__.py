@@ -74,7 +74,8 @@ class Stats(ctypes.Structure):
                 ("ms_last_run", ctypes.c_double), ("ms_join", ctypes.c_double),
                 ("ms_eval", ctypes.c_double), ("jw_word_ops", ctypes.c_uint64),
                 ("h2d_bytes", ctypes.c_uint64), ("ms_create", ctypes.c_double),
-                ("ingest_on_device", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("ingest_on_device", ctypes.c_uint32), ("tile_right", ctypes.c_uint32),
+                ("eval_variant", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
     def as_dict(self) -> Dict[str, float]:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -409,6 +410,15 @@ class Session:
             raise HbxError(st, f"needs capacity {p.n_required}")
         _check(st, self.ctx.h)
         return int(p.n_written)
+
+    def count(self, mode, stream_ptr: Optional[int] = None) -> int:
+        """Runs once without an output buffer; returns the number of matches
+        (the capacity a run_device call needs)."""
+        p = Pairs(None, None, 0, 0, 0)
+        st = lib().hbx_session_run(self.h, _mode(mode), ctypes.byref(p), stream_ptr)
+        if st not in (OK, ERR_CAPACITY):
+            _check(st, self.ctx.h)
+        return int(p.n_required)
 
     def stats(self) -> Stats:
         s = Stats()

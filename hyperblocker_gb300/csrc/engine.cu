@@ -424,6 +424,14 @@ void grow_output(hbx_session* S, uint64_t need) {
   }
 }
 
+// Output pairs a repeated run must have room for: the distinct pairs of a
+// run whose output overflowed, or (duplicate set full) its pass count.
+uint64_t needed_capacity(const hbx_session* S, const dev::Counters& c) {
+  uint64_t need = c.out_count;
+  if (c.seen_overflow) need = std::max<uint64_t>(need, c.passes);
+  return std::max<uint64_t>(need, S->out_l.n + 1);
+}
+
 dev::Counters read_counters(hbx_session* S, cudaStream_t st) {
   dev::Counters c{};
   HBX_CUDA(cudaMemcpyAsync(&c, S->d_ctr.p, sizeof c, cudaMemcpyDeviceToHost, st));
@@ -630,23 +638,31 @@ void autotune(hbx_session* S, cudaStream_t st) {
   std::vector<int> variants = {0, 1};
   if (o.tile_right > 0) tiles = {(uint32_t)o.tile_right};
   if (o.eval_variant > 0) variants = {o.eval_variant - 1};
-  float best = 1e30f;
-  uint32_t best_tr = tiles[0];
-  int best_v = variants[0];
+  std::vector<std::pair<uint32_t, int>> cand;
   for (uint32_t tr : tiles)
-    for (int v : variants) {
-      configure(S, tr, v);
-      timed_batched_run(S, st);  // warm: caches, and the output buffer size
+    for (int v : variants) cand.emplace_back(tr, v);
+  // interleaved rounds, best time per candidate: drifts of clock or cache
+  // state hit every candidate alike; one round when runs are long
+  std::vector<float> best_ms(cand.size(), 1e30f);
+  for (int round = 0; round < 3; round++) {
+    for (size_t k = 0; k < cand.size(); k++) {
+      configure(S, cand[k].first, cand[k].second);
+      float ms = timed_batched_run(S, st);
       const dev::Counters c = read_counters(S, st);
-      if (c.out_count > S->out_l.n || c.seen_overflow)
-        grow_output(S, std::max<uint64_t>(c.out_count + c.seen_overflow, S->out_l.n + 1));
-      const float ms = std::min(timed_batched_run(S, st), timed_batched_run(S, st));
-      if (ms < best) {
-        best = ms;
-        best_tr = tr;
-        best_v = v;
+      if (c.out_count > S->out_l.n || c.seen_overflow) {
+        grow_output(S, needed_capacity(S, c));
+        ms = timed_batched_run(S, st);
       }
+      best_ms[k] = std::min(best_ms[k], ms);
     }
+    if (*std::min_element(best_ms.begin(), best_ms.end()) >= 50.0f) break;
+  }
+  size_t bk = 0;
+  for (size_t k = 1; k < cand.size(); k++)
+    if (best_ms[k] < best_ms[bk]) bk = k;
+  const uint32_t best_tr = cand[bk].first;
+  const int best_v = cand[bk].second;
+  const float best = best_ms[bk];
   configure(S, best_tr, best_v);
   char buf[64];
   std::snprintf(buf, sizeof buf, "%u, %d, %.4f", best_tr, best_v, best);
@@ -731,6 +747,8 @@ void session_run(hbx_session* S, hbx_mode mode, cudaStream_t st) {
     S->stats.fma_ambiguous = c.ambiguous;
     S->stats.long_string_pairs = c.long_pairs;
     S->stats.n_launches = launches;
+    S->stats.tile_right = S->tile_right;
+    S->stats.eval_variant = (uint32_t)S->variant + 1;
     unsigned long long total_items = 0;
     HBX_CUDA(cudaMemcpyAsync(&total_items, S->d_rule_base.p + S->rb.size(), sizeof total_items,
                              cudaMemcpyDeviceToHost, st));
@@ -741,7 +759,7 @@ void session_run(hbx_session* S, hbx_mode mode, cudaStream_t st) {
       fail(HBX_ERR_CUDA, "evaluation finished " + std::to_string(c.items_done) + " of " +
                              std::to_string(total_items) + " work items");
     if (c.out_count <= S->out_l.n && c.seen_overflow == 0) return;
-    grow_output(S, std::max<uint64_t>(c.out_count + c.seen_overflow, S->out_l.n + 1));
+    grow_output(S, needed_capacity(S, c));
   }
   fail(HBX_ERR_CAPACITY, "output kept growing");
 }

@@ -518,14 +518,19 @@ struct Stage {
 // of them (the reference stops at the first rule that passes,
 // global_func.cuh:161-165); a device hash set of emitted (left, right) keys
 // keeps exactly one report.  Open addressing with linear probing over
-// seen_mask + 1 slots (all ones = empty); if the probe runs past its limit the
-// set is too small: the pair is counted in seen_overflow and the host reruns
-// with a larger set.
+// seen_mask + 1 slots (all ones = empty).  The set is sized for a load of at
+// most one half, where probe runs stay far below kMaxProbes; a run past it
+// means the set is too small for this run's distinct pairs: seen_overflow is
+// set, the host repeats the run with a set sized from the pass count
+// (Counters::passes, an upper bound on the distinct pairs), and the reports
+// left in this run skip the set.
+constexpr unsigned long long kMaxProbes = 4096;
 __device__ __forceinline__ bool first_report(const EvalParams& P, uint32_t lrow, uint32_t rrow) {
+  if (*(volatile unsigned long long*)&P.ctr->seen_overflow) return false;
   const unsigned long long key = ((unsigned long long)lrow << 32) | rrow;
   unsigned long long h = key * 0x9E3779B97F4A7C15ull;
   h ^= h >> 29;
-  for (unsigned long long probe = 0; probe <= P.seen_mask; probe++) {
+  for (unsigned long long probe = 0; probe <= P.seen_mask && probe < kMaxProbes; probe++) {
     const unsigned long long slot = (h + probe) & P.seen_mask;
     const unsigned long long prev = atomicCAS(P.seen + slot, ~0ull, key);
     if (prev == ~0ull) return true;
@@ -538,7 +543,12 @@ __device__ __forceinline__ bool first_report(const EvalParams& P, uint32_t lrow,
 // Emits final matches of one warp step with one atomic per warp.
 __device__ __forceinline__ void emit(const EvalParams& P, bool pass, uint32_t lrow, uint32_t rrow,
                                      int lane) {
-  if (pass && P.seen) pass = first_report(P, lrow, rrow);
+  if (P.seen) {
+    const unsigned cm = __ballot_sync(kFull, pass);
+    if (!cm) return;
+    if (lane == 0) atomicAdd(&P.ctr->passes, (unsigned long long)__popc(cm));
+    if (pass) pass = first_report(P, lrow, rrow);
+  }
   const unsigned pm = __ballot_sync(kFull, pass);
   if (!pm) return;
   unsigned long long base = 0;

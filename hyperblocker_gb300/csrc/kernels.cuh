@@ -174,7 +174,8 @@ struct Counters {
   unsigned long long watchdog_trips;
   unsigned long long items_done;
   unsigned long long jw_word_ops;  // algorithmic work of the JW evaluations
-  unsigned long long seen_overflow;  // pairs the duplicate set had no room for
+  unsigned long long seen_overflow;  // nonzero: the duplicate set had no room (run repeats)
+  unsigned long long passes;  // rule-level passes before de-duplication (plans with several rules)
 };
 
 struct EvalParams {

@@ -896,7 +896,8 @@ bool progress(hbx_server* S, Slot& B) {
       // grow and evaluate again (the join is unchanged)
       PoolScope scope(S->ctx->pool, B.st);
       uint64_t cap = B.capacity;
-      while (cap < c.out_count + c.seen_overflow) cap *= 2;
+      const uint64_t need = c.seen_overflow ? std::max<uint64_t>(c.out_count, c.passes) : c.out_count;
+      while (cap < need || cap == B.capacity) cap *= 2;
       B.capacity = cap;
       B.out_l.alloc(cap);
       B.out_r.alloc(cap);

@@ -340,10 +340,12 @@ void run_static(int device, const hbx_plan* plan, const hbx_table* left, const h
                                   cudaMemcpyDeviceToHost, st));
   HBX_STATIC_CUDA(cudaStreamSynchronize(st));
   if (c.items_done != total_items) hbx::fail(HBX_ERR_CUDA, "evaluation did not finish its work");
-  out->n_required = c.out_count + c.seen_overflow;
+  out->n_required = c.seen_overflow ? std::max<uint64_t>(c.out_count, c.passes) : c.out_count;
   out->n_written = 0;
   if (stats) {
     *stats = hbx_stats{};
+    stats->tile_right = Y.tile_right;
+    stats->eval_variant = 1;
     stats->pairs_covered = E.pairs_covered;
     stats->pair_comparisons = c.comparisons;
     stats->n_matches = c.out_count;

@@ -115,6 +115,8 @@ typedef struct hbx_stats {
   uint64_t h2d_bytes;         /* bytes uploaded when the session was created */
   double ms_create;           /* host wall time of the session's creation */
   uint32_t ingest_on_device;  /* 1 when the tables were encoded on the device */
+  uint32_t tile_right;        /* right rows per work item of the last run */
+  uint32_t eval_variant;      /* evaluation kernel of the last run (hbx_opts numbering) */
   uint32_t reserved;
 } hbx_stats;
 
