@@ -442,6 +442,8 @@ def run_engine(args, rank, world, local_rank):
             "frac": achieved / peak_tops,
             "traffic": _traffic_per_launch(),
             "ops_per_launch": ops, "ms_per_launch": ms_eval,
+            "pairs_scanned_per_launch": int(sess.stats().pairs_scanned),
+            "scan_steps_per_launch": int(sess.stats().scan_steps),
             "tile_right": int(sess.stats().tile_right),
             "eval_variant": int(sess.stats().eval_variant),
             "peak_source": f"nominal: {n_sm} SMs x 128 INT32 lanes / 2 per 64-bit op x "

@@ -75,7 +75,8 @@ class Stats(ctypes.Structure):
                 ("ms_eval", ctypes.c_double), ("jw_word_ops", ctypes.c_uint64),
                 ("h2d_bytes", ctypes.c_uint64), ("ms_create", ctypes.c_double),
                 ("ingest_on_device", ctypes.c_uint32), ("tile_right", ctypes.c_uint32),
-                ("eval_variant", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("eval_variant", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("pairs_scanned", ctypes.c_uint64), ("scan_steps", ctypes.c_uint64)]
 
     def as_dict(self) -> Dict[str, float]:
         return {k: getattr(self, k) for k, _ in self._fields_}

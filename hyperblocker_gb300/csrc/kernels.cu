@@ -177,6 +177,132 @@ __global__ void k_items_final(const Rule* rules, uint32_t rule, uint32_t tile_ri
   }
 }
 
+// ---- fused join for small key domains (every rule's left key domain at most
+// kFusedJoinMaxDomain): one launch each for keys + histograms, offsets + work
+// items, and the scatter, covering every rule and both tables.
+
+// Keys and key histograms of every rule for both tables; histograms of
+// domains up to kSharedHistKeys are kept per block in shared memory.
+__global__ void k_join_count(Side L, Side R, const Rule* rules, uint32_t n_rules) {
+  extern __shared__ uint32_t s_cnt[];
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x;
+  for (uint32_t r = 0; r < n_rules; r++) {
+    const Rule& Q = rules[r];
+    for (int side = 0; side < 2; side++) {
+      const Side& S = side ? R : L;
+      const uint32_t D = side ? Q.domain : Q.domain_l;
+      uint32_t* keys = side ? Q.key_r : Q.key_l;
+      uint32_t* cnt = side ? Q.cnt_r : Q.cnt_l;
+      const bool split = !side && Q.n_wclass > 1;
+      const bool sh = D <= kSharedHistKeys;
+      if (sh) {
+        for (uint32_t k = threadIdx.x; k < D; k += blockDim.x) s_cnt[k] = 0;
+        __syncthreads();
+      }
+      for (uint32_t row = t0; row < S.n_rows; row += stride) {
+        uint32_t k = row_key(S, Q, row);
+        if (split) k += Q.domain * word_class(S.str_meta[(size_t)Q.wclass_slot * S.n_rows + row].loc.y);
+        keys[row] = k;
+        atomicAdd(sh ? s_cnt + k : cnt + k, 1u);
+      }
+      if (sh) {
+        __syncthreads();
+        for (uint32_t k = threadIdx.x; k < D; k += blockDim.x)
+          if (s_cnt[k]) atomicAdd(cnt + k, s_cnt[k]);
+        __syncthreads();
+      }
+    }
+  }
+}
+
+// One block (1024 threads) per rule: row offsets per key for both tables,
+// work items per left key, and the rule's pair-comparison count.
+__global__ void k_join_scan(const Rule* rules, uint32_t tile_right, unsigned long long* comparisons) {
+  __shared__ uint32_t s_w32[32];
+  __shared__ uint32_t s_t32;
+  __shared__ unsigned long long s_w64[32];
+  __shared__ unsigned long long s_t64, s_p64;
+  const Rule& Q = rules[blockIdx.x];
+  // row offsets: left keys, then right keys
+  for (int side = 0; side < 2; side++) {
+    const uint32_t D = side ? Q.domain : Q.domain_l;
+    const uint32_t* cnt = side ? Q.cnt_r : Q.cnt_l;
+    uint32_t* off = side ? Q.off_r : Q.off_l;
+    uint32_t carry = 0;
+    for (uint32_t base = 0; base < D; base += kScanChunk) {
+      const uint32_t b = base + threadIdx.x * 4u;
+      uint32_t v[4], sum = 0;
+      for (int k = 0; k < 4; k++) {
+        v[k] = b + k < D ? cnt[b + k] : 0u;
+        sum += v[k];
+      }
+      uint32_t ex = block_excl_scan<uint32_t>(sum, s_w32, &s_t32) + carry;
+      for (int k = 0; k < 4; k++) {
+        if (b + k < D) off[b + k] = ex;
+        ex += v[k];
+      }
+      carry += s_t32;
+      __syncthreads();
+    }
+  }
+  // work items per left key (exclusive, with the total at domain_l)
+  unsigned long long carry = 0, pairs = 0;
+  for (uint32_t base = 0; base < Q.domain_l; base += kScanChunk) {
+    const uint32_t b = base + threadIdx.x * 4u;
+    unsigned long long v[4], sum = 0, pr = 0;
+    for (int k = 0; k < 4; k++) {
+      unsigned long long p = 0;
+      v[k] = b + k < Q.domain_l ? key_items(Q, b + k, tile_right, &p) : 0ull;
+      sum += v[k];
+      pr += p;
+    }
+    unsigned long long ex = block_excl_scan<unsigned long long>(sum, s_w64, &s_t64) + carry;
+    for (int k = 0; k < 4; k++) {
+      if (b + k < Q.domain_l) Q.item_off[b + k] = ex;
+      ex += v[k];
+    }
+    carry += s_t64;
+    block_excl_scan<unsigned long long>(pr, s_w64, &s_p64);
+    pairs += s_p64;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    Q.item_off[Q.domain_l] = carry;
+    if (pairs) atomicAdd(comparisons, pairs);
+  }
+}
+
+// Rows of every rule grouped by key (counting-sort scatter, right rows with
+// their first similarity column's metadata), and the rules' item bases.
+__global__ void k_join_scatter(Side L, Side R, const Rule* rules, uint32_t n_rules,
+                               unsigned long long* rule_base) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    unsigned long long acc = 0;
+    for (uint32_t r = 0; r < n_rules; r++) {
+      rule_base[r] = acc;
+      acc += rules[r].item_off[rules[r].domain_l];
+    }
+    rule_base[n_rules] = acc;
+  }
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x;
+  for (uint32_t r = 0; r < n_rules; r++) {
+    const Rule& Q = rules[r];
+    for (uint32_t row = t0; row < L.n_rows; row += stride) {
+      const uint32_t k = Q.key_l[row];
+      Q.sorted_l[Q.off_l[k] + atomicAdd(Q.cur_l + k, 1u)] = row;
+    }
+    const StrMeta* meta_in = R.str_meta + (size_t)Q.sim_r[0] * R.n_rows;
+    for (uint32_t row = t0; row < R.n_rows; row += stride) {
+      const uint32_t k = Q.key_r[row];
+      const uint32_t pos = Q.off_r[k] + atomicAdd(Q.cur_r + k, 1u);
+      Q.sorted_r[pos] = row;
+      if (Q.sorted_meta_r) Q.sorted_meta_r[pos] = meta_in[row];
+    }
+  }
+}
+
 __global__ void k_rule_base(const Rule* rules, uint32_t n_rules, unsigned long long* base) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
     unsigned long long acc = 0;
@@ -522,15 +648,18 @@ struct Stage {
 // most one half, where probe runs stay far below kMaxProbes; a run past it
 // means the set is too small for this run's distinct pairs: seen_overflow is
 // set, the host repeats the run with a set sized from the pass count
-// (Counters::passes, an upper bound on the distinct pairs), and the reports
-// left in this run skip the set.
+// (Counters::passes, an upper bound on the distinct pairs).  Reports whose
+// probe run reaches kCheckProbe look at the overflow flag first and give up
+// once it is set, so an overflowing run costs a few probes per report; runs
+// of a set sized as intended rarely get that far and never read the flag.
 constexpr unsigned long long kMaxProbes = 4096;
+constexpr unsigned long long kCheckProbe = 8;
 __device__ __forceinline__ bool first_report(const EvalParams& P, uint32_t lrow, uint32_t rrow) {
-  if (*(volatile unsigned long long*)&P.ctr->seen_overflow) return false;
   const unsigned long long key = ((unsigned long long)lrow << 32) | rrow;
   unsigned long long h = key * 0x9E3779B97F4A7C15ull;
   h ^= h >> 29;
   for (unsigned long long probe = 0; probe <= P.seen_mask && probe < kMaxProbes; probe++) {
+    if (probe == kCheckProbe && *(volatile unsigned long long*)&P.ctr->seen_overflow) return false;
     const unsigned long long slot = (h + probe) & P.seen_mask;
     const unsigned long long prev = atomicCAS(P.seen + slot, ~0ull, key);
     if (prev == ~0ull) return true;
@@ -602,6 +731,14 @@ __device__ __forceinline__ uint32_t prefix16(const uint4& a, const uint4& b) {
   return 16u;
 }
 
+// Per-lane work counts of the evaluation loop, summed into Counters at exit:
+// algorithmic JW word operations (every evaluation, scanned or not), pairs
+// that reached a bit-parallel scan, and scan steps (4 symbols each).
+struct WorkTally {
+  unsigned long long ops;
+  uint32_t scans, steps;
+};
+
 constexpr uint32_t kPrefixUnknown = 0xffu;
 constexpr uint32_t kRing = kRingEntries;  // per-warp ring of pairs waiting for a scan
 
@@ -613,7 +750,7 @@ constexpr uint32_t kRing = kRingEntries;  // per-warp ring of pairs waiting for 
 // Returns the rows appended.
 __device__ __forceinline__ uint32_t filter_batch(const EvalParams& P, const Stage& A, uint32_t e0,
                                                  uint32_t tail, uint32_t lrow, uint32_t* lw,
-                                                 unsigned long long* ops) {
+                                                 WorkTally* ops) {
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
   const uint32_t nR = P.R.n_rows;
@@ -639,7 +776,7 @@ __device__ __forceinline__ uint32_t filter_batch(const EvalParams& P, const Stag
       pass = jw_exact(0, A.la, 0, 0, A.thr, &P.ctr->ambiguous);
     } else {
       const uint32_t ls = min(A.la, lb), ll = max(A.la, lb);
-      *ops += jw_eval_ops(ls, ll);
+      ops->ops += jw_eval_ops(ls, ll);
       const uint32_t p16 = prefix16(A.a_head, m.head);
       if (p16 == 16u && ls > 16u) {
         scan = true;  // prefix longer than 16: measured exactly before the scan
@@ -678,7 +815,7 @@ __device__ __forceinline__ uint32_t filter_batch(const EvalParams& P, const Stag
 // last stage); returns their count.
 template <int W>
 __device__ __forceinline__ uint32_t run_stage(const EvalParams& P, const Stage& A, uint32_t lrow,
-                                           unsigned long long* ops) {
+                                           WorkTally* ops) {
   constexpr int S = row_words(W);
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
@@ -725,6 +862,7 @@ __device__ __forceinline__ uint32_t run_stage(const EvalParams& P, const Stage& 
         allowed = (int)n_iter - need;
         i = 0;
         busy = true;
+        ops->scans++;
         if (n_iter > 16u) nxt = __ldg(reinterpret_cast<const uint4*>(b + 16));
 #pragma unroll
         for (int k = 0; k < W; k++) {
@@ -749,6 +887,7 @@ __device__ __forceinline__ uint32_t run_stage(const EvalParams& P, const Stage& 
       for (int c = 0; c < 4; c++)
         bp_step<W, S>(A.tab, (wd >> (8 * c)) & 0xffu, win, mt, (i + (uint32_t)c) < h ? 1u : 0u);
       i += 4;
+      ops->steps++;
       if (i >= n_iter || (i & 15u) == 0) {
         uint32_t m = 0;
 #pragma unroll
@@ -773,7 +912,7 @@ __device__ __forceinline__ uint32_t run_stage(const EvalParams& P, const Stage& 
 // Stage over a left string the fast path does not take (longer than 256
 // bytes, or no room for its table): the reference's own loops per lane.
 __device__ __forceinline__ uint32_t run_stage_slow(const EvalParams& P, const Stage& A,
-                                                   unsigned long long* ops, uint32_t lrow) {
+                                                   WorkTally* ops, uint32_t lrow) {
   const int lane = threadIdx.x & 31;
   uint32_t lw = 0;
   for (uint32_t e0 = 0; e0 < A.n; e0 += 32) {
@@ -783,7 +922,7 @@ __device__ __forceinline__ uint32_t run_stage_slow(const EvalParams& P, const St
     bool pass = false;
     if (act) {
       const uint4 mb = P.R.str_meta[(size_t)A.slot_r * P.R.n_rows + rrow].loc;
-      if (mb.y && A.la) *ops += jw_eval_ops(min(A.la, mb.y), max(A.la, mb.y));
+      if (mb.y && A.la) ops->ops += jw_eval_ops(min(A.la, mb.y), max(A.la, mb.y));
       pass = sim_pass_slow(A.a, A.la, P.R.arena + 16ull * mb.x, mb.y, A.thr, P.ctr);
     }
     __syncwarp();
@@ -794,7 +933,7 @@ __device__ __forceinline__ uint32_t run_stage_slow(const EvalParams& P, const St
 }
 
 __device__ __forceinline__ uint32_t stage_dispatch(uint32_t W, const EvalParams& P, const Stage& A,
-                                                   uint32_t lrow, unsigned long long* ops) {
+                                                   uint32_t lrow, WorkTally* ops) {
   switch (W) {
     case 1: return run_stage<1>(P, A, lrow, ops);
     case 2: return run_stage<2>(P, A, lrow, ops);
@@ -889,7 +1028,7 @@ __device__ __forceinline__ void eval_body(const EvalParams& P) {
   uint32_t c_rule = 0xffffffffu, c_key = 0;
   unsigned long long c_lo = 1, c_hi = 0;
   unsigned long long done = 0;
-  unsigned long long ops = 0;
+  WorkTally tally{0ull, 0u, 0u};
 
   for (;;) {
     unsigned long long v = 0;
@@ -979,9 +1118,9 @@ __device__ __forceinline__ void eval_body(const EvalParams& P) {
         uint32_t n_next;
         if (fast) {
           A.tab = tab;
-          n_next = stage_dispatch(W, P, A, lrow, &ops);
+          n_next = stage_dispatch(W, P, A, lrow, &tally);
         } else {
-          n_next = run_stage_slow(P, A, &ops, lrow);
+          n_next = run_stage_slow(P, A, &tally, lrow);
         }
         A.meta = nullptr;  // later stages: survivors kept in A.rows
         A.n = n_next;
@@ -1001,8 +1140,17 @@ __device__ __forceinline__ void eval_body(const EvalParams& P) {
 out:
   if (lane == 0 && done) atomicAdd(&P.ctr->items_done, done);
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) ops += __shfl_down_sync(kFull, ops, o);
-  if (lane == 0 && ops) atomicAdd(&P.ctr->jw_word_ops, ops);
+  unsigned long long ops = tally.ops, scans = tally.scans, steps = tally.steps;
+  for (int o = 16; o > 0; o >>= 1) {
+    ops += __shfl_down_sync(kFull, ops, o);
+    scans += __shfl_down_sync(kFull, scans, o);
+    steps += __shfl_down_sync(kFull, steps, o);
+  }
+  if (lane == 0) {
+    if (ops) atomicAdd(&P.ctr->jw_word_ops, ops);
+    if (scans) atomicAdd(&P.ctr->scans, scans);
+    if (steps) atomicAdd(&P.ctr->scan_steps, steps);
+  }
 }
 
 // Dense variant: 3 CTAs (24 warps) per SM, at most 85 registers per thread.

@@ -176,6 +176,8 @@ struct Counters {
   unsigned long long jw_word_ops;  // algorithmic work of the JW evaluations
   unsigned long long seen_overflow;  // nonzero: the duplicate set had no room (run repeats)
   unsigned long long passes;  // rule-level passes before de-duplication (plans with several rules)
+  unsigned long long scans;       // pairs that reached a bit-parallel scan
+  unsigned long long scan_steps;  // scan steps of 4 symbols
 };
 
 struct EvalParams {
@@ -220,6 +222,14 @@ __global__ void k_scan_top_u64(unsigned long long* partial, uint32_t nb);
 __global__ void k_items_final(const Rule* rules, uint32_t rule, uint32_t tile_right,
                               const unsigned long long* partial);
 __global__ void k_rule_base(const Rule* rules, uint32_t n_rules, unsigned long long* base);
+// fused join (every rule's left key domain <= kFusedJoinMaxDomain); k_join_count
+// takes min(max domain, kSharedHistKeys) * 4 bytes of dynamic shared memory
+constexpr uint32_t kFusedJoinMaxDomain = 1u << 16;
+constexpr uint32_t kSharedHistKeys = 8192;
+__global__ void k_join_count(Side L, Side R, const Rule* rules, uint32_t n_rules);
+__global__ void k_join_scan(const Rule* rules, uint32_t tile_right, unsigned long long* comparisons);
+__global__ void k_join_scatter(Side L, Side R, const Rule* rules, uint32_t n_rules,
+                               unsigned long long* rule_base);
 // ------------------------------------------------------------------ evaluation
 __global__ void k_eval(EvalParams P);       // 3 CTAs per SM (register-limited)
 __global__ void k_eval_wide(EvalParams P);  // 2 CTAs per SM (more registers)

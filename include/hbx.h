@@ -118,6 +118,8 @@ typedef struct hbx_stats {
   uint32_t tile_right;        /* right rows per work item of the last run */
   uint32_t eval_variant;      /* evaluation kernel of the last run (hbx_opts numbering) */
   uint32_t reserved;
+  uint64_t pairs_scanned;     /* JW evaluations the filters could not settle (bit-parallel scans) */
+  uint64_t scan_steps;        /* steps of those scans, 4 symbols each */
 } hbx_stats;
 
 /* ---- context ------------------------------------------------------------ */
