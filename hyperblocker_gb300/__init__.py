@@ -75,7 +75,7 @@ class Stats(ctypes.Structure):
                 ("ms_eval", ctypes.c_double), ("jw_word_ops", ctypes.c_uint64),
                 ("h2d_bytes", ctypes.c_uint64), ("ms_create", ctypes.c_double),
                 ("ingest_on_device", ctypes.c_uint32), ("tile_right", ctypes.c_uint32),
-                ("eval_variant", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("eval_variant", ctypes.c_uint32), ("n_windows", ctypes.c_uint32),
                 ("pairs_scanned", ctypes.c_uint64), ("scan_steps", ctypes.c_uint64)]
 
     def as_dict(self) -> Dict[str, float]:
@@ -141,6 +141,9 @@ SIGNATURES = {
                                         ctypes.c_int64, ctypes.POINTER(Pairs), _VP,
                                         ctypes.POINTER(Stats)]),
     "hbx_static_last_error": (ctypes.c_char_p, []),
+    "hbx_block_streamed": (ctypes.c_int, [_VP, _VP, _VP, _VP, ctypes.c_uint64, ctypes.c_int64,
+                                          ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(Pairs),
+                                          ctypes.POINTER(Stats)]),
     "hbx_serve_open": (ctypes.c_int, [_VP, ctypes.POINTER(_VP), ctypes.c_int32, _VP,
                                       ctypes.POINTER(ServeOpts), ctypes.POINTER(_VP)]),
     "hbx_serve_submit": (ctypes.c_int, [_VP, ctypes.c_uint64, ctypes.c_int32, ctypes.POINTER(Columns)]),
@@ -464,6 +467,29 @@ def block(ctx: Context, plan: Plan, left: Table, right: Table, n_partitions: int
         n = int(p.n_written)
         if n + n // 4 > getattr(ctx, "_capacity_hint", 1 << 16):
             ctx._capacity_hint = n + n // 4
+        return np.stack([ol[:n], orr[:n]], axis=1), s
+
+
+def block_streamed(ctx: Context, plan: Plan, left: Table, right: Table, n_partitions: int,
+                   window_bytes: int, prefix_idx: int = INT_MAX, mode="batched",
+                   capacity: Optional[int] = None):
+    """``hbx_block_streamed``: partition windows of at most ``window_bytes``
+    of device memory, two in flight; returns (pairs (n, 2) uint32, stats)."""
+    if capacity is None:
+        capacity = getattr(ctx, "_capacity_hint", 1 << 16)
+    while True:
+        ol = np.empty(max(capacity, 1), dtype=np.uint32)
+        orr = np.empty(max(capacity, 1), dtype=np.uint32)
+        p = Pairs(ol.ctypes.data, orr.ctypes.data, capacity, 0, 0)
+        s = Stats()
+        st = lib().hbx_block_streamed(ctx.h, plan.h, left.h, right.h, n_partitions, prefix_idx,
+                                      _mode(mode), window_bytes, ctypes.byref(p), ctypes.byref(s))
+        if st == ERR_CAPACITY:
+            capacity = int(p.n_required)
+            ctx._capacity_hint = max(getattr(ctx, "_capacity_hint", 0), capacity + capacity // 4)
+            continue
+        _check(st, ctx.h)
+        n = int(p.n_written)
         return np.stack([ol[:n], orr[:n]], axis=1), s
 
 

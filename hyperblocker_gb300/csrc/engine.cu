@@ -782,6 +782,7 @@ void session_run(hbx_session* S, hbx_mode mode, cudaStream_t st) {
     S->stats.pairs_scanned = c.scans;
     S->stats.scan_steps = c.scan_steps;
     S->stats.tile_right = S->tile_right;
+    S->stats.n_windows = 1;
     S->stats.eval_variant = (uint32_t)S->variant + 1;
     unsigned long long total_items = 0;
     HBX_CUDA(cudaMemcpyAsync(&total_items, S->d_rule_base.p + S->rb.size(), sizeof total_items,
@@ -796,6 +797,21 @@ void session_run(hbx_session* S, hbx_mode mode, cudaStream_t st) {
     grow_output(S, needed_capacity(S, c));
   }
   fail(HBX_ERR_CAPACITY, "output kept growing");
+}
+
+void run_to_host(hbx_session* S, hbx_mode mode, std::vector<uint32_t>* l, std::vector<uint32_t>* r) {
+  cudaStream_t st = S->ctx->stream;
+  S->one_shot = true;  // no graph for a single run
+  PoolScope scope(S->ctx->pool, st);
+  session_run(S, mode, st);
+  const uint64_t n = S->stats.n_matches;
+  l->resize(n);
+  r->resize(n);
+  if (n) {
+    HBX_CUDA(cudaMemcpyAsync(l->data(), S->out_l.p, n * 4, cudaMemcpyDeviceToHost, st));
+    HBX_CUDA(cudaMemcpyAsync(r->data(), S->out_r.p, n * 4, cudaMemcpyDeviceToHost, st));
+    HBX_CUDA(cudaStreamSynchronize(st));
+  }
 }
 
 }  // namespace hbx

@@ -317,6 +317,48 @@ struct DevCol {
 
 }  // namespace
 
+std::vector<uint32_t> bucket_rows(const Table& t, int part_col, int64_t prefix_idx,
+                                  uint64_t n_part, int n_sm, cudaStream_t st) {
+  const uint64_t n = (uint64_t)t.n_rows;
+  std::vector<uint32_t> out(n, 0);
+  const int pre = prefix_idx != INT_MAX ? (int)prefix_idx : -1;
+  if (!n || (part_col < 0 && pre < 0)) return out;
+  constexpr uint64_t kChunk = 1ull << 22;
+  DBuf<unsigned long long> hist;
+  hist.alloc(n_part);
+  DBuf<uint32_t> d_out;
+  d_out.alloc(std::min(n, kChunk));
+  const size_t hist_smem = n_part <= ing::kSharedHist ? n_part * sizeof(uint32_t) : 0;
+  for (uint64_t r0 = 0; r0 < n; r0 += kChunk) {
+    const uint64_t r1 = std::min(n, r0 + kChunk), m = r1 - r0;
+    DBuf<uint8_t> b[2];
+    DBuf<int64_t> o[2];
+    ing::ColDev view[2] = {{nullptr, nullptr, 0}, {nullptr, nullptr, 0}};
+    const int cols[2] = {part_col, pre};
+    for (int k = 0; k < 2; k++) {
+      if (cols[k] < 0) continue;
+      const Column& c = t.cols[(size_t)cols[k]];
+      const int64_t a = c.off[r0], z = c.off[r1];
+      std::vector<int64_t> off(m + 1);
+      for (uint64_t i = 0; i <= m; i++) off[i] = c.off[r0 + i] - a;
+      b[k].alloc(std::max<int64_t>(z - a, 16));
+      o[k].alloc(m + 1);
+      if (z > a)
+        HBX_CUDA(cudaMemcpyAsync(b[k].p, c.bytes.data() + a, (size_t)(z - a), cudaMemcpyHostToDevice, st));
+      HBX_CUDA(cudaMemcpyAsync(o[k].p, off.data(), (m + 1) * 8, cudaMemcpyHostToDevice, st));
+      HBX_CUDA(cudaStreamSynchronize(st));  // off is a local vector
+      view[k] = ing::ColDev{b[k].p, o[k].p, 0};
+    }
+    ing::k_buckets<<<grid_for(m, n_sm, 4), 256, hist_smem, st>>>(
+        view[0], part_col >= 0 ? 1u : 0u, view[1], pre >= 0 ? 1u : 0u, n_part, (uint32_t)m, d_out.p,
+        hist.p);
+    check_launch("bucket_rows");
+    HBX_CUDA(cudaMemcpyAsync(out.data() + r0, d_out.p, m * 4, cudaMemcpyDeviceToHost, st));
+    HBX_CUDA(cudaStreamSynchronize(st));
+  }
+  return out;
+}
+
 void pin_table(const hbx_table* ct) {
   hbx_table* t = const_cast<hbx_table*>(ct);
   std::lock_guard<std::mutex> lock(t->pin_mu);

@@ -83,6 +83,11 @@ void scan_u32(const uint32_t* in, uint32_t n, uint32_t* out, cudaStream_t st);
 bool device_encode(const hbx_table* left, const hbx_table* right, Encoded* E, SideBufs* L,
                    SideBufs* R, int n_sm, cudaStream_t st, uint64_t* h2d, std::string* why);
 
+// Partition bucket of every row of a table (data_mngr.h:150-202) computed on
+// the device from the partition and prefix columns only, in chunks of rows.
+std::vector<uint32_t> bucket_rows(const Table& t, int part_col, int64_t prefix_idx,
+                                  uint64_t n_partitions, int n_sm, cudaStream_t st);
+
 // Page-locks the column buffers of a table (once; later calls return at
 // once) so that copies from them run at full link speed.  Failure to lock is
 // not an error: copies then go through the driver's staging buffers.

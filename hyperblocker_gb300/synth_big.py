@@ -120,15 +120,15 @@ class Gen:
     def _zipf_words(self, k: int) -> np.ndarray:
         return self.word_lut[self.rng.integers(0, 1 << 22, size=k)]
 
-    def titles(self, n: int) -> Tuple[np.ndarray, np.ndarray]:
-        K = 24
-        target = self.rng.integers(20, 121, size=n)
+    def titles(self, n: int, lo: int = 20, hi: int = 120) -> Tuple[np.ndarray, np.ndarray]:
+        K = 24 if hi <= 120 else 64
+        target = self.rng.integers(lo, hi + 1, size=n)
         ids = self._zipf_words(n * K).reshape(n, K)
         wl = self.words.lens[ids]
         cum = np.cumsum(wl + 1, axis=1) - 1  # length when words 0..j are taken
         # words until the target is reached, never past 120 characters
         take = np.ones_like(cum, dtype=bool)
-        take[:, 1:] = (cum[:, :-1] < target[:, None]) & (cum[:, 1:] <= 120)
+        take[:, 1:] = (cum[:, :-1] < target[:, None]) & (cum[:, 1:] <= hi)
         take = np.logical_and.accumulate(take, axis=1)
         counts = take.sum(axis=1)
         sel = ids[take]
@@ -137,8 +137,8 @@ class Gen:
         tl[np.cumsum(counts) - 1] -= 1
         return _rows_from_padded(self.word_sp[sel], tl, counts)
 
-    def authors(self, n: int) -> Tuple[np.ndarray, np.ndarray]:
-        k = self.rng.integers(1, 7, size=n)
+    def authors(self, n: int, kmin: int = 1, kmax: int = 6) -> Tuple[np.ndarray, np.ndarray]:
+        k = self.rng.integers(kmin, kmax + 1, size=n)
         m = int(k.sum())
         f = self.rng.integers(0, self.n_first, size=m)
         l = self.rng.integers(0, self.n_last, size=m)
@@ -313,6 +313,60 @@ def rule_yaml6(eq_cols: Sequence[int], sims: Sequence[tuple]) -> str:
     doc = synth.rule_yaml(eq_cols, [(c, float(t)) for c, t in sims])
     return doc.replace("[0, 0, 1, 2, 3, 4]", "[0, 0, 1, 2, 3, 4, 5]").replace(
         "[1, 0, 1, 2, 3, 4]", "[1, 0, 1, 2, 3, 4, 5]")
+
+
+# ------------------------------------------------------- long strings (C5)
+def _zipf_key_idx(rng, n: int, n_keys: int, s: float = 1.0) -> np.ndarray:
+    w = 1.0 / np.arange(1, n_keys + 1, dtype=np.float64) ** s
+    cdf = np.cumsum(w) / w.sum()
+    return np.minimum(np.searchsorted(cdf, rng.random(n), side="right"), n_keys - 1)
+
+
+def _c5_rows(g: Gen, n: int, id_base: int, key_perm: np.ndarray) -> List[Tuple[np.ndarray, np.ndarray]]:
+    parts: List[List[Tuple[np.ndarray, np.ndarray]]] = [[] for _ in range(4)]
+    for s0 in range(0, n, CHUNK):
+        k = min(CHUNK, n - s0)
+        parts[0].append(_ids(id_base + s0, k))
+        parts[1].append(g.titles(k, 64, 256))
+        parts[2].append(g.authors(k, 5, 16))
+        # the blocking key: a uint32 per bucket, written as decimal text
+        keys = key_perm[_zipf_key_idx(g.rng, k, len(key_perm))]
+        parts[3].append(_join(Tokens.of([b"%d" % x for x in np.unique(keys)]),
+                              np.searchsorted(np.unique(keys), keys).astype(np.int64),
+                              np.ones(k, dtype=np.int64)))
+    return [_concat(p) for p in parts]
+
+
+NAMES_C5 = ["id", "title", "authors", "key"]
+
+
+def c5(n_left: int = 1_000_000, n_right: int = 1_000_000, n_true: int = 20_000,
+       n_keys: int = 1 << 20) -> BigWorkload:
+    """Long strings: titles 64-256 and authors of 5-16 names (about 64-256
+    characters), an equality key of n_keys uint32 values with Zipf(1.0)
+    occupancy, 3 rules, 64 partitions.  The quoted configuration is 20M x 20M;
+    sizes are parameters."""
+    g = Gen(5)
+    key_perm = g.rng.integers(0, 1 << 32, size=n_keys, dtype=np.uint64)
+    left = _with_header(NAMES_C5, _c5_rows(g, n_left, 20_000_000, key_perm))
+    n_true = min(n_true, n_left, n_right)
+    src = np.sort(g.rng.integers(0, n_left, size=n_true))
+    right_rows = _c5_rows(g, n_right - n_true, 60_000_000, key_perm)
+    right = _with_header(NAMES_C5, _append(right_rows, perturbed_copies(
+        g, left, src, 60_000_000 + n_right - n_true)))
+    T, A, K = 1, 2, 3
+    rules = [rule_yaml_c5([K], [(T, 0.9)]), rule_yaml_c5([K], [(A, 0.88)]),
+             rule_yaml_c5([K], [(T, 0.85), (A, 0.85)])]
+    return BigWorkload("c5_long_strings", left, right, rules, 64,
+                       "3 rules on a Zipf(1.0) key over 2^20 values: JW(title)>=0.9 | "
+                       "JW(authors)>=0.88 | JW(title)>=0.85 and JW(authors)>=0.85")
+
+
+def rule_yaml_c5(eq_cols: Sequence[int], sims: Sequence[tuple]) -> str:
+    """synth.rule_yaml for the 4-column schema (id, title, authors, key)."""
+    doc = synth.rule_yaml(eq_cols, [(c, float(t)) for c, t in sims])
+    return doc.replace("[0, 0, 1, 2, 3, 4]", "[0, 0, 1, 2, 3]").replace(
+        "[1, 0, 1, 2, 3, 4]", "[1, 0, 1, 2, 3]")
 
 
 # ---------------------------------------------------------------- serving (C4)

@@ -117,7 +117,7 @@ typedef struct hbx_stats {
   uint32_t ingest_on_device;  /* 1 when the tables were encoded on the device */
   uint32_t tile_right;        /* right rows per work item of the last run */
   uint32_t eval_variant;      /* evaluation kernel of the last run (hbx_opts numbering) */
-  uint32_t reserved;
+  uint32_t n_windows;         /* partition windows of the call (hbx_block_streamed), else 1 */
   uint64_t pairs_scanned;     /* JW evaluations the filters could not settle (bit-parallel scans) */
   uint64_t scan_steps;        /* steps of those scans, 4 symbols each */
 } hbx_stats;
@@ -177,6 +177,19 @@ hbx_status hbx_block(hbx_ctx* ctx, const hbx_plan* plan, const hbx_table* left,
 hbx_status hbx_write_pairs(hbx_ctx* ctx, const hbx_table* left, const hbx_table* right,
                            const uint32_t* l_row, const uint32_t* r_row, uint64_t n,
                            const char* path);
+
+/* hbx_block for tables whose encoding need not fit the device at once (the
+ * reference's per-partition pipeline, host_producer.h:75-104, with a memory
+ * bound): partitions are grouped into windows of at most window_bytes of
+ * device memory (a partition larger than that is split by its left rows), and
+ * two workers with their own streams process windows in turn, so one
+ * window's copies and encoding overlap another's evaluation.  Same pairs as
+ * hbx_block (in another order); stats->n_windows counts the windows and
+ * ms_last_run is the wall time of the call.  out holds HOST pointers. */
+hbx_status hbx_block_streamed(hbx_ctx* ctx, const hbx_plan* plan, const hbx_table* left,
+                              const hbx_table* right, uint64_t n_partitions, int64_t prefix_idx,
+                              hbx_mode mode, uint64_t window_bytes, hbx_pairs* out,
+                              hbx_stats* stats);
 
 /* The run_hyperblocker_exec command line (examples/run_hyperblocker.cu:22-59):
  * -data_l -data_r -rule_dir -o -n_partitions [-sep -scheduler -read_header
