@@ -23,8 +23,9 @@ Jaro-Winkler pair evaluation and compaction of the matching pairs.
   the ``roofline`` block for the conventions), ``cpu_baseline``: the oracle
   (the reference's brute-force algorithm restated in C++) on all host cores.
 
-At N=1 two more workloads are measured and reported in the same line:
-``c3`` (1M x 1M rows, 8 rules, 64 Zipf-sized partitions: batched vs plain)
+At N=1 more workloads are measured and reported in the same line: ``c3``
+(1M x 1M rows, 8 rules, 64 Zipf-sized partitions: batched vs plain), ``c5``
+(long strings, one-shot vs partition windows streamed under a memory budget)
 and ``serving`` (10M resident right rows, a Poisson trace of left-record
 requests: p50/p99/p999 latency and pair-comparisons/s); ``--sections`` picks.
 
@@ -242,6 +243,48 @@ def bench_c3(args, ctx, dev):
     return out
 
 
+def bench_c5(args, ctx):
+    """C5 shape at args.c5_rows x args.c5_rows: titles and authors of 64-256
+    characters, a Zipf(1.0) key over 2^20 values, 3 rules, 64 partitions.
+    The same job runs once through hbx_block (both tables encoded on the
+    device at once) and once through hbx_block_streamed with partition windows
+    of at most args.c5_window_mb MiB (two windows in flight, each window's
+    copies and encoding overlapping the other's evaluation); both are timed
+    end to end (host tables to host pairs) and must give the same pairs."""
+    import numpy as np
+
+    import hyperblocker_gb300 as hb
+    from hyperblocker_gb300 import synth_big
+
+    n = args.c5_rows
+    w = synth_big.c5(n, n, max(1, n // 50))
+    plan = hb.Plan.from_yaml(w.rules, ctx)
+    L = hb.Table.from_columns(w.left.cols, ctx)
+    R = hb.Table.from_columns(w.right.cols, ctx)
+    budget = args.c5_window_mb << 20
+    hb.block(ctx, plan, L, R, w.n_partitions, hb.INT_MAX, "batched")  # warm: tuning, page-locking
+    t = time.perf_counter()
+    one, s1 = hb.block(ctx, plan, L, R, w.n_partitions, hb.INT_MAX, "batched")
+    t_one = time.perf_counter() - t
+    hb.block_streamed(ctx, plan, L, R, w.n_partitions, budget)  # warm
+    t = time.perf_counter()
+    st_pairs, s2 = hb.block_streamed(ctx, plan, L, R, w.n_partitions, budget)
+    t_st = time.perf_counter() - t
+    same = len(one) == len(st_pairs) and np.array_equal(
+        one[np.lexsort((one[:, 1], one[:, 0]))], st_pairs[np.lexsort((st_pairs[:, 1], st_pairs[:, 0]))])
+    return {"workload": f"c5 shape: {n:,} x {n:,} rows, titles and authors 64-256 characters, "
+                        "Zipf(1.0) key over 2^20 values, 3 rules, 64 partitions",
+            "unit": UNIT, "pair_comparisons": int(s1.pair_comparisons),
+            "matches": int(s1.n_matches), "same_pairs": bool(same),
+            "long_string_pairs": int(s1.long_string_pairs),
+            "one_shot": {"value": s1.pair_comparisons / t_one, "wall_ms": 1000 * t_one,
+                         "ms_eval": s1.ms_eval},
+            "streamed": {"value": s2.pair_comparisons / t_st, "wall_ms": 1000 * t_st,
+                         "windows": int(s2.n_windows), "window_mib": args.c5_window_mb,
+                         "ms_eval_summed": s2.ms_eval, "ms_create_summed": s2.ms_create},
+            "timing": "end to end, host tables to host pairs, host clock"}
+
+
 def bench_serving(args, ctx):
     """C4: a resident right table of args.serve_rows rows; args.serve_requests
     requests of log-uniform 1-50k left records arriving Poisson at
@@ -457,6 +500,8 @@ def run_engine(args, rank, world, local_rank):
         extra = {}
         if world == 1 and "c3" in args.sections:
             extra["c3"] = bench_c3(args, ctx, dev)
+        if world == 1 and "c5" in args.sections:
+            extra["c5"] = bench_c5(args, ctx)
         if world == 1 and "serve" in args.sections:
             extra["serving"] = bench_serving(args, ctx)
         line = {
@@ -502,9 +547,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sections", default="c3,serve",
                     help="extra measurements at N=1, comma separated: c3 (1M x 1M batching "
-                         "workload), serve (resident-table serving trace); '' for none")
+                         "workload), serve (resident-table serving trace), c5 (long strings, "
+                         "one-shot vs streamed partition windows; minutes); '' for none")
     ap.add_argument("--c3-rows", type=int, default=1_000_000)
     ap.add_argument("--c3-steps", type=int, default=2)
+    ap.add_argument("--c5-rows", type=int, default=500_000)
+    ap.add_argument("--c5-window-mb", type=int, default=512)
     ap.add_argument("--serve-rows", type=int, default=10_000_000)
     ap.add_argument("--serve-requests", type=int, default=800)
     ap.add_argument("--serve-rate", type=float, default=200.0)

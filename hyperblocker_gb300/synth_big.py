@@ -355,11 +355,11 @@ def c5(n_left: int = 1_000_000, n_right: int = 1_000_000, n_true: int = 20_000,
     right = _with_header(NAMES_C5, _append(right_rows, perturbed_copies(
         g, left, src, 60_000_000 + n_right - n_true)))
     T, A, K = 1, 2, 3
-    rules = [rule_yaml_c5([K], [(T, 0.9)]), rule_yaml_c5([K], [(A, 0.88)]),
-             rule_yaml_c5([K], [(T, 0.85), (A, 0.85)])]
+    rules = [rule_yaml_c5([K], [(T, 0.95)]), rule_yaml_c5([K], [(A, 0.94)]),
+             rule_yaml_c5([K], [(T, 0.92), (A, 0.92)])]
     return BigWorkload("c5_long_strings", left, right, rules, 64,
-                       "3 rules on a Zipf(1.0) key over 2^20 values: JW(title)>=0.9 | "
-                       "JW(authors)>=0.88 | JW(title)>=0.85 and JW(authors)>=0.85")
+                       "3 rules on a Zipf(1.0) key over 2^20 values: JW(title)>=0.95 | "
+                       "JW(authors)>=0.94 | JW(title)>=0.92 and JW(authors)>=0.92")
 
 
 def rule_yaml_c5(eq_cols: Sequence[int], sims: Sequence[tuple]) -> str:
