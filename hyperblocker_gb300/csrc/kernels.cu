@@ -537,10 +537,12 @@ __device__ __forceinline__ bool jw_decide(uint32_t m, uint32_t ls, uint32_t ll, 
 __device__ __forceinline__ int m_need_lo(uint32_t ls, uint32_t ll, uint32_t p, float thr) {
   if (p >= 10u) return 0;
   const float c = 0.1f * (float)p;
-  // __fdividef errs by at most 2 ulp: a few 1e-5 matches at most, far inside
-  // the 0.05 margin below
+  // every quotient here is __fdividef (at most 2 ulp off): the relative error
+  // of mr stays below 1e-6, under 3e-4 matches for ls <= 256, far inside the
+  // 0.05 margin below
   const float jn = __fdividef(thr - c, 1.0f - c);
-  const float mr = __fdividef(3.0f * jn - 1.0f, __frcp_rn((float)ls) + __frcp_rn((float)ll));
+  const float inv = __fdividef(1.0f, (float)ls) + __fdividef(1.0f, (float)ll);
+  const float mr = __fdividef(3.0f * jn - 1.0f, inv);
   const float v = ceilf(mr - 0.05f);
   if (!(v > 0.0f)) return 0;
   return v > 1.0e6f ? 1000000 : (int)v;

@@ -236,6 +236,9 @@ struct Slot {
   DBuf<uint32_t> out_l, out_r;
   uint64_t capacity = 0;
   uint64_t cmp_first = 0;  // comparisons counted by the first evaluation pass
+  dev::WarpLayout wl{};    // this batch's shared-memory layout
+  size_t smem_bytes = 0;
+  int blocks_per_sm = 1;
   Pinned stage, h_out, h_ctr;  // h_ctr: Counters + total items + comparisons per instance
   ~Slot() {
     release();  // buffers return to the pool on this slot's stream first
@@ -288,12 +291,10 @@ struct hbx_server {
   int left_cols_min = 0;
   bool any_multi_rule = false;
   uint64_t resident_bytes = 0;
-  // kernel configuration
-  dev::WarpLayout wl{};
+  // kernel configuration (each batch lays out its own Peq tables)
   uint32_t tile_right = 128;
   int variant = 1;
-  size_t smem_bytes = 0;
-  int blocks_per_sm = 1;
+  uint32_t max_peq = 0;  // shared-memory words per warp the Peq tables may take
   // queue and results
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
@@ -516,9 +517,9 @@ void open_server(hbx_server* S, const hbx_plan* const* plans, int32_t n_plans, c
   const uint32_t cap_warp_words = (uint32_t)(smem_cap / 4 / dev::kWarpsPerCta) / 4 * 4;
   const uint32_t fixed_words = dev::warp_layout_fixed_words(S->tile_right);
   if (fixed_words + 4 > cap_warp_words) fail(HBX_ERR_INVALID_ARG, "tile_right too large");
-  const uint32_t max_peq = cap_warp_words - fixed_words;
+  S->max_peq = cap_warp_words - fixed_words;
   const uint32_t full_rows = (uint32_t)dev::row_words(kFastMaxLen / 32);
-  uint32_t warp_words = 4;
+  uint32_t warp_words = 4;  // largest layout any batch can need: strings up to 256
 
   // ---- rules and their resident right-side joins
   for (int32_t p = 0; p < n_plans; p++) {
@@ -542,11 +543,7 @@ void open_server(hbx_server* S, const hbx_plan* const* plans, int32_t n_plans, c
         d.sim_r[s] = (uint32_t)pr.sim_r[s];
         d.thr[s] = pr.thr[s];
         const uint32_t words = (S->n_symbols * full_rows + 3) / 4 * 4;
-        if (off + words <= max_peq) {
-          d.peq_rows_words[s] = full_rows;
-          d.peq_off[s] = off;
-          off += words;
-        }
+        if (off + words <= S->max_peq) off += words;
       }
       warp_words = std::max(warp_words, off);
       d.domain = (uint32_t)D;
@@ -581,12 +578,8 @@ void open_server(hbx_server* S, const hbx_plan* const* plans, int32_t n_plans, c
       S->rules.push_back(std::move(T));
     }
   }
-  S->wl = dev::warp_layout(warp_words, S->tile_right);
-  S->smem_bytes = (size_t)S->wl.warp_words * 4 * dev::kWarpsPerCta;
-  raise_smem_limit(kern, S->smem_bytes);
-  int bps = 0;
-  HBX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, kThreads, S->smem_bytes));
-  S->blocks_per_sm = std::max(1, bps);
+  raise_smem_limit(kern, (size_t)dev::warp_layout(warp_words, S->tile_right).warp_words * 4 *
+                             dev::kWarpsPerCta);
   HBX_CUDA(cudaStreamSynchronize(st));
 
   uint64_t rb = S->R.eq.n * 4 + S->R.arena.n + S->R.meta.n * sizeof(dev::StrMeta) + S->R.bucket.n * 4;
@@ -694,6 +687,19 @@ void launch_batch(hbx_server* S, Slot& B) {
       if (S->left_cols[k] == c) return k;
     return (size_t)0;
   };
+  // Peq row stride the batch's left strings need per string slot: the
+  // longest string of the slot in this batch decides
+  std::vector<uint32_t> need(S->lstr.size(), 0);
+  for (size_t sl = 0; sl < S->lstr.size(); sl++) {
+    int64_t mx = 0;
+    for (auto& e : B.ents) {
+      const Column& col = e.r->rows.cols[(size_t)S->lstr[sl]];
+      for (uint32_t i = e.r0; i < e.r1; i++) mx = std::max<int64_t>(mx, col.off[i + 1] - col.off[i]);
+    }
+    const uint32_t m = (uint32_t)std::min<int64_t>(mx, kFastMaxLen);
+    need[sl] = m ? (uint32_t)dev::row_words((int)((m + 31) / 32)) : 0u;
+  }
+  uint32_t warp_words = 4;
 
   // ---- encode the batch against the resident dictionaries and alphabet
   B.L.eq.alloc(std::max<size_t>(S->pairs.size() * (size_t)N, 1));
@@ -741,6 +747,19 @@ void launch_batch(hbx_server* S, Slot& B) {
       HBX_CUDA(cudaMemsetAsync(I.cnt_l.p, 0, (size_t)t.domain_l * 4, st));
       HBX_CUDA(cudaMemsetAsync(I.cur_l.p, 0, (size_t)t.domain_l * 4, st));
       dev::Rule d = t;
+      uint32_t off = 0;
+      for (uint32_t s = 0; s < d.n_sim; s++) {
+        const uint32_t rw = need[d.sim_l[s]];
+        const uint32_t words = (S->n_symbols * rw + 3) / 4 * 4;
+        d.peq_rows_words[s] = 0;
+        d.peq_off[s] = 0;
+        if (rw && off + words <= S->max_peq) {
+          d.peq_rows_words[s] = rw;
+          d.peq_off[s] = off;
+          off += words;
+        }
+      }
+      warp_words = std::max(warp_words, off);
       d.key_l = I.key_l.p;
       d.cnt_l = I.cnt_l.p;
       d.off_l = I.off_l.p;
@@ -749,6 +768,14 @@ void launch_batch(hbx_server* S, Slot& B) {
       d.sorted_l = I.sorted_l.p;
       B.h_rules.push_back(d);
     }
+  B.wl = dev::warp_layout(warp_words, S->tile_right);
+  B.smem_bytes = (size_t)B.wl.warp_words * 4 * dev::kWarpsPerCta;
+  {
+    int bps = 0;
+    HBX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, dev::eval_kernel(S->variant), kThreads,
+                                                           B.smem_bytes));
+    B.blocks_per_sm = std::max(1, bps);
+  }
   const uint32_t ni = (uint32_t)B.inst.size();
   B.d_rules.alloc(ni);
   HBX_CUDA(cudaMemcpyAsync(B.d_rules.p, B.h_rules.data(), ni * sizeof(dev::Rule),
@@ -801,12 +828,12 @@ void launch_eval(hbx_server* S, Slot& B) {
   P.rule_item_base = B.d_base.p;
   P.n_seg = 0;
   P.tile_right = S->tile_right;
-  P.warp_words = S->wl.warp_words;
-  P.queue_off = S->wl.queue_off;
-  P.stage_meta_off = S->wl.stage_meta_off;
-  P.stage_rows_off = S->wl.stage_rows_off;
-  P.sig_off = S->wl.sig_off;
-  P.mbar_off = S->wl.mbar_off;
+  P.warp_words = B.wl.warp_words;
+  P.queue_off = B.wl.queue_off;
+  P.stage_meta_off = B.wl.stage_meta_off;
+  P.stage_rows_off = B.wl.stage_rows_off;
+  P.sig_off = B.wl.sig_off;
+  P.mbar_off = B.wl.mbar_off;
   P.out_l = B.out_l.p;
   P.out_r = B.out_r.p;
   P.capacity = B.capacity;
@@ -814,8 +841,8 @@ void launch_eval(hbx_server* S, Slot& B) {
   P.watchdog_cycles = 0;
   P.seen = B.seen.p;
   P.seen_mask = B.seen.p ? B.seen.n - 1 : 0;
-  const int grid = S->ctx->n_sm * S->blocks_per_sm;
-  dev::eval_kernel(S->variant)<<<grid, kThreads, S->smem_bytes, st>>>(P);
+  const int grid = S->ctx->n_sm * B.blocks_per_sm;
+  dev::eval_kernel(S->variant)<<<grid, kThreads, B.smem_bytes, st>>>(P);
   check_launch("serving k_eval");
   uint8_t* h = (uint8_t*)B.h_ctr.p;
   HBX_CUDA(cudaMemcpyAsync(h, B.d_ctr.p, sizeof(dev::Counters), cudaMemcpyDeviceToHost, st));
