@@ -352,7 +352,8 @@ uint32_t enqueue_join(hbx_session* S, cudaStream_t st) {
     const size_t smem = std::min<uint32_t>(max_d, dev::kSharedHistKeys) * sizeof(uint32_t);
     const int grid = row_grid(std::max(nL, nR), n_sm);
     dev::k_join_count<<<grid, 256, smem, st>>>(S->side_l, S->side_r, S->d_rules.p, n_rules);
-    dev::k_join_scan<<<n_rules, 1024, 0, st>>>(S->d_rules.p, S->tile_right, &S->d_ctr.p->comparisons);
+    dev::k_join_scan<<<dim3(n_rules, 3), 1024, 0, st>>>(S->d_rules.p, S->tile_right,
+                                                        &S->d_ctr.p->comparisons);
     dev::k_join_scatter<<<grid, 256, 0, st>>>(S->side_l, S->side_r, S->d_rules.p, n_rules,
                                                S->d_rule_base.p);
     launch_check("join kernels");

@@ -216,16 +216,17 @@ __global__ void k_join_count(Side L, Side R, const Rule* rules, uint32_t n_rules
   }
 }
 
-// One block (1024 threads) per rule: row offsets per key for both tables,
-// work items per left key, and the rule's pair-comparison count.
+// Three blocks (1024 threads) per rule (blockIdx.x), one per independent
+// scan (blockIdx.y): 0 = row offsets per left key, 1 = row offsets per right
+// key, 2 = work items per left key and the rule's pair-comparison count.
 __global__ void k_join_scan(const Rule* rules, uint32_t tile_right, unsigned long long* comparisons) {
   __shared__ uint32_t s_w32[32];
   __shared__ uint32_t s_t32;
   __shared__ unsigned long long s_w64[32];
-  __shared__ unsigned long long s_t64, s_p64;
+  __shared__ unsigned long long s_t64;
   const Rule& Q = rules[blockIdx.x];
-  // row offsets: left keys, then right keys
-  for (int side = 0; side < 2; side++) {
+  if (blockIdx.y < 2) {
+    const int side = (int)blockIdx.y;
     const uint32_t D = side ? Q.domain : Q.domain_l;
     const uint32_t* cnt = side ? Q.cnt_r : Q.cnt_l;
     uint32_t* off = side ? Q.off_r : Q.off_l;
@@ -245,6 +246,7 @@ __global__ void k_join_scan(const Rule* rules, uint32_t tile_right, unsigned lon
       carry += s_t32;
       __syncthreads();
     }
+    return;
   }
   // work items per left key (exclusive, with the total at domain_l)
   unsigned long long carry = 0, pairs = 0;
@@ -263,14 +265,13 @@ __global__ void k_join_scan(const Rule* rules, uint32_t tile_right, unsigned lon
       ex += v[k];
     }
     carry += s_t64;
-    block_excl_scan<unsigned long long>(pr, s_w64, &s_p64);
-    pairs += s_p64;
+    pairs += pr;
     __syncthreads();
   }
-  if (threadIdx.x == 0) {
-    Q.item_off[Q.domain_l] = carry;
-    if (pairs) atomicAdd(comparisons, pairs);
-  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) pairs += __shfl_xor_sync(kFull, pairs, o);
+  if ((threadIdx.x & 31) == 0 && pairs) atomicAdd(comparisons, pairs);
+  if (threadIdx.x == 0) Q.item_off[Q.domain_l] = carry;
 }
 
 // Rows of every rule grouped by key (counting-sort scatter, right rows with
