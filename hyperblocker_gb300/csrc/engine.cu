@@ -77,6 +77,8 @@ struct hbx_session {
   uint32_t warp_words = 4;
   uint32_t tile_right = 128;
   hbx::dev::WarpLayout wl{};
+  hbx::dev::PeqShape peq_shape{};
+  hbx::DBuf<uint32_t> peq;  // Peq tables of the left strings [slot][row]
   int variant = 0;  // evaluation kernel: 0 = k_eval, 1 = k_eval_wide
   bool tuned = false;
   bool one_shot = false;  // runs once (hbx_block): no graph is captured
@@ -123,47 +125,21 @@ int row_grid(uint64_t n, int n_sm) {
 
 // Tile shape and kernel variant of a session: right rows per work item
 // (tile_right) and the evaluation kernel (0: 3 CTAs per SM, 1: 2 CTAs per SM
-// with more registers).  Lays out each warp's shared memory (Peq tables per
-// similarity predicate, then dev::warp_layout), uploads the rule descriptors,
-// raises the kernel's shared-memory limit if needed and drops the graph.
+// with more registers).  Lays out each warp's shared memory
+// (dev::warp_layout), uploads the rule descriptors, raises the kernel's
+// shared-memory limit if needed and drops the graph.
 void configure(hbx_session* S, uint32_t tile_right, int variant) {
   hbx_ctx* C = S->ctx;
-  const Encoded& E = S->E;
-  S->tile_right = std::min<uint32_t>(2048, std::max<uint32_t>(32, (tile_right + 31) / 32 * 32));
+  S->tile_right = std::min<uint32_t>(512, std::max<uint32_t>(32, (tile_right + 31) / 32 * 32));
   S->variant = variant ? 1 : 0;
   const dev::EvalKernel kern = dev::eval_kernel(S->variant);
-  const uint32_t NS = E.n_symbols;
   const size_t smem_cap = std::min<size_t>(C->smem_optin, 200 * 1024);
   const uint32_t cap_warp_words = (uint32_t)(smem_cap / 4 / dev::kWarpsPerCta) / 4 * 4;
-  const uint32_t fixed_words = dev::warp_layout_fixed_words(S->tile_right);
-  if (fixed_words + 4 > cap_warp_words) fail(HBX_ERR_INVALID_ARG, "tile_right too large");
-  const uint32_t max_warp_words = cap_warp_words - fixed_words;
-  uint32_t warp_words = 4;
-  for (size_t r = 0; r < E.rules.size(); r++) {
-    const RuleEnc& re = E.rules[r];
-    dev::Rule& d = S->h_rules[r];
-    uint32_t off = 0;
-    for (size_t s = 0; s < re.sim_slot_l.size(); s++) {
-      const uint32_t mx = std::min<uint32_t>(E.L.str_maxlen[(size_t)re.sim_slot_l[s]], kFastMaxLen);
-      const uint32_t S32 = mx ? (uint32_t)dev::row_words((int)((mx + 31) / 32)) : 0u;
-      const uint32_t words = (NS * S32 + 3) / 4 * 4;
-      if (S32 && off + words <= max_warp_words) {
-        d.peq_rows_words[s] = S32;
-        d.peq_off[s] = off;
-        off += words;
-      } else {
-        d.peq_rows_words[s] = 0;  // evaluated by the exact per-lane path
-        d.peq_off[s] = 0;
-      }
-    }
-    warp_words = std::max(warp_words, off);
-  }
-  S->wl = dev::warp_layout(warp_words, S->tile_right);
+  S->wl = dev::warp_layout(S->tile_right);
   S->warp_words = S->wl.warp_words;
+  if (S->warp_words > cap_warp_words) fail(HBX_ERR_INVALID_ARG, "tile_right too large");
   // every warp region lies inside the dynamic allocation
   S->smem_bytes = (size_t)S->warp_words * 4 * dev::kWarpsPerCta;
-  if (warp_words % 4 || S->warp_words > cap_warp_words)
-    fail(HBX_ERR_CUDA, "shared-memory layout exceeds its allocation");
   HBX_CUDA(cudaMemcpyAsync(S->d_rules.p, S->h_rules.data(), S->h_rules.size() * sizeof(dev::Rule),
                            cudaMemcpyHostToDevice, C->stream));
   HBX_CUDA(cudaStreamSynchronize(C->stream));
@@ -300,9 +276,27 @@ void setup_session(hbx_session* S, uint64_t h2d_tables) {
   S->d_rules.alloc(E.rules.size());
   S->d_rule_base.alloc(E.rules.size() + 1);
   S->d_ctr.alloc(1);
-  const uint32_t tile = C->opts.tile_right > 0 ? (uint32_t)C->opts.tile_right : 128u;
-  const int variant = C->opts.eval_variant > 0 ? C->opts.eval_variant - 1 : 0;
+  const uint32_t tile = C->opts.tile_right > 0 ? (uint32_t)C->opts.tile_right : 64u;
+  const int variant = C->opts.eval_variant > 0 ? C->opts.eval_variant - 1 : 1;
   configure(S, tile, variant);
+
+  // Peq tables of every left string slot, shaped for the longest left
+  // string any similarity predicate reads
+  {
+    uint32_t mx = 1;
+    for (const RuleEnc& re : E.rules)
+      for (int sl : re.sim_slot_l) mx = std::max(mx, E.L.str_maxlen[(size_t)sl]);
+    S->peq_shape = dev::peq_shape(mx, E.n_symbols);
+    const uint32_t n_slots = (uint32_t)E.L.str_maxlen.size();
+    const size_t words = (size_t)n_slots * nL * S->peq_shape.tab_words;
+    S->peq.alloc(std::max<size_t>(words, 4));
+    if (words) {
+      const uint64_t warps = (uint64_t)n_slots * nL;
+      const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((warps + 7) / 8, (uint64_t)C->n_sm * 16));
+      dev::k_peq_build<<<grid, 256, 0, st>>>(S->side_l, n_slots, S->peq_shape, S->peq.p);
+      launch_check("k_peq_build");
+    }
+  }
 
   // partition boundaries of every rule's left key space, per word class
   // (plain form): entry (rule, class, p) = first left key of partition p
@@ -395,12 +389,7 @@ dev::EvalParams eval_params(hbx_session* S) {
   P.n_symbols = S->E.n_symbols;
   P.rule_item_base = S->d_rule_base.p;
   P.tile_right = S->tile_right;
-  P.warp_words = S->warp_words;
-  P.queue_off = S->wl.queue_off;
-  P.stage_meta_off = S->wl.stage_meta_off;
-  P.stage_rows_off = S->wl.stage_rows_off;
-  P.sig_off = S->wl.sig_off;
-  P.mbar_off = S->wl.mbar_off;
+  dev::set_layout(&P, S->wl, S->peq_shape, S->peq.p);
   P.out_l = S->out_l.p;
   P.out_r = S->out_r.p;
   P.capacity = S->out_l.n;
@@ -557,6 +546,7 @@ std::string workload_signature(const hbx_session* S) {
   cudaDeviceProp prop;
   std::string sig;
   if (cudaGetDeviceProperties(&prop, S->ctx->device) == cudaSuccess) sig = prop.name;
+  sig += "|k2";  // evaluation kernel generation: entries of earlier kernels do not apply
   auto bucket = [](uint64_t n) {  // power-of-two bucket
     uint32_t b = 0;
     while ((1ull << b) < n) b++;
@@ -660,7 +650,7 @@ void autotune(hbx_session* S, cudaStream_t st) {
       return;
     }
   }
-  std::vector<uint32_t> tiles = {64, 128, 256};
+  std::vector<uint32_t> tiles = {32, 64, 128};
   std::vector<int> variants = {0, 1};
   if (o.tile_right > 0) tiles = {(uint32_t)o.tile_right};
   if (o.eval_variant > 0) variants = {o.eval_variant - 1};

@@ -395,23 +395,24 @@ struct Neg<8> {
   }
 };
 
+// One symbol row of a Peq table (device memory, read-only path).
 template <int S>
 __device__ __forceinline__ void load_row(const uint32_t* row, uint32_t (&pe)[S]) {
   if constexpr (S == 1) {
-    pe[0] = row[0];
+    pe[0] = __ldg(row);
   } else if constexpr (S == 2) {
-    const uint2 v = *reinterpret_cast<const uint2*>(row);
+    const uint2 v = __ldg(reinterpret_cast<const uint2*>(row));
     pe[0] = v.x;
     pe[1] = v.y;
   } else if constexpr (S == 4) {
-    const uint4 v = *reinterpret_cast<const uint4*>(row);
+    const uint4 v = __ldg(reinterpret_cast<const uint4*>(row));
     pe[0] = v.x;
     pe[1] = v.y;
     pe[2] = v.z;
     pe[3] = v.w;
   } else {
-    const uint4 v = *reinterpret_cast<const uint4*>(row);
-    const uint4 u = *reinterpret_cast<const uint4*>(row + 4);
+    const uint4 v = __ldg(reinterpret_cast<const uint4*>(row));
+    const uint4 u = __ldg(reinterpret_cast<const uint4*>(row + 4));
     pe[0] = v.x;
     pe[1] = v.y;
     pe[2] = v.z;
@@ -562,24 +563,6 @@ __device__ __noinline__ bool sim_pass_slow(const uint8_t* a, uint32_t la, const 
   return jw_exact(m, mn, max(la, lb), p, thr, &ctr->ambiguous);
 }
 
-// Peq table of the warp's left string: row `sym` (stride S words) has bit j of
-// word k set when a[32k + j] == sym.  Built with __match_any_sync: lanes that
-// hold the same symbol agree on the mask, the lowest of them stores it.
-__device__ __forceinline__ void build_peq(uint32_t* tab, uint32_t S, uint32_t n_symbols,
-                                          const uint8_t* a, uint32_t la, int lane) {
-  const uint32_t words = n_symbols * S;
-  for (uint32_t w = (uint32_t)lane; w < words; w += 32) tab[w] = 0u;
-  __syncwarp();
-  const uint32_t W = (la + 31u) >> 5;
-  for (uint32_t k = 0; k < W; k++) {
-    const uint32_t j = k * 32u + (uint32_t)lane;
-    const uint32_t sym = j < la ? (uint32_t)a[j] : 0xffffffffu;
-    const unsigned mm = __match_any_sync(kFull, sym);
-    if (j < la && lane == __ffs(mm) - 1) tab[sym * S + k] = mm;
-  }
-  __syncwarp();
-}
-
 __device__ __forceinline__ uint32_t find_key(const unsigned long long* item_off, uint32_t domain,
                                              unsigned long long local) {
   uint32_t lo = 0, hi = domain;  // item_off[lo] <= local < item_off[hi]
@@ -625,23 +608,6 @@ __device__ __forceinline__ void bp_step(const uint32_t* __restrict__ tab, uint32
   for (int k = W - 1; k > 0; k--) win[k] = __funnelshift_l(win[k - 1], win[k], 1);
   win[0] = (win[0] << 1) | grow;
 }
-
-struct Stage {
-  const uint32_t* tab;      // Peq table of the left string (shared memory)
-  const uint8_t* a;         // left string (symbols, 16-byte aligned)
-  uint32_t la;
-  uint4 a_head;             // its first 16 symbols
-  float thr;
-  uint32_t slot_r;          // string slot of the right column
-  uint32_t* rows;           // right rows of the input list (shared memory); survivors
-                            // are written back over consumed entries
-  const StrMeta* meta;      // first stage: the rows' staged string metadata, else null
-  const uint4* a_sig;       // count signature of the left string (shared memory)
-  uint4* q;                 // ring of pairs to scan, 2 x uint4 per entry:
-                            // {row, offset/16, length, p << 16 | need}, first 16 symbols
-  uint32_t n;               // rows in the input list
-  bool last;                // survivors are final matches
-};
 
 // First report of a pair?  With several rules a pair can match more than one
 // of them (the reference stops at the first rule that passes,
@@ -695,19 +661,6 @@ __device__ __forceinline__ void emit(const EvalParams& P, bool pass, uint32_t lr
   }
 }
 
-// Passes of one warp step: final (dedup + emit) or into the next stage's list,
-// written over list entries that have already been read.
-__device__ __forceinline__ void route(const EvalParams& P, const Stage& A, bool pass, uint32_t lrow,
-                                      uint32_t rrow, int lane, uint32_t* lw) {
-  if (A.last) {
-    emit(P, pass, lrow, rrow, lane);
-  } else {
-    const unsigned pm = __ballot_sync(kFull, pass);
-    if (pass) A.rows[*lw + __popc(pm & ((1u << lane) - 1u))] = rrow;
-    *lw += __popc(pm);
-  }
-}
-
 // Upper bound on the Jaro matches of two strings from their count signatures
 // (dev::StrMeta): sum over buckets of the smaller count.
 __device__ __forceinline__ uint32_t sig_bound(const uint4& a0, const uint4& a1, const uint4& b0,
@@ -742,208 +695,249 @@ struct WorkTally {
   uint32_t scans, steps;
 };
 
-constexpr uint32_t kPrefixUnknown = 0xffu;
-constexpr uint32_t kRing = kRingEntries;  // per-warp ring of pairs waiting for a scan
+// Does the left string of length la have a Peq table (PeqShape)?
+__device__ __forceinline__ bool has_table(const EvalParams& P, uint32_t la) {
+  return la > 0u && la <= P.fast_max;
+}
 
-// Filter one batch of 32 input rows: one 32-byte metadata record per right row
-// gives its length and first 16 symbols, hence the common prefix p (when below
-// 16) and the match count the threshold needs; rows that cannot reach it are
-// decided here, the rest are appended to the ring of pairs to scan together
-// with their first 16 symbols.  Empty right strings are decided here too.
-// Returns the rows appended.
-__device__ __forceinline__ uint32_t filter_batch(const EvalParams& P, const Stage& A, uint32_t e0,
-                                                 uint32_t tail, uint32_t lrow, uint32_t* lw,
-                                                 WorkTally* ops) {
+__device__ __forceinline__ const uint32_t* peq_table(const EvalParams& P, uint32_t slot,
+                                                     uint32_t lrow) {
+  return P.peq + ((size_t)slot * P.L.n_rows + lrow) * P.tab_words;
+}
+
+// Ring of pairs waiting for a scan, kRingEntries entries of three 16-byte
+// records per warp:
+//   {right row, right offset / 16, right length, need | p << 10 | s << 15 | kAdvance?}
+//   {first 16 symbols of the right string}
+//   {left row, left length, left offset / 16, rule}
+// for the similarity predicate s of the rule.  A kAdvance entry is a pair
+// that passed predicate s without a scan: the lane that takes it goes on
+// with predicate s + 1.
+constexpr uint32_t kRing = kRingEntries;
+constexpr uint32_t kPrefixUnknown = 31u;  // common prefix longer than 16: measured at the scan
+constexpr uint32_t kAdvance = 1u << 18;
+
+__device__ __forceinline__ uint32_t ring_tag(uint32_t need, uint32_t p, uint32_t s) {
+  return need | (p << 10) | (s << 15);
+}
+
+// Bit-parallel scan state of one lane: the pair's Peq table and right
+// string, the symbols in hand (cur) and the next 16 (nxt), the window and
+// matched masks, lengths, position, common prefix, the mismatches it can
+// still afford and the threshold.
+template <int W>
+struct Scan {
+  const uint32_t* tab;
+  const uint8_t* b;
+  uint4 cur, nxt;
+  uint32_t win[W], mt[W];
+  uint32_t ls, ll, i, n_iter, h, p;
+  int allowed;
+  float thr;
+};
+
+// Starts the scan of a pair (la, lb: lengths; p: common prefix or
+// kPrefixUnknown; need: matches the threshold needs).  false = decided
+// (fails) without a scan.
+template <int W>
+__device__ __forceinline__ bool scan_begin(Scan<W>& z, const uint32_t* tab, const uint8_t* a,
+                                           const uint8_t* b, const uint4& head_b, uint32_t la,
+                                           uint32_t lb, uint32_t p, int need, float thr,
+                                           WorkTally* ops) {
+  z.ls = min(la, lb);
+  z.ll = max(la, lb);
+  z.h = (z.ls + 1u) >> 1;
+  z.n_iter = min(lb, la + z.h);
+  if (p == kPrefixUnknown) {
+    p = prefix_len(a, b, z.ls);
+    need = m_need_lo(z.ls, z.ll, p, thr);
+  }
+  if (need > (int)min(z.n_iter, z.ls)) return false;
+  z.p = p;
+  z.thr = thr;
+  z.allowed = (int)z.n_iter - need;
+  z.i = 0;
+  z.tab = tab;
+  z.b = b;
+  z.cur = head_b;
+  if (z.n_iter > 16u) z.nxt = __ldg(reinterpret_cast<const uint4*>(b + 16));
+#pragma unroll
+  for (int k = 0; k < W; k++) {
+    const int nb = (int)z.h + 1 - 32 * k;
+    z.win[k] = nb >= 32 ? 0xffffffffu : (nb <= 0 ? 0u : ((1u << nb) - 1u));
+    z.mt[k] = 0u;
+  }
+  ops->scans++;
+  return true;
+}
+
+// One scan step of 4 symbols; every 16 symbols the pair stops once even
+// matching every remaining symbol stays below its bound.  Returns true when
+// the pair is decided (*pass = the decision).
+template <int W>
+__device__ __forceinline__ bool scan_step(Scan<W>& z, bool* pass, Counters* ctr, WorkTally* ops) {
+  constexpr int S = row_words(W);
+  if ((z.i & 15u) == 0 && z.i) {
+    // chunk i/16 arrived one chunk ago; ask for the one after it
+    z.cur = z.nxt;
+    if (z.i + 16u < z.n_iter) z.nxt = __ldg(reinterpret_cast<const uint4*>(z.b + z.i + 16u));
+  }
+  const uint32_t wd = z.cur.x;
+  z.cur.x = z.cur.y;
+  z.cur.y = z.cur.z;
+  z.cur.z = z.cur.w;
+#pragma unroll
+  for (int c = 0; c < 4; c++)
+    bp_step<W, S>(z.tab, (wd >> (8 * c)) & 0xffu, z.win, z.mt, (z.i + (uint32_t)c) < z.h ? 1u : 0u);
+  z.i += 4;
+  ops->steps++;
+  if (z.i >= z.n_iter || (z.i & 15u) == 0) {
+    uint32_t m = 0;
+#pragma unroll
+    for (int k = 0; k < W; k++) m += __popc(z.mt[k]);
+    if (z.i >= z.n_iter) {
+      *pass = jw_decide(m, z.ls, z.ll, z.p, z.thr, &ctr->ambiguous);
+      return true;
+    }
+    if ((int)(z.i - m) > z.allowed) {
+      *pass = false;  // even matching every remaining symbol stays below
+      return true;
+    }
+  }
+  return false;
+}
+
+// The similarity predicates after predicate s of a pair that passed it, in
+// order, until one needs a scan (returns 2, the scan state set up and s its
+// index), one fails (0) or all pass (1).  Each predicate first goes through
+// the filters of the first one: length bound, common prefix, count
+// signatures.
+template <int W>
+__device__ __forceinline__ int advance(const EvalParams& P, uint32_t rule, uint32_t* s,
+                                       uint32_t lrow, uint32_t rrow, Scan<W>& z, WorkTally* ops) {
+  const Rule* R = P.rules + rule;
+  const uint32_t n_sim = R->n_sim;
+  for (uint32_t k = *s + 1; k < n_sim; k++) {
+    *s = k;
+    const uint32_t sl = R->sim_l[k], sr = R->sim_r[k];
+    const float thr = R->thr[k];
+    const StrMeta* am = P.L.str_meta + (size_t)sl * P.L.n_rows + lrow;
+    const StrMeta* bm = P.R.str_meta + (size_t)sr * P.R.n_rows + rrow;
+    const uint4 al = am->loc, bl = bm->loc;
+    const uint32_t la = al.y, lb = bl.y;
+    const uint8_t* a = P.L.arena + 16ull * al.x;
+    const uint8_t* b = P.R.arena + 16ull * bl.x;
+    if (!has_table(P, la)) {  // the reference's own loops
+      if (la && lb) ops->ops += jw_eval_ops(min(la, lb), max(la, lb));
+      if (!sim_pass_slow(a, la, b, lb, thr, P.ctr)) return 0;
+      continue;
+    }
+    if (lb == 0) {
+      if (!jw_exact(0, la, 0, 0, thr, &P.ctr->ambiguous)) return 0;
+      continue;
+    }
+    const uint32_t ls = min(la, lb), ll = max(la, lb);
+    ops->ops += jw_eval_ops(ls, ll);
+    const uint4 bh = bm->head;
+    const uint32_t p16 = prefix16(am->head, bh);
+    uint32_t p = kPrefixUnknown;
+    int need = 0;
+    if (!(p16 == 16u && ls > 16u)) {
+      p = min(p16, ls);
+      need = m_need_lo(ls, ll, p, thr);
+      const uint32_t n_iter = min(lb, la + ((ls + 1u) >> 1));
+      if (need > (int)min(n_iter, ls)) return 0;
+      if (need > 0 &&
+          (int)sig_bound(am->sig[0], am->sig[1], bm->sig[0], bm->sig[1]) < need)
+        return 0;
+    }
+    return scan_begin<W>(z, peq_table(P, sl, lrow), a, b, bh, la, lb, p, need, thr, ops) ? 2 : 0;
+  }
+  return 1;
+}
+
+// Warp-uniform state of the evaluation loop kept in shared memory (every
+// lane reads it; every lane writes the same values, after a __syncwarp when
+// the values were read in the same step): the cached (rule, left key) with
+// its item range and blocks, the claim in each staging buffer, and the item
+// being filtered.
+struct WarpCtl {
+  unsigned long long k_lo, k_hi;  // item range of the cached (rule, left key)
+  uint32_t k_rule, k_key, k_nl, k_offl, k_offr, k_endr;  // its left count, block offsets
+  uint32_t c_rule[2], c_lrow[2], c_n[2], c_shift[2];  // claim per staging buffer (n = 0: none)
+  uint32_t i_rule, i_lrow, i_more, i_fast;  // the item being filtered
+  float i_thr;
+};
+static_assert(sizeof(WarpCtl) <= kWarpCtlWords * 4, "warp control block outgrows its words");
+
+// Filter one batch of 32 right rows of the item against its first
+// similarity predicate: one staged metadata record per right row gives its
+// length and first 16 symbols, hence the common prefix p (when below 16) and
+// the match count the threshold needs, and its count signature, an upper
+// bound on the matches; pairs that cannot reach the threshold are decided
+// here, the rest go to the ring with their first 16 symbols.  Empty right
+// strings are decided here too.  lm: the item's left string metadata.
+// Returns the entries appended.
+__device__ __forceinline__ uint32_t filter_batch(const EvalParams& P, const WarpCtl* C,
+                                                 const StrMeta* lm, const uint32_t* rows,
+                                                 const StrMeta* meta, uint32_t n, uint32_t e0,
+                                                 uint4* q, uint32_t tail, WorkTally* ops) {
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
-  const uint32_t nR = P.R.n_rows;
   const uint32_t e = e0 + (uint32_t)lane;
-  const bool act = e < A.n;
-  const uint32_t rrow = act ? A.rows[e] : 0u;
-  const StrMeta* mp = nullptr;
-  StrMeta m;
+  const bool act = e < n;
+  const uint32_t rrow = act ? rows[e] : 0u;
+  const uint32_t la = lm->loc.y, a_off = lm->loc.x;
+  const bool more = C->i_more != 0;
+  const float thr = C->i_thr;
+  uint4 loc = make_uint4(0, 0, 0, 0), head = make_uint4(0, 0, 0, 0);
   if (act) {
-    mp = A.meta ? A.meta + e : P.R.str_meta + (size_t)A.slot_r * nR + rrow;
-    m.loc = mp->loc;
-    m.head = mp->head;
-  } else {
-    m.loc = make_uint4(0, 0, 0, 0);
-    m.head = make_uint4(0, 0, 0, 0);
+    loc = meta[e].loc;
+    head = meta[e].head;
   }
   bool pass = false, scan = false;
   uint32_t p = 0;
   int need = 0;
   if (act) {
-    const uint32_t lb = m.loc.y;
-    if (lb == 0) {
-      pass = jw_exact(0, A.la, 0, 0, A.thr, &P.ctr->ambiguous);
+    const uint32_t lb = loc.y;
+    if (!C->i_fast) {  // the reference's own loops
+      if (la && lb) ops->ops += jw_eval_ops(min(la, lb), max(la, lb));
+      pass = sim_pass_slow(P.L.arena + 16ull * a_off, la, P.R.arena + 16ull * loc.x, lb, thr,
+                           P.ctr);
+    } else if (lb == 0) {
+      pass = jw_exact(0, la, 0, 0, thr, &P.ctr->ambiguous);
     } else {
-      const uint32_t ls = min(A.la, lb), ll = max(A.la, lb);
+      const uint32_t ls = min(la, lb), ll = max(la, lb);
       ops->ops += jw_eval_ops(ls, ll);
-      const uint32_t p16 = prefix16(A.a_head, m.head);
+      const uint32_t p16 = prefix16(lm->head, head);
       if (p16 == 16u && ls > 16u) {
         scan = true;  // prefix longer than 16: measured exactly before the scan
         p = kPrefixUnknown;
       } else {
         p = min(p16, ls);
-        need = m_need_lo(ls, ll, p, A.thr);
-        const uint32_t n_iter = min(lb, A.la + ((ls + 1u) >> 1));
+        need = m_need_lo(ls, ll, p, thr);
+        const uint32_t n_iter = min(lb, la + ((ls + 1u) >> 1));
         scan = need <= (int)min(n_iter, ls);  // else the threshold is out of reach
         // the count signatures bound the matches from above: below the need,
         // the pair cannot pass
         if (scan && need > 0 &&
-            (int)sig_bound(A.a_sig[0], A.a_sig[1], mp->sig[0], mp->sig[1]) < need)
+            (int)sig_bound(lm->sig[0], lm->sig[1], meta[e].sig[0], meta[e].sig[1]) < need)
           scan = false;
       }
     }
   }
-  const unsigned qm = __ballot_sync(kFull, scan);
-  if (scan) {
+  const bool push = scan || (pass && more);
+  const unsigned qm = __ballot_sync(kFull, push);
+  const uint32_t lrow = C->i_lrow;
+  if (push) {
     const uint32_t slot = (tail + __popc(qm & lt)) & (kRing - 1);
-    A.q[2 * slot] = make_uint4(rrow, m.loc.x, m.loc.y, (p << 16) | (uint32_t)need);
-    A.q[2 * slot + 1] = m.head;
+    uint4* en = q + kRingWords / 4 * slot;
+    en[0] = make_uint4(rrow, loc.x, loc.y, scan ? ring_tag((uint32_t)need, p, 0) : kAdvance);
+    en[1] = head;
+    en[2] = make_uint4(lrow, la, a_off, C->i_rule);
   }
-  route(P, A, pass, lrow, rrow, lane, lw);
+  emit(P, pass && !more, lrow, rrow, lane);
   return __popc(qm);
-}
-
-// One similarity stage of one work item.  Lanes take the next queued pair as
-// soon as theirs is decided, and the ring is refilled by filter batches as it
-// drains, so lanes stay busy whatever the strings' lengths and however many
-// rows the filter drops.  A pair starts from the 16 symbols the ring carries
-// and loads each next 16-symbol chunk one chunk ahead, so scans do not wait on
-// memory.  Every loop turn scans one 4-symbol word for every busy lane; every
-// 16 symbols a pair stops once even matching every remaining symbol stays
-// below its bound.  Survivors go to the next stage's row list (or out, in the
-// last stage); returns their count.
-template <int W>
-__device__ __forceinline__ uint32_t run_stage(const EvalParams& P, const Stage& A, uint32_t lrow,
-                                           WorkTally* ops) {
-  constexpr int S = row_words(W);
-  const int lane = threadIdx.x & 31;
-  const unsigned lt = (1u << lane) - 1u;
-  uint32_t in_pos = 0, head = 0, tail = 0, lw = 0;
-  bool busy = false;
-  uint32_t rrow = 0, ls = 0, ll = 0, i = 0, n_iter = 0, h = 0, p = 0;
-  int allowed = 0;
-  const uint8_t* b = nullptr;
-  uint4 cur = make_uint4(0, 0, 0, 0), nxt = make_uint4(0, 0, 0, 0);
-  uint32_t win[W], mt[W];
-#pragma unroll
-  for (int k = 0; k < W; k++) win[k] = mt[k] = 0u;
-  for (;;) {
-    const unsigned idle = __ballot_sync(kFull, !busy);
-    const uint32_t n_idle = __popc(idle);
-    // refill the ring until it holds a pair for every idle lane
-    while (tail - head < n_idle && in_pos < A.n && tail - head <= kRing - 32) {
-      tail += filter_batch(P, A, in_pos, tail, lrow, &lw, ops);
-      in_pos += 32;
-    }
-    bool fin = false, pass = false;
-    const uint32_t avail = tail - head;
-    const uint32_t rank = __popc(idle & lt);
-    if (!busy && rank < avail) {
-      const uint32_t slot = (head + rank) & (kRing - 1);
-      const uint4 qe = A.q[2 * slot];
-      cur = A.q[2 * slot + 1];
-      rrow = qe.x;
-      b = P.R.arena + 16ull * qe.y;
-      const uint32_t lb = qe.z;
-      ls = min(A.la, lb);
-      ll = max(A.la, lb);
-      h = (ls + 1u) >> 1;
-      n_iter = min(lb, A.la + h);
-      p = qe.w >> 16;
-      int need = (int)(qe.w & 0xffffu);
-      if (p == kPrefixUnknown) {
-        p = prefix_len(A.a, b, ls);
-        need = m_need_lo(ls, ll, p, A.thr);
-      }
-      if (need > (int)min(n_iter, ls)) {
-        fin = true;
-      } else {
-        allowed = (int)n_iter - need;
-        i = 0;
-        busy = true;
-        ops->scans++;
-        if (n_iter > 16u) nxt = __ldg(reinterpret_cast<const uint4*>(b + 16));
-#pragma unroll
-        for (int k = 0; k < W; k++) {
-          const int nb = (int)h + 1 - 32 * k;
-          win[k] = nb >= 32 ? 0xffffffffu : (nb <= 0 ? 0u : ((1u << nb) - 1u));
-          mt[k] = 0u;
-        }
-      }
-    }
-    head += min(n_idle, avail);
-    if (busy) {
-      if ((i & 15u) == 0 && i) {
-        // chunk i/16 arrived one chunk ago; ask for the one after it
-        cur = nxt;
-        if (i + 16u < n_iter) nxt = __ldg(reinterpret_cast<const uint4*>(b + i + 16u));
-      }
-      const uint32_t wd = cur.x;
-      cur.x = cur.y;
-      cur.y = cur.z;
-      cur.z = cur.w;
-#pragma unroll
-      for (int c = 0; c < 4; c++)
-        bp_step<W, S>(A.tab, (wd >> (8 * c)) & 0xffu, win, mt, (i + (uint32_t)c) < h ? 1u : 0u);
-      i += 4;
-      ops->steps++;
-      if (i >= n_iter || (i & 15u) == 0) {
-        uint32_t m = 0;
-#pragma unroll
-        for (int k = 0; k < W; k++) m += __popc(mt[k]);
-        if (i >= n_iter) {
-          fin = true;
-          busy = false;
-          pass = jw_decide(m, ls, ll, p, A.thr, &P.ctr->ambiguous);
-        } else if ((int)(i - m) > allowed) {
-          fin = true;  // even matching every remaining symbol stays below
-          busy = false;
-        }
-      }
-    }
-    route(P, A, fin && pass, lrow, rrow, lane, &lw);
-    if (!__any_sync(kFull, busy) && head == tail && in_pos >= A.n) break;
-  }
-  __syncwarp();
-  return lw;
-}
-
-// Stage over a left string the fast path does not take (longer than 256
-// bytes, or no room for its table): the reference's own loops per lane.
-__device__ __forceinline__ uint32_t run_stage_slow(const EvalParams& P, const Stage& A,
-                                                   WorkTally* ops, uint32_t lrow) {
-  const int lane = threadIdx.x & 31;
-  uint32_t lw = 0;
-  for (uint32_t e0 = 0; e0 < A.n; e0 += 32) {
-    const uint32_t e = e0 + (uint32_t)lane;
-    const bool act = e < A.n;
-    const uint32_t rrow = act ? A.rows[e] : 0u;
-    bool pass = false;
-    if (act) {
-      const uint4 mb = P.R.str_meta[(size_t)A.slot_r * P.R.n_rows + rrow].loc;
-      if (mb.y && A.la) ops->ops += jw_eval_ops(min(A.la, mb.y), max(A.la, mb.y));
-      pass = sim_pass_slow(A.a, A.la, P.R.arena + 16ull * mb.x, mb.y, A.thr, P.ctr);
-    }
-    __syncwarp();
-    route(P, A, pass, lrow, rrow, lane, &lw);
-  }
-  __syncwarp();
-  return lw;
-}
-
-__device__ __forceinline__ uint32_t stage_dispatch(uint32_t W, const EvalParams& P, const Stage& A,
-                                                   uint32_t lrow, WorkTally* ops) {
-  switch (W) {
-    case 1: return run_stage<1>(P, A, lrow, ops);
-    case 2: return run_stage<2>(P, A, lrow, ops);
-    case 3: return run_stage<3>(P, A, lrow, ops);
-    case 4: return run_stage<4>(P, A, lrow, ops);
-    default: return run_stage<8>(P, A, lrow, ops);
-  }
 }
 
 // Maps a position of the launch's work list to a global work item: the list
@@ -1005,41 +999,39 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   return false;
 }
 
-// The evaluation kernel body, instantiated twice below with different
-// register budgets (see k_eval / k_eval_wide).
-__device__ __forceinline__ void eval_body(const EvalParams& P) {
-  extern __shared__ __align__(16) uint32_t smem[];
-  const int lane = threadIdx.x & 31;
-  const int warp = threadIdx.x >> 5;
-  uint32_t* region = smem + (size_t)warp * P.warp_words;
-  uint4* q = reinterpret_cast<uint4*>(region + P.queue_off);
-  StrMeta* st_meta = reinterpret_cast<StrMeta*>(region + P.stage_meta_off);
-  uint32_t* st_rows = region + P.stage_rows_off;
-  uint4* l_sig = reinterpret_cast<uint4*>(region + P.sig_off);
-  uint64_t* bar = reinterpret_cast<uint64_t*>(region + P.mbar_off);
-  if (lane == 0) mbar_init(bar);
-  __syncwarp();
-  uint32_t phase = 0;
-  unsigned long long n_work = 0;  // length of this launch's work list
-  if (P.n_seg == 0) {
-    n_work = P.rule_item_base[P.n_rules];
-  } else {
-    for (uint32_t k = 0; k < P.n_seg; k++) n_work += P.seg_end[k] - P.seg_begin[k];
-  }
-  const long long t_start = clock64();
-  // warp-level cache of the last (rule, left key) item range
-  uint32_t c_rule = 0xffffffffu, c_key = 0;
-  unsigned long long c_lo = 1, c_hi = 0;
-  unsigned long long done = 0;
-  WorkTally tally{0ull, 0u, 0u};
 
-  for (;;) {
-    unsigned long long v = 0;
-    if (lane == 0) v = atomicAdd(&P.ctr->work_next, 1ull);
-    v = __shfl_sync(kFull, v, 0);
-    if (v >= n_work) break;
+// Work positions a warp claims with one atomic: consecutive items mostly
+// share their (rule, left key), so the warp's key cache serves the rest.
+constexpr uint32_t kClaimChunk = 4;
+
+// Claims the next work item whose rule has similarity predicates and starts
+// the bulk copies of its right rows, their metadata and its left string's
+// metadata into staging buffer b (completing on bar).  Items of rules with
+// equalities only are emitted on the spot.  Positions come from the warp's
+// chunk [*cv, *cv_end), refilled by one atomic.  Once the work list is
+// exhausted or the cycle budget has run out, *stop is set and this and every
+// later claim leave c_n[b] = 0.
+__device__ __forceinline__ void claim_item(const EvalParams& P, WarpCtl* C, uint32_t b,
+                                           uint32_t* buf, uint64_t* bar, unsigned long long n_work,
+                                           long long t_start, bool* stop, unsigned long long* cv,
+                                           unsigned long long* cv_end, unsigned long long* done) {
+  const int lane = threadIdx.x & 31;
+  while (!*stop) {
+    if (*cv >= *cv_end) {
+      unsigned long long v0 = 0;
+      if (lane == 0) v0 = atomicAdd(&P.ctr->work_next, (unsigned long long)kClaimChunk);
+      v0 = __shfl_sync(kFull, v0, 0);
+      if (v0 >= n_work) {
+        *stop = true;
+        break;
+      }
+      *cv = v0;
+      *cv_end = min(v0 + kClaimChunk, n_work);
+    }
+    const unsigned long long v = (*cv)++;
     if (P.watchdog_cycles && (unsigned long long)(clock64() - t_start) > P.watchdog_cycles) {
       if (lane == 0) atomicAdd(&P.ctr->watchdog_trips, 1ull);
+      *stop = true;
       break;
     }
     const unsigned long long it = P.n_seg ? seg_item(P, v) : v;
@@ -1047,103 +1039,240 @@ __device__ __forceinline__ void eval_body(const EvalParams& P) {
     while (r + 1 < P.n_rules && P.rule_item_base[r + 1] <= it) r++;
     const Rule& R = P.rules[r];
     const unsigned long long local = it - P.rule_item_base[r];
-    if (r != c_rule || local < c_lo || local >= c_hi) {
-      c_rule = r;
-      c_key = find_key(R.item_off, R.domain_l, local);
-      c_lo = R.item_off[c_key];
-      c_hi = R.item_off[c_key + 1];
+    unsigned long long lo = C->k_lo;
+    uint32_t nl = C->k_nl, offl = C->k_offl, offr = C->k_offr, endr = C->k_endr;
+    if (r != C->k_rule || local < lo || local >= C->k_hi) {
+      const uint32_t jl = find_key(R.item_off, R.domain_l, local);  // (word class, join key)
+      const uint32_t key = jl % R.domain;                           // join key
+      lo = R.item_off[jl];
+      const unsigned long long hi = R.item_off[jl + 1];
+      nl = R.cnt_l[jl];
+      offl = R.off_l[jl];
+      offr = R.off_r[key];
+      endr = offr + R.cnt_r[key];
+      __syncwarp();
+      C->k_rule = r;
+      C->k_key = jl;
+      C->k_lo = lo;
+      C->k_hi = hi;
+      C->k_nl = nl;
+      C->k_offl = offl;
+      C->k_offr = offr;
+      C->k_endr = endr;
     }
-    const uint32_t jl = c_key;            // left key (word class, join key)
-    const uint32_t key = jl % R.domain;   // join key
-    const unsigned long long in_key = local - c_lo;
-    const uint32_t nl = R.cnt_l[jl], nr = R.cnt_r[key];
+    const unsigned long long in_key = local - lo;
     const uint32_t ri = (uint32_t)(in_key / nl);
     const uint32_t li = (uint32_t)(in_key - (unsigned long long)ri * nl);
-    const uint32_t lrow = R.sorted_l[R.off_l[jl] + li];
-    const uint32_t rb0 = R.off_r[key] + ri * P.tile_right;
-    const uint32_t rb1 = min(rb0 + P.tile_right, R.off_r[key] + nr);
-
+    const uint32_t lrow = R.sorted_l[offl + li];
+    const uint32_t rb0 = offr + ri * P.tile_right;
+    const uint32_t rb1 = min(rb0 + P.tile_right, endr);
     if (R.n_sim == 0) {  // equalities only: every candidate matches
       for (uint32_t rb = rb0; rb < rb1; rb += 32) {
         const uint32_t idx = rb + (uint32_t)lane;
         const uint32_t rrow = idx < rb1 ? R.sorted_r[idx] : 0u;
         emit(P, idx < rb1, lrow, rrow, lane);
       }
-    } else {
-      // stage the item's right rows and their string metadata (two contiguous,
-      // 16-byte aligned blocks) with bulk copies while the Peq table is built
-      const uint32_t a0 = rb0 & ~3u;
-      if (lane == 0) {
-        const uint32_t mbytes = (rb1 - rb0) * (uint32_t)sizeof(StrMeta);
-        const uint32_t rbytes = ((rb1 - a0) * 4u + 15u) & ~15u;
-        // the previous item's reads of these buffers are done (__syncwarp);
-        // order them before the asynchronous writes
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        mbar_expect_tx(bar, mbytes + rbytes);
-        bulk_g2s(st_meta, R.sorted_meta_r + rb0, mbytes, bar);
-        bulk_g2s(st_rows, R.sorted_r + a0, rbytes, bar);
-      }
-      bool staged = false;
-      Stage A;
-      A.rows = st_rows + (rb0 - a0);
-      A.meta = st_meta;
-      A.q = q;
-      A.n = rb1 - rb0;
-      for (uint32_t s = 0; s < R.n_sim && A.n > 0; s++) {
-        const uint32_t sl = R.sim_l[s];
-        const StrMeta* amp = P.L.str_meta + (size_t)sl * P.L.n_rows + lrow;
-        const uint4 aloc = amp->loc;
-        A.la = aloc.y;
-        A.a = P.L.arena + 16ull * aloc.x;
-        A.a_head = amp->head;
-        if (lane < 2) l_sig[lane] = amp->sig[lane];
-        __syncwarp();
-        A.a_sig = l_sig;
-        A.thr = R.thr[s];
-        A.slot_r = R.sim_r[s];
-        A.last = s + 1 == R.n_sim;
-        const uint32_t W = (A.la + 31u) >> 5;
-        const bool fast =
-            A.la > 0 && A.la <= 256 && R.peq_rows_words[s] >= (uint32_t)row_words((int)W);
-        uint32_t* tab = region + R.peq_off[s];
-        if (fast) build_peq(tab, (uint32_t)row_words((int)W), P.n_symbols, A.a, A.la, lane);
-        if (!staged) {
-          staged = true;
-          const bool ok = mbar_wait(bar, phase);
-          phase ^= 1u;
-          if (!__all_sync(kFull, ok)) {
-            // the copy never completed: report, wait (bounded) for it, stop
-            if (lane == 0) atomicAdd(&P.ctr->watchdog_trips, 1ull);
-            mbar_wait(bar, phase ^ 1u);
-            goto out;
-          }
-        }
-        uint32_t n_next;
-        if (fast) {
-          A.tab = tab;
-          n_next = stage_dispatch(W, P, A, lrow, &tally);
-        } else {
-          n_next = run_stage_slow(P, A, &tally, lrow);
-        }
-        A.meta = nullptr;  // later stages: survivors kept in A.rows
-        A.n = n_next;
-      }
-      if (!staged) {  // no stage ran: still consume the phase of this item's copies
-        const bool ok = mbar_wait(bar, phase);
-        phase ^= 1u;
-        if (!__all_sync(kFull, ok)) {
-          if (lane == 0) atomicAdd(&P.ctr->watchdog_trips, 1ull);
-          goto out;
-        }
-      }
-      __syncwarp();
+      (*done)++;
+      continue;
     }
-    done++;
+    const uint32_t a0 = rb0 & ~3u;
+    if (lane == 0) {
+      const uint32_t mbytes = (rb1 - rb0) * (uint32_t)sizeof(StrMeta);
+      const uint32_t rbytes = ((rb1 - a0) * 4u + 15u) & ~15u;
+      const StrMeta* lm = P.L.str_meta + (size_t)R.sim_l[0] * P.L.n_rows + lrow;
+      // earlier reads of this buffer are done (__syncwarp before the claim);
+      // order them before the asynchronous writes
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_expect_tx(bar, mbytes + rbytes + (uint32_t)sizeof(StrMeta));
+      bulk_g2s(buf, R.sorted_meta_r + rb0, mbytes, bar);
+      bulk_g2s(buf + P.buf_rows_off, R.sorted_r + a0, rbytes, bar);
+      bulk_g2s(buf + P.buf_lmeta_off, lm, (uint32_t)sizeof(StrMeta), bar);
+    }
+    C->c_rule[b] = r;
+    C->c_lrow[b] = lrow;
+    C->c_n[b] = rb1 - rb0;
+    C->c_shift[b] = rb0 - a0;
+    return;
   }
-out:
-  if (lane == 0 && done) atomicAdd(&P.ctr->items_done, done);
+  C->c_n[b] = 0;
+}
+
+// The evaluation loop of one warp, for scans over W-word masks.  Work items
+// (one left row x up to tile_right right rows of one candidate block) are
+// claimed one ahead, so the bulk copies of the next item run while the
+// current one is filtered.  Filtered pairs queue in the warp's ring; lanes
+// take the next queued pair as soon as theirs is decided, whichever item it
+// came from, since every pair reads its left string's Peq table from device
+// memory; the ring is refilled from the current item, then the next ones, as
+// it drains.  A pair that passes a predicate goes on with the rule's next
+// one in the same lane; matches leave by warp-aggregated atomics.
+template <int W>
+__device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
+                                          unsigned long long n_work, WorkTally* ops,
+                                          unsigned long long* done) {
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  uint4* q = reinterpret_cast<uint4*>(region);
+  WarpCtl* C = reinterpret_cast<WarpCtl*>(region + P.ctl_off);
+  uint64_t* bar0 = reinterpret_cast<uint64_t*>(region + P.mbar_off);
+  const long long t_start = clock64();
+  if (lane == 0) {
+    C->k_rule = 0xffffffffu;
+    C->k_lo = 1ull;
+    C->k_hi = 0ull;
+  }
+  __syncwarp();
+  bool stop = false;
+  unsigned long long cv = 0, cv_end = 0;  // the warp's claimed work positions
+  claim_item(P, C, 0, region + P.buf_off0, bar0, n_work, t_start, &stop, &cv, &cv_end, done);
+  claim_item(P, C, 1, region + P.buf_off1, bar0 + 1, n_work, t_start, &stop, &cv, &cv_end, done);
+  uint32_t cb = 0;      // buffer of the current item (the other holds the next)
+  uint32_t phs = 0;     // bit b: mbarrier phase of buffer b
+  bool active = false;  // current item waited for and being filtered
+  uint32_t in_pos = 0, cur_n = C->c_n[0];
+  uint32_t head = 0, tail = 0;
+  // lane state
+  bool busy = false;
+  uint32_t rrow = 0, lrow = 0, rule = 0, s = 0;
+  Scan<W> z;
+  z.tab = nullptr;
+  z.b = nullptr;
+  z.cur = z.nxt = make_uint4(0, 0, 0, 0);
+  z.ls = z.ll = z.i = z.n_iter = z.h = z.p = 0;
+  z.allowed = 0;
+  z.thr = 0.0f;
 #pragma unroll
+  for (int k = 0; k < W; k++) z.win[k] = z.mt[k] = 0u;
+
+  for (;;) {
+    const unsigned idle = __ballot_sync(kFull, !busy);
+    const uint32_t n_idle = __popc(idle);
+    // refill the ring until it holds a pair for every idle lane
+    while (tail - head < n_idle && tail - head <= kRing - 32) {
+      uint32_t* buf = region + (cb ? P.buf_off1 : P.buf_off0);
+      if (active) {
+        if (in_pos < cur_n) {
+          tail += filter_batch(P, C, reinterpret_cast<const StrMeta*>(buf + P.buf_lmeta_off),
+                               buf + P.buf_rows_off + C->c_shift[cb],
+                               reinterpret_cast<const StrMeta*>(buf), cur_n, in_pos, q, tail, ops);
+          in_pos += 32;
+          continue;
+        }
+        // the item is filtered: its buffer takes the item after the next one
+        active = false;
+        __syncwarp();
+        claim_item(P, C, cb, buf, bar0 + cb, n_work, t_start, &stop, &cv, &cv_end, done);
+        cb ^= 1u;
+        buf = region + (cb ? P.buf_off1 : P.buf_off0);
+        cur_n = C->c_n[cb];
+      }
+      if (cur_n == 0) break;  // no work left (claims run in order)
+      const bool ok = mbar_wait(bar0 + cb, (phs >> cb) & 1u);
+      phs ^= 1u << cb;
+      if (!__all_sync(kFull, ok)) {
+        // a copy never completed: report, wait once more (bounded) for it
+        // and for the other buffer's copies, stop
+        if (lane == 0) atomicAdd(&P.ctr->watchdog_trips, 1ull);
+        mbar_wait(bar0 + cb, ((phs >> cb) & 1u) ^ 1u);
+        if (C->c_n[cb ^ 1u]) mbar_wait(bar0 + (cb ^ 1u), (phs >> (cb ^ 1u)) & 1u);
+        return;
+      }
+      active = true;
+      in_pos = 0;
+      (*done)++;
+      const StrMeta* lm = reinterpret_cast<const StrMeta*>(buf + P.buf_lmeta_off);
+      const uint32_t ir = C->c_rule[cb];
+      const Rule& R = P.rules[ir];
+      const uint32_t il = C->c_lrow[cb];
+      const uint32_t la = lm->loc.y;
+      C->i_rule = ir;
+      C->i_lrow = il;
+      C->i_thr = R.thr[0];
+      C->i_more = R.n_sim > 1 ? 1u : 0u;
+      C->i_fast = has_table(P, la) ? 1u : 0u;
+    }
+    // idle lanes take the next queued pairs
+    bool fin = false, pass = false;
+    const uint32_t avail = tail - head;
+    const uint32_t rank = __popc(idle & lt);
+    if (!busy && rank < avail) {
+      const uint4* en = q + kRingWords / 4 * ((head + rank) & (kRing - 1));
+      const uint4 e0 = en[0], e2 = en[2];
+      rrow = e0.x;
+      lrow = e2.x;
+      rule = e2.w;
+      s = (e0.w >> 15) & 7u;
+      int st = 0;
+      if (e0.w & kAdvance) {
+        st = advance<W>(P, rule, &s, lrow, rrow, z, ops);
+      } else {
+        const Rule* R = P.rules + rule;
+        const uint32_t sl = R->sim_l[s];
+        const uint32_t p = (e0.w >> 10) & 31u;
+        st = scan_begin<W>(z, peq_table(P, sl, lrow), P.L.arena + 16ull * e2.z,
+                           P.R.arena + 16ull * e0.y, en[1], e2.y, e0.z, p, (int)(e0.w & 1023u),
+                           R->thr[s], ops)
+                 ? 2
+                 : 0;
+      }
+      if (st == 2) {
+        busy = true;
+      } else {
+        fin = true;
+        pass = st == 1;
+      }
+    }
+    head += min(n_idle, avail);
+    if (busy) {
+      bool ok = false;
+      if (scan_step<W>(z, &ok, P.ctr, ops)) {
+        busy = false;
+        int st = ok ? 1 : 0;
+        if (ok) st = advance<W>(P, rule, &s, lrow, rrow, z, ops);
+        if (st == 2) {
+          busy = true;
+        } else {
+          fin = true;
+          pass = st == 1;
+        }
+      }
+    }
+    emit(P, fin && pass, lrow, rrow, lane);
+    if (!__any_sync(kFull, busy) && head == tail && !active && cur_n == 0) break;
+  }
+}
+
+// The evaluation kernel body, instantiated twice below with different
+// register budgets (see k_eval / k_eval_wide).
+__device__ __forceinline__ void eval_body(const EvalParams& P) {
+  extern __shared__ __align__(16) uint32_t smem[];
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  uint32_t* region = smem + (size_t)warp * P.warp_words;
+  if (lane == 0) {
+    uint64_t* bar = reinterpret_cast<uint64_t*>(region + P.mbar_off);
+    mbar_init(bar);
+    mbar_init(bar + 1);
+  }
+  __syncwarp();
+  unsigned long long n_work = 0;  // length of this launch's work list
+  if (P.n_seg == 0) {
+    n_work = P.rule_item_base[P.n_rules];
+  } else {
+    for (uint32_t k = 0; k < P.n_seg; k++) n_work += P.seg_end[k] - P.seg_begin[k];
+  }
+  unsigned long long done = 0;
+  WorkTally tally{0ull, 0u, 0u};
+  switch (P.peq_w) {
+    case 1: eval_loop<1>(P, region, n_work, &tally, &done); break;
+    case 2: eval_loop<2>(P, region, n_work, &tally, &done); break;
+    case 3: eval_loop<3>(P, region, n_work, &tally, &done); break;
+    case 4: eval_loop<4>(P, region, n_work, &tally, &done); break;
+    default: eval_loop<8>(P, region, n_work, &tally, &done); break;
+  }
+  if (lane == 0 && done) atomicAdd(&P.ctr->items_done, done);
   unsigned long long ops = tally.ops, scans = tally.scans, steps = tally.steps;
+#pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     ops += __shfl_down_sync(kFull, ops, o);
     scans += __shfl_down_sync(kFull, scans, o);
@@ -1153,6 +1282,35 @@ out:
     if (ops) atomicAdd(&P.ctr->jw_word_ops, ops);
     if (scans) atomicAdd(&P.ctr->scans, scans);
     if (steps) atomicAdd(&P.ctr->scan_steps, steps);
+  }
+}
+
+// Peq tables (PeqShape): one warp per (slot, row); the table is cleared,
+// then every symbol's mask per 32-symbol word is built with __match_any_sync
+// (lanes holding the same symbol agree on it; the lowest of them stores it).
+__global__ void k_peq_build(Side L, uint32_t n_slots, PeqShape shape, uint32_t* peq) {
+  const int lane = threadIdx.x & 31;
+  const unsigned long long n_tasks = (unsigned long long)n_slots * L.n_rows;
+  const unsigned long long n_warps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
+  for (unsigned long long t = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+       t < n_tasks; t += n_warps) {
+    const uint4 loc = L.str_meta[t].loc;  // slot-major: t = slot * n_rows + row
+    const uint32_t la = loc.y;
+    if (la == 0 || la > shape.fast_max) continue;
+    uint32_t* tab = peq + t * shape.tab_words;
+    uint4* t4 = reinterpret_cast<uint4*>(tab);
+    for (uint32_t w = (uint32_t)lane; w < shape.tab_words / 4; w += 32)
+      t4[w] = make_uint4(0, 0, 0, 0);
+    __syncwarp();
+    const uint8_t* a = L.arena + 16ull * loc.x;
+    const uint32_t nw = (la + 31u) >> 5;
+    for (uint32_t k = 0; k < nw; k++) {
+      const uint32_t j = k * 32u + (uint32_t)lane;
+      const uint32_t sym = j < la ? (uint32_t)a[j] : 0xffffffffu;
+      const unsigned mm = __match_any_sync(kFull, sym);
+      if (j < la && lane == __ffs(mm) - 1) tab[sym * shape.s + k] = mm;
+    }
+    __syncwarp();
   }
 }
 

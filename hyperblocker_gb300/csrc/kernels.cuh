@@ -9,15 +9,18 @@
 //                     of one candidate block).
 //   3. k_scatter      rows grouped by key (counting sort) -> candidate blocks
 //                     L_key x R_key.
-//   4. k_eval         persistent, warp-granular work stealing over the items
-//                     of every rule: the warp's left string becomes a Peq
-//                     bitmask table in shared memory (built with __match_any);
-//                     a rule's similarity predicates run as stages over a
-//                     shared-memory queue of survivors; inside a stage lanes
-//                     take the next right row as soon as theirs is decided
-//                     (bit-parallel Jaro, exact early-fail bound), so lanes do
-//                     not wait on longer strings; matches leave by
-//                     warp-aggregated atomics.
+//   4. k_peq_build    Peq bitmask table of every left string (built with
+//                     __match_any), in device memory.
+//   5. k_eval         persistent, warp-granular work stealing over the items
+//                     of every rule: a warp filters an item's right rows
+//                     (staged by bulk copies, the next item's copies in
+//                     flight) against the first similarity predicate and
+//                     queues the pairs that need a scan in a shared-memory
+//                     ring; lanes take the next queued pair, of whatever
+//                     item, as soon as theirs is decided (bit-parallel Jaro
+//                     from the left string's table, exact early-fail bound),
+//                     and go on with the rule's next predicate in the same
+//                     lane; matches leave by warp-aggregated atomics.
 //
 // Semantics reproduced (reference = HyperBlocker):
 //   * pairs are compared only inside a partition (data_mngr.h:150-216, the
@@ -101,8 +104,6 @@ struct Rule {
   uint32_t radix[kMaxEq];
   uint32_t sim_l[kMaxSim], sim_r[kMaxSim];
   float thr[kMaxSim];
-  uint32_t peq_rows_words[kMaxSim];  // words per symbol row reserved (1,2,4,8), 0 = none
-  uint32_t peq_off[kMaxSim];         // word offset of the sim's table in a warp region
   uint32_t domain;    // D: join keys
   // Left rows are grouped by (word class, key): the word class is the number
   // of 32-symbol words of the left string of the first similarity predicate
@@ -131,33 +132,58 @@ struct Rule {
 constexpr uint32_t kWordClasses = 5;
 constexpr uint32_t kMaxSegments = 8;
 constexpr uint32_t kRingEntries = 64;
+constexpr uint32_t kRingWords = 12;  // words per ring entry (three 16-byte records)
 
-// Shared memory of one warp of k_eval, in 32-bit words: the Peq tables
-// (peq_words, a multiple of 4), then the scan ring (kRingEntries x 32 bytes),
-// the staged item metadata (tile_right StrMeta records), the staged item rows
-// (tile_right + 8: a 16-byte-aligned copy starts up to 3 rows early and rounds
-// up; the same words then hold the rows that survive each stage), the count
-// signature of the stage's left string (8 words) and one mbarrier.  Every
-// offset is a multiple of 4 words (16 bytes) when tile_right is a multiple of
-// 32.
-struct WarpLayout {
-  uint32_t queue_off, stage_meta_off, stage_rows_off, sig_off, mbar_off, warp_words;
+// Peq tables of the left strings, in device memory: one per (left string
+// slot, left row), tab_words 32-bit words each; row `sym` (peq_s words) has
+// bit j of word k set when a[32k + j] == sym.  Strings of 1 to fast_max
+// symbols have a table; fast_max = 32 * peq_w <= 256.
+struct PeqShape {
+  uint32_t w;          // words the scans run on: 1, 2, 3, 4 or 8
+  uint32_t s;          // words per symbol row: row_words(w)
+  uint32_t tab_words;  // words per table (a multiple of 4: tables are 16-byte aligned)
+  uint32_t fast_max;   // longest left string with a table
 };
 
-inline WarpLayout warp_layout(uint32_t peq_words, uint32_t tile_right) {
-  WarpLayout w;
-  w.queue_off = peq_words;
-  w.stage_meta_off = w.queue_off + 8 * kRingEntries;
-  w.stage_rows_off = w.stage_meta_off + (uint32_t)(sizeof(StrMeta) / 4) * tile_right;
-  w.sig_off = w.stage_rows_off + tile_right + 8;
-  w.mbar_off = w.sig_off + 8;
-  w.warp_words = w.mbar_off + 4;
-  return w;
+// Shape for left strings up to max_len symbols (capped at 256) over an
+// alphabet of n_symbols symbols.
+inline PeqShape peq_shape(uint32_t max_len, uint32_t n_symbols) {
+  const uint32_t len = max_len < 1 ? 1 : (max_len > 256 ? 256 : max_len);
+  const uint32_t w0 = (len + 31) / 32;
+  PeqShape p;
+  p.w = w0 <= 4 ? w0 : 8;
+  p.s = (uint32_t)row_words((int)p.w);
+  p.tab_words = (n_symbols * p.s + 3) / 4 * 4;
+  p.fast_max = 32 * p.w;
+  return p;
 }
 
-// Words of a warp's layout that do not depend on the Peq tables.
-inline uint32_t warp_layout_fixed_words(uint32_t tile_right) {
-  return warp_layout(0, tile_right).warp_words;
+// Shared memory of one warp of k_eval, in 32-bit words: the ring of pairs
+// waiting for a scan (kRingEntries x kRingWords), two staging buffers (while
+// the warp filters one work item, the bulk copies of the next one fill the
+// other) and two mbarriers.  A staging buffer holds the item's right-row
+// metadata (tile_right StrMeta records), its right rows (tile_right + 8: a
+// 16-byte-aligned copy starts up to 3 rows early and rounds up) and the
+// metadata of its left string.  Every offset is a multiple of 4 words (16
+// bytes) when tile_right is a multiple of 32.  A control block of
+// kWarpCtlWords words follows.
+struct WarpLayout {
+  uint32_t buf_off[2], buf_rows_off, buf_lmeta_off, mbar_off, ctl_off, warp_words;
+};
+constexpr uint32_t kWarpCtlWords = 40;  // the warp's control block (kernels.cu: WarpCtl)
+
+inline WarpLayout warp_layout(uint32_t tile_right) {
+  WarpLayout w;
+  const uint32_t meta_words = (uint32_t)(sizeof(StrMeta) / 4) * tile_right;
+  w.buf_rows_off = meta_words;
+  w.buf_lmeta_off = meta_words + (tile_right + 8 + 3) / 4 * 4;
+  const uint32_t buf_words = w.buf_lmeta_off + (uint32_t)(sizeof(StrMeta) / 4);
+  w.buf_off[0] = kRingWords * kRingEntries;
+  w.buf_off[1] = w.buf_off[0] + buf_words;
+  w.mbar_off = w.buf_off[1] + buf_words;
+  w.ctl_off = w.mbar_off + 4;
+  w.warp_words = w.ctl_off + kWarpCtlWords;
+  return w;
 }
 
 __host__ __device__ inline uint32_t word_class(uint32_t len) {
@@ -193,12 +219,11 @@ struct EvalParams {
   unsigned long long seg_begin[kMaxSegments];
   unsigned long long seg_end[kMaxSegments];
   uint32_t tile_right;  // TR
-  uint32_t warp_words;      // shared-memory words per warp (see warp_layout)
-  uint32_t queue_off;       // word offset of the warp's scan ring
-  uint32_t stage_meta_off;  // word offset of the staged item metadata
-  uint32_t stage_rows_off;  // word offset of the staged item rows / survivor list
-  uint32_t sig_off;         // word offset of the left string's count signature
-  uint32_t mbar_off;        // word offset of the warp's mbarrier (8-byte aligned)
+  // shared-memory words per warp and offsets inside a warp's region (warp_layout)
+  uint32_t warp_words, buf_off0, buf_off1, buf_rows_off, buf_lmeta_off, mbar_off, ctl_off;
+  // Peq tables of the left strings (PeqShape): [left string slot][left row]
+  const uint32_t* peq;
+  uint32_t peq_w, tab_words, fast_max;
   uint32_t* out_l;
   uint32_t* out_r;
   unsigned long long capacity;
@@ -208,6 +233,21 @@ struct EvalParams {
   unsigned long long* seen;
   unsigned long long seen_mask;  // slots - 1 (a power of two minus one)
 };
+
+// Host: the shared-memory layout and Peq tables of a launch.
+inline void set_layout(EvalParams* P, const WarpLayout& w, const PeqShape& s, const uint32_t* peq) {
+  P->warp_words = w.warp_words;
+  P->buf_off0 = w.buf_off[0];
+  P->buf_off1 = w.buf_off[1];
+  P->buf_rows_off = w.buf_rows_off;
+  P->buf_lmeta_off = w.buf_lmeta_off;
+  P->mbar_off = w.mbar_off;
+  P->ctl_off = w.ctl_off;
+  P->peq = peq;
+  P->peq_w = s.w;
+  P->tab_words = s.tab_words;
+  P->fast_max = s.fast_max;
+}
 
 // ------------------------------------------------------------------ join
 __global__ void k_keys_hist(Side S, const Rule* rules, uint32_t rule, int side);
@@ -231,6 +271,8 @@ __global__ void k_join_scan(const Rule* rules, uint32_t tile_right, unsigned lon
 __global__ void k_join_scatter(Side L, Side R, const Rule* rules, uint32_t n_rules,
                                unsigned long long* rule_base);
 // ------------------------------------------------------------------ evaluation
+// Peq tables of every left string of n_slots string slots (PeqShape).
+__global__ void k_peq_build(Side L, uint32_t n_slots, PeqShape shape, uint32_t* peq);
 __global__ void k_eval(EvalParams P);       // 3 CTAs per SM (register-limited)
 __global__ void k_eval_wide(EvalParams P);  // 2 CTAs per SM (more registers)
 

@@ -236,9 +236,8 @@ struct Slot {
   DBuf<uint32_t> out_l, out_r;
   uint64_t capacity = 0;
   uint64_t cmp_first = 0;  // comparisons counted by the first evaluation pass
-  dev::WarpLayout wl{};    // this batch's shared-memory layout
-  size_t smem_bytes = 0;
-  int blocks_per_sm = 1;
+  dev::PeqShape shape{};   // Peq tables of this batch's left strings
+  DBuf<uint32_t> peq;
   Pinned stage, h_out, h_ctr;  // h_ctr: Counters + total items + comparisons per instance
   ~Slot() {
     release();  // buffers return to the pool on this slot's stream first
@@ -260,6 +259,7 @@ struct Slot {
     d_ctr.reset();
     out_l.reset();
     out_r.reset();
+    peq.reset();
     capacity = 0;
     state = 0;
   }
@@ -291,10 +291,12 @@ struct hbx_server {
   int left_cols_min = 0;
   bool any_multi_rule = false;
   uint64_t resident_bytes = 0;
-  // kernel configuration (each batch lays out its own Peq tables)
-  uint32_t tile_right = 128;
+  // kernel configuration
+  uint32_t tile_right = 64;
   int variant = 1;
-  uint32_t max_peq = 0;  // shared-memory words per warp the Peq tables may take
+  dev::WarpLayout wl{};
+  size_t smem_bytes = 0;
+  int blocks_per_sm = 1;
   // queue and results
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
@@ -508,18 +510,16 @@ void open_server(hbx_server* S, const hbx_plan* const* plans, int32_t n_plans, c
   S->R.comp.alloc(1);
   S->side_r = dev::Side{S->R.bucket.p, S->R.eq.p, S->R.comp.p, S->R.arena.p, S->R.meta.p, nR};
 
-  // ---- kernel configuration: Peq tables sized for left strings up to 256
-  S->tile_right = S->opts.tile_right > 0 ? (uint32_t)S->opts.tile_right : 128u;
+  // ---- kernel configuration
+  S->tile_right = S->opts.tile_right > 0 ? (uint32_t)S->opts.tile_right : 64u;
   S->tile_right = std::min<uint32_t>(512, std::max<uint32_t>(32, (S->tile_right + 31) / 32 * 32));
   S->variant = S->opts.eval_variant == 1 ? 0 : 1;
   const dev::EvalKernel kern = dev::eval_kernel(S->variant);
   const size_t smem_cap = std::min<size_t>(C->smem_optin, 200 * 1024);
   const uint32_t cap_warp_words = (uint32_t)(smem_cap / 4 / dev::kWarpsPerCta) / 4 * 4;
-  const uint32_t fixed_words = dev::warp_layout_fixed_words(S->tile_right);
-  if (fixed_words + 4 > cap_warp_words) fail(HBX_ERR_INVALID_ARG, "tile_right too large");
-  S->max_peq = cap_warp_words - fixed_words;
-  const uint32_t full_rows = (uint32_t)dev::row_words(kFastMaxLen / 32);
-  uint32_t warp_words = 4;  // largest layout any batch can need: strings up to 256
+  S->wl = dev::warp_layout(S->tile_right);
+  if (S->wl.warp_words > cap_warp_words) fail(HBX_ERR_INVALID_ARG, "tile_right too large");
+  S->smem_bytes = (size_t)S->wl.warp_words * 4 * dev::kWarpsPerCta;
 
   // ---- rules and their resident right-side joins
   for (int32_t p = 0; p < n_plans; p++) {
@@ -537,15 +537,11 @@ void open_server(hbx_server* S, const hbx_plan* const* plans, int32_t n_plans, c
         if (D > kMaxKeyDomain)
           fail(HBX_ERR_UNSUPPORTED, "a served rule's equality key domain is above 2^24");
       }
-      uint32_t off = 0;
       for (size_t s = 0; s < pr.sim_l.size(); s++) {
         d.sim_l[s] = (uint32_t)pr.sim_l[s];
         d.sim_r[s] = (uint32_t)pr.sim_r[s];
         d.thr[s] = pr.thr[s];
-        const uint32_t words = (S->n_symbols * full_rows + 3) / 4 * 4;
-        if (off + words <= S->max_peq) off += words;
       }
-      warp_words = std::max(warp_words, off);
       d.domain = (uint32_t)D;
       d.n_wclass = (d.n_sim && D * dev::kWordClasses <= (1ull << 22)) ? dev::kWordClasses : 1u;
       d.wclass_slot = d.n_sim ? d.sim_l[0] : 0u;
@@ -578,8 +574,12 @@ void open_server(hbx_server* S, const hbx_plan* const* plans, int32_t n_plans, c
       S->rules.push_back(std::move(T));
     }
   }
-  raise_smem_limit(kern, (size_t)dev::warp_layout(warp_words, S->tile_right).warp_words * 4 *
-                             dev::kWarpsPerCta);
+  raise_smem_limit(kern, S->smem_bytes);
+  {
+    int bps = 0;
+    HBX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, kThreads, S->smem_bytes));
+    S->blocks_per_sm = std::max(1, bps);
+  }
   HBX_CUDA(cudaStreamSynchronize(st));
 
   uint64_t rb = S->R.eq.n * 4 + S->R.arena.n + S->R.meta.n * sizeof(dev::StrMeta) + S->R.bucket.n * 4;
@@ -618,6 +618,8 @@ uint64_t estimate(const hbx_server* S, const Table& t, int32_t plan, uint32_t r0
   };
   for (int c : S->left_cols) b += bytes(c) + 8 * (n + 1) + 16;
   for (int c : S->lstr) b += bytes(c) + 15 * n + 16 + 40 * n;  // arena, metadata, scan
+  // Peq tables, at most 8 words per symbol row
+  b += 4ull * ((8ull * S->n_symbols + 3) / 4 * 4) * n * S->lstr.size() + 16;
   b += sizeof(dev::StrMeta) * n * S->lstr.size() + 4 * n * S->pairs.size();
   for (int r : S->plan_rules[(size_t)plan]) {
     const dev::Rule& d = S->rules[(size_t)r]->d;
@@ -687,19 +689,15 @@ void launch_batch(hbx_server* S, Slot& B) {
       if (S->left_cols[k] == c) return k;
     return (size_t)0;
   };
-  // Peq row stride the batch's left strings need per string slot: the
-  // longest string of the slot in this batch decides
-  std::vector<uint32_t> need(S->lstr.size(), 0);
-  for (size_t sl = 0; sl < S->lstr.size(); sl++) {
-    int64_t mx = 0;
+  // Peq tables shaped for the batch's longest left string (bytes bound symbols)
+  int64_t max_len = 1;
+  for (size_t sl = 0; sl < S->lstr.size(); sl++)
     for (auto& e : B.ents) {
       const Column& col = e.r->rows.cols[(size_t)S->lstr[sl]];
-      for (uint32_t i = e.r0; i < e.r1; i++) mx = std::max<int64_t>(mx, col.off[i + 1] - col.off[i]);
+      for (uint32_t i = e.r0; i < e.r1; i++)
+        max_len = std::max<int64_t>(max_len, col.off[i + 1] - col.off[i]);
     }
-    const uint32_t m = (uint32_t)std::min<int64_t>(mx, kFastMaxLen);
-    need[sl] = m ? (uint32_t)dev::row_words((int)((m + 31) / 32)) : 0u;
-  }
-  uint32_t warp_words = 4;
+  B.shape = dev::peq_shape((uint32_t)std::min<int64_t>(max_len, 1 << 20), S->n_symbols);
 
   // ---- encode the batch against the resident dictionaries and alphabet
   B.L.eq.alloc(std::max<size_t>(S->pairs.size() * (size_t)N, 1));
@@ -723,6 +721,16 @@ void launch_batch(hbx_server* S, Slot& B) {
   }
   B.L.comp.alloc(1);
   B.side_l = dev::Side{nullptr, B.L.eq.p, B.L.comp.p, B.L.arena.p, B.L.meta.p, N};
+  {
+    const uint32_t n_slots = (uint32_t)S->lstr.size();
+    const size_t words = (size_t)n_slots * N * B.shape.tab_words;
+    B.peq.alloc(std::max<size_t>(words, 4));
+    if (words) {
+      const uint64_t warps = (uint64_t)n_slots * N;
+      const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((warps + 7) / 8, (uint64_t)C->n_sm * 16));
+      dev::k_peq_build<<<grid, 256, 0, st>>>(B.side_l, n_slots, B.shape, B.peq.p);
+    }
+  }
   check_launch("serving batch encode");
 
   // ---- rule instances: (request, rule of its plan)
@@ -747,19 +755,6 @@ void launch_batch(hbx_server* S, Slot& B) {
       HBX_CUDA(cudaMemsetAsync(I.cnt_l.p, 0, (size_t)t.domain_l * 4, st));
       HBX_CUDA(cudaMemsetAsync(I.cur_l.p, 0, (size_t)t.domain_l * 4, st));
       dev::Rule d = t;
-      uint32_t off = 0;
-      for (uint32_t s = 0; s < d.n_sim; s++) {
-        const uint32_t rw = need[d.sim_l[s]];
-        const uint32_t words = (S->n_symbols * rw + 3) / 4 * 4;
-        d.peq_rows_words[s] = 0;
-        d.peq_off[s] = 0;
-        if (rw && off + words <= S->max_peq) {
-          d.peq_rows_words[s] = rw;
-          d.peq_off[s] = off;
-          off += words;
-        }
-      }
-      warp_words = std::max(warp_words, off);
       d.key_l = I.key_l.p;
       d.cnt_l = I.cnt_l.p;
       d.off_l = I.off_l.p;
@@ -768,14 +763,6 @@ void launch_batch(hbx_server* S, Slot& B) {
       d.sorted_l = I.sorted_l.p;
       B.h_rules.push_back(d);
     }
-  B.wl = dev::warp_layout(warp_words, S->tile_right);
-  B.smem_bytes = (size_t)B.wl.warp_words * 4 * dev::kWarpsPerCta;
-  {
-    int bps = 0;
-    HBX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, dev::eval_kernel(S->variant), kThreads,
-                                                           B.smem_bytes));
-    B.blocks_per_sm = std::max(1, bps);
-  }
   const uint32_t ni = (uint32_t)B.inst.size();
   B.d_rules.alloc(ni);
   HBX_CUDA(cudaMemcpyAsync(B.d_rules.p, B.h_rules.data(), ni * sizeof(dev::Rule),
@@ -828,12 +815,7 @@ void launch_eval(hbx_server* S, Slot& B) {
   P.rule_item_base = B.d_base.p;
   P.n_seg = 0;
   P.tile_right = S->tile_right;
-  P.warp_words = B.wl.warp_words;
-  P.queue_off = B.wl.queue_off;
-  P.stage_meta_off = B.wl.stage_meta_off;
-  P.stage_rows_off = B.wl.stage_rows_off;
-  P.sig_off = B.wl.sig_off;
-  P.mbar_off = B.wl.mbar_off;
+  dev::set_layout(&P, S->wl, B.shape, B.peq.p);
   P.out_l = B.out_l.p;
   P.out_r = B.out_r.p;
   P.capacity = B.capacity;
@@ -841,8 +823,8 @@ void launch_eval(hbx_server* S, Slot& B) {
   P.watchdog_cycles = 0;
   P.seen = B.seen.p;
   P.seen_mask = B.seen.p ? B.seen.n - 1 : 0;
-  const int grid = S->ctx->n_sm * B.blocks_per_sm;
-  dev::eval_kernel(S->variant)<<<grid, kThreads, B.smem_bytes, st>>>(P);
+  const int grid = S->ctx->n_sm * S->blocks_per_sm;
+  dev::eval_kernel(S->variant)<<<grid, kThreads, S->smem_bytes, st>>>(P);
   check_launch("serving k_eval");
   uint8_t* h = (uint8_t*)B.h_ctr.p;
   HBX_CUDA(cudaMemcpyAsync(h, B.d_ctr.p, sizeof(dev::Counters), cudaMemcpyDeviceToHost, st));

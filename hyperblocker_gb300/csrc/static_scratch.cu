@@ -121,7 +121,9 @@ struct Layout {
   uint32_t* part_u32 = nullptr;
   unsigned long long* part_u64 = nullptr;
   hbx::dev::WarpLayout wl{};
-  uint32_t tile_right = 128;
+  hbx::dev::PeqShape shape{};
+  uint32_t* peq = nullptr;
+  uint32_t tile_right = 64;
 };
 
 // Places every buffer; with c.base == nullptr it only measures.
@@ -140,10 +142,7 @@ void place(Carve& c, const hbx::Encoded& E, uint64_t capacity, size_t smem_cap, 
   };
   side(E.L, Y->L, nL, ml);
   side(E.R, Y->R, nR, mr);
-  const uint32_t NS = E.n_symbols;
-  const uint32_t cap_warp_words = (uint32_t)(smem_cap / 4 / dev::kWarpsPerCta) / 4 * 4;
-  const uint32_t max_warp_words = cap_warp_words - dev::warp_layout_fixed_words(Y->tile_right);
-  uint32_t warp_words = 4;
+  uint32_t max_len = 1;
   Y->rules.assign(E.rules.size(), dev::Rule{});
   Y->nb.assign(E.rules.size(), 0);
   Y->nb_l.assign(E.rules.size(), 0);
@@ -159,21 +158,12 @@ void place(Carve& c, const hbx::Encoded& E, uint64_t capacity, size_t smem_cap, 
       d.eq_slot[e] = (uint32_t)re.eq_slot[e];
       d.radix[e] = re.radix[e];
     }
-    uint32_t off = 0;
     for (size_t s = 0; s < re.sim_slot_l.size(); s++) {
       d.sim_l[s] = (uint32_t)re.sim_slot_l[s];
       d.sim_r[s] = (uint32_t)re.sim_slot_r[s];
       d.thr[s] = re.thr[s];
-      const uint32_t mx = std::min<uint32_t>(E.L.str_maxlen[(size_t)re.sim_slot_l[s]], hbx::kFastMaxLen);
-      const uint32_t S32 = mx ? (uint32_t)dev::row_words((int)((mx + 31) / 32)) : 0u;
-      const uint32_t words = (NS * S32 + 3) / 4 * 4;
-      if (S32 && off + words <= max_warp_words) {
-        d.peq_rows_words[s] = S32;
-        d.peq_off[s] = off;
-        off += words;
-      }
+      max_len = std::max(max_len, E.L.str_maxlen[(size_t)re.sim_slot_l[s]]);
     }
-    warp_words = std::max(warp_words, off);
     d.domain = (uint32_t)re.domain;
     const bool split = !re.sim_slot_l.empty() &&
                        re.domain * dev::kWordClasses <= (uint64_t)hbx::kMaxKeyDomain * 4;
@@ -196,7 +186,11 @@ void place(Carve& c, const hbx::Encoded& E, uint64_t capacity, size_t smem_cap, 
     Y->nb_l[r] = (d.domain_l + dev::kScanChunk - 1) / dev::kScanChunk;
     max_nb = std::max(max_nb, std::max(Y->nb[r], Y->nb_l[r]));
   }
-  Y->wl = dev::warp_layout(warp_words, Y->tile_right);
+  Y->wl = dev::warp_layout(Y->tile_right);
+  if ((size_t)Y->wl.warp_words * 4 * dev::kWarpsPerCta > smem_cap)
+    hbx::fail(HBX_ERR_INVALID_ARG, "tile_right too large");
+  Y->shape = dev::peq_shape(max_len, E.n_symbols);
+  Y->peq = c.take<uint32_t>(std::max<size_t>((size_t)E.L.str_maxlen.size() * nL * Y->shape.tab_words, 4));
   Y->part_u32 = c.take<uint32_t>(max_nb);
   Y->part_u64 = c.take<unsigned long long>(max_nb);
   Y->d_rules = c.take<dev::Rule>(E.rules.size());
@@ -294,6 +288,10 @@ void run_static(int device, const hbx_plan* plan, const hbx_table* left, const h
     if (nR) dev::k_scatter<<<grid_for(nR), 256, 0, st>>>(Y.R, Y.d_rules, ru, 1);
   }
   dev::k_rule_base<<<1, 32, 0, st>>>(Y.d_rules, (uint32_t)Y.rules.size(), Y.rule_base);
+  const uint32_t n_slots = (uint32_t)E.L.str_maxlen.size();
+  if (n_slots && nL)
+    dev::k_peq_build<<<grid_for((uint32_t)std::min<uint64_t>((uint64_t)n_slots * nL * 32, 1u << 30)), 256, 0,
+                       st>>>(Y.L, n_slots, Y.shape, Y.peq);
   HBX_STATIC_CUDA(cudaGetLastError());
 
   dev::EvalParams P{};
@@ -305,12 +303,7 @@ void run_static(int device, const hbx_plan* plan, const hbx_table* left, const h
   P.rule_item_base = Y.rule_base;
   P.n_seg = 0;
   P.tile_right = Y.tile_right;
-  P.warp_words = Y.wl.warp_words;
-  P.queue_off = Y.wl.queue_off;
-  P.stage_meta_off = Y.wl.stage_meta_off;
-  P.stage_rows_off = Y.wl.stage_rows_off;
-  P.sig_off = Y.wl.sig_off;
-  P.mbar_off = Y.wl.mbar_off;
+  dev::set_layout(&P, Y.wl, Y.shape, Y.peq);
   P.out_l = out->l_row;
   P.out_r = out->r_row;
   P.capacity = out->capacity;
@@ -322,15 +315,15 @@ void run_static(int device, const hbx_plan* plan, const hbx_table* left, const h
     static std::mutex mu;
     std::lock_guard<std::mutex> lock(mu);
     cudaFuncAttributes fa;
-    HBX_STATIC_CUDA(cudaFuncGetAttributes(&fa, dev::k_eval));
+    HBX_STATIC_CUDA(cudaFuncGetAttributes(&fa, dev::k_eval_wide));
     if ((size_t)fa.maxDynamicSharedSizeBytes < smem)
-      HBX_STATIC_CUDA(cudaFuncSetAttribute(dev::k_eval, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      HBX_STATIC_CUDA(cudaFuncSetAttribute(dev::k_eval_wide, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem));
   }
   int bps = 0;
-  HBX_STATIC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, dev::k_eval,
+  HBX_STATIC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, dev::k_eval_wide,
                                                                 dev::kWarpsPerCta * 32, smem));
-  dev::k_eval<<<n_sm * std::max(1, bps), dev::kWarpsPerCta * 32, smem, st>>>(P);
+  dev::k_eval_wide<<<n_sm * std::max(1, bps), dev::kWarpsPerCta * 32, smem, st>>>(P);
   HBX_STATIC_CUDA(cudaGetLastError());
 
   dev::Counters c{};
@@ -345,7 +338,7 @@ void run_static(int device, const hbx_plan* plan, const hbx_table* left, const h
   if (stats) {
     *stats = hbx_stats{};
     stats->tile_right = Y.tile_right;
-    stats->eval_variant = 1;
+    stats->eval_variant = 2;
     stats->pairs_covered = E.pairs_covered;
     stats->pair_comparisons = c.comparisons;
     stats->n_matches = c.out_count;

@@ -167,7 +167,7 @@ def test_cli_drop_in(built, golden, tmp_path):
     assert len(open(out, "rb").read().splitlines()) == 2 * len(lines)  # append mode
 
 
-@pytest.mark.parametrize("tile", [32, 64, 256])
+@pytest.mark.parametrize("tile", [32, 64, 128])
 @pytest.mark.parametrize("variant", [1, 2])
 def test_tile_shapes_and_kernel_variants_agree(built, tile, variant):
     """Every tile shape and both evaluation kernels give the oracle's pairs."""
@@ -179,6 +179,28 @@ def test_tile_shapes_and_kernel_variants_agree(built, tile, variant):
         got, st = _engine_pairs(c, docs, cl, cr, 2, _util.INT_MAX, mode)
         assert np.array_equal(got, want.pairs), (tile, variant, mode)
     c.close()
+
+
+@pytest.mark.parametrize("variant", [1, 2])
+def test_pairs_of_many_items_share_a_warp(built, variant):
+    """A warp's lanes scan pairs of different work items, rules and
+    predicates at once: an equality-only rule (emitted at claim time) beside
+    rules of one and two predicates over strings of 0-300 bytes (every scan
+    width, tables and the reference loops in one launch), many small
+    candidate blocks, every tile shape."""
+    cl, cr = _util.random_tables(911, 300, 700, b"abcde ", 300, n_eq_values=40)
+    docs = [synth.rule_yaml([3, 4], []),
+            synth.rule_yaml([3], [(1, 0.62)]),
+            synth.rule_yaml([4], [(2, 0.58), (1, 0.52)])]
+    want = api.run_block(api.CTable(cl), api.CTable(cr), _oracle_plan(docs), 3)
+    for tile in (32, 64, 128):
+        c = hb.Context(0, tile_right=tile, eval_variant=variant)
+        for mode in MODES:
+            got, st = _engine_pairs(c, docs, cl, cr, 3, _util.INT_MAX, mode)
+            assert np.array_equal(got, want.pairs), (tile, mode)
+            assert st.pair_comparisons == want.pair_comparisons
+            assert st.fma_ambiguous == 0
+        c.close()
 
 
 def test_autotuner_choice_is_cached_and_exact(built, tmp_path, monkeypatch):
