@@ -135,7 +135,7 @@ void configure(hbx_session* S, uint32_t tile_right, int variant) {
   const dev::EvalKernel kern = dev::eval_kernel(S->variant);
   const size_t smem_cap = std::min<size_t>(C->smem_optin, 200 * 1024);
   const uint32_t cap_warp_words = (uint32_t)(smem_cap / 4 / dev::kWarpsPerCta) / 4 * 4;
-  S->wl = dev::warp_layout(S->tile_right);
+  S->wl = dev::warp_layout_fit(S->tile_right, smem_cap);
   S->warp_words = S->wl.warp_words;
   if (S->warp_words > cap_warp_words) fail(HBX_ERR_INVALID_ARG, "tile_right too large");
   // every warp region lies inside the dynamic allocation

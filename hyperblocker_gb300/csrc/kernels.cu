@@ -771,7 +771,8 @@ __device__ __forceinline__ bool scan_begin(Scan<W>& z, const uint32_t* tab, cons
   return true;
 }
 
-// One scan step of 4 symbols; every 16 symbols the pair stops once even
+// One scan step of 8 symbols (the row loads of all 8 in flight at once);
+// every 16 symbols the pair stops once even
 // matching every remaining symbol stays below its bound.  Returns true when
 // the pair is decided (*pass = the decision).
 template <int W>
@@ -782,15 +783,17 @@ __device__ __forceinline__ bool scan_step(Scan<W>& z, bool* pass, Counters* ctr,
     z.cur = z.nxt;
     if (z.i + 16u < z.n_iter) z.nxt = __ldg(reinterpret_cast<const uint4*>(z.b + z.i + 16u));
   }
-  const uint32_t wd = z.cur.x;
-  z.cur.x = z.cur.y;
-  z.cur.y = z.cur.z;
-  z.cur.z = z.cur.w;
+  const uint32_t wd = z.cur.x, wd2 = z.cur.y;
+  z.cur.x = z.cur.z;
+  z.cur.y = z.cur.w;
 #pragma unroll
   for (int c = 0; c < 4; c++)
     bp_step<W, S>(z.tab, (wd >> (8 * c)) & 0xffu, z.win, z.mt, (z.i + (uint32_t)c) < z.h ? 1u : 0u);
-  z.i += 4;
-  ops->steps++;
+#pragma unroll
+  for (int c = 0; c < 4; c++)
+    bp_step<W, S>(z.tab, (wd2 >> (8 * c)) & 0xffu, z.win, z.mt, (z.i + 4u + (uint32_t)c) < z.h ? 1u : 0u);
+  z.i += 8;
+  ops->steps += 2;
   if (z.i >= z.n_iter || (z.i & 15u) == 0) {
     uint32_t m = 0;
 #pragma unroll
@@ -858,13 +861,27 @@ __device__ __forceinline__ int advance(const EvalParams& P, uint32_t rule, uint3
 
 // Warp-uniform state of the evaluation loop kept in shared memory (every
 // lane reads it; every lane writes the same values, after a __syncwarp when
-// the values were read in the same step): the cached (rule, left key) with
-// its item range and blocks, the claim in each staging buffer, and the item
-// being filtered.
+// the values were read in the same step): the work items the warp has
+// claimed, the claim in each staging buffer, and the item being filtered.
+constexpr uint32_t kMaxClaimChunk = 16;
+// A claimed work item: the sources of its bulk copies (right-row metadata
+// from the block's first row, right rows from the 16-byte boundary at or
+// before it, the left string's metadata), left row, rule, rows, the shift of
+// the first row past the boundary, the rule's predicate count and first
+// threshold.
+struct ItemDesc {
+  const StrMeta* meta_src;
+  const uint32_t* rows_src;
+  const StrMeta* lm_src;
+  uint32_t lrow, rule, n, shift, n_sim;
+  float thr0;
+};
 struct WarpCtl {
-  unsigned long long k_lo, k_hi;  // item range of the cached (rule, left key)
-  uint32_t k_rule, k_key, k_nl, k_offl, k_offr, k_endr;  // its left count, block offsets
-  uint32_t c_rule[2], c_lrow[2], c_n[2], c_shift[2];  // claim per staging buffer (n = 0: none)
+  ItemDesc desc[kMaxClaimChunk];  // claimed items not yet staged
+  uint32_t c_rule[kMaxStageBufs], c_lrow[kMaxStageBufs];  // claim per staging buffer
+  uint32_t c_n[kMaxStageBufs], c_shift[kMaxStageBufs];    // (n = 0: none)
+  uint32_t c_more[kMaxStageBufs];
+  float c_thr[kMaxStageBufs];
   uint32_t i_rule, i_lrow, i_more, i_fast;  // the item being filtered
   float i_thr;
 };
@@ -1000,98 +1017,130 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
 }
 
 
-// Work positions a warp claims with one atomic: consecutive items mostly
-// share their (rule, left key), so the warp's key cache serves the rest.
-constexpr uint32_t kClaimChunk = 4;
+// Key of the item at position `local` of a rule's item space, searched in
+// [lo, hi): item_off[lo] <= local < item_off[hi].
+__device__ __forceinline__ uint32_t find_key_in(const unsigned long long* item_off, uint32_t lo,
+                                                uint32_t hi, unsigned long long local) {
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(item_off + mid) <= local)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+// Claims up to `chunk` consecutive work positions with one atomic and
+// computes their item descriptors into C->desc, one lane per item, so the
+// dependent loads of every item (rule fields included) overlap.  Within one rule, the first and
+// last lanes find their keys over the whole key space and the others search
+// only between those two.  Returns the count (0: the work list is exhausted).
+__device__ __forceinline__ uint32_t claim_chunk(const EvalParams& P, WarpCtl* C,
+                                                unsigned long long n_work, uint32_t chunk) {
+  const int lane = threadIdx.x & 31;
+  unsigned long long v0 = 0;
+  if (lane == 0) v0 = atomicAdd(&P.ctr->work_next, (unsigned long long)chunk);
+  v0 = __shfl_sync(kFull, v0, 0);
+  if (v0 >= n_work) return 0;
+  const uint32_t n = (uint32_t)min((unsigned long long)chunk, n_work - v0);
+  const uint32_t k = min((uint32_t)lane, n - 1);  // lanes past n repeat the last item
+  const unsigned long long v = v0 + k;
+  const unsigned long long it = P.n_seg ? seg_item(P, v) : v;
+  uint32_t r = 0;
+  while (r + 1 < P.n_rules && P.rule_item_base[r + 1] <= it) r++;
+  const Rule& R = P.rules[r];
+  const unsigned long long local = it - P.rule_item_base[r];
+  const uint32_t r_first = __shfl_sync(kFull, r, 0), r_last = __shfl_sync(kFull, r, n - 1);
+  uint32_t jl;  // left key (word class, join key)
+  if (r_first == r_last) {
+    uint32_t kb = 0;
+    if (k == 0 || k == n - 1) kb = find_key(R.item_off, R.domain_l, local);
+    const uint32_t k0 = __shfl_sync(kFull, kb, 0), k1 = __shfl_sync(kFull, kb, n - 1);
+    jl = find_key_in(R.item_off, k0, k1 + 1, local);
+  } else {
+    jl = find_key(R.item_off, R.domain_l, local);
+  }
+  const uint32_t key = jl % R.domain;  // join key
+  const unsigned long long in_key = local - R.item_off[jl];
+  const uint32_t nl = R.cnt_l[jl];
+  const uint32_t ri = (uint32_t)(in_key / nl);
+  const uint32_t li = (uint32_t)(in_key - (unsigned long long)ri * nl);
+  const uint32_t lrow = R.sorted_l[R.off_l[jl] + li];
+  const uint32_t offr = R.off_r[key];
+  const uint32_t rb0 = offr + ri * P.tile_right;
+  const uint32_t rb1 = min(rb0 + P.tile_right, offr + R.cnt_r[key]);
+  const uint32_t a0 = rb0 & ~3u;
+  ItemDesc d;
+  d.n_sim = R.n_sim;
+  d.meta_src = d.n_sim ? R.sorted_meta_r + rb0 : nullptr;
+  d.rows_src = R.sorted_r + a0;
+  d.lm_src = d.n_sim ? P.L.str_meta + (size_t)R.sim_l[0] * P.L.n_rows + lrow : nullptr;
+  d.lrow = lrow;
+  d.rule = r;
+  d.n = rb1 - rb0;
+  d.shift = rb0 - a0;
+  d.thr0 = d.n_sim ? R.thr[0] : 0.0f;
+  __syncwarp();  // earlier reads of the descriptors are done
+  if ((uint32_t)lane < n) C->desc[lane] = d;
+  __syncwarp();
+  return n;
+}
 
 // Claims the next work item whose rule has similarity predicates and starts
 // the bulk copies of its right rows, their metadata and its left string's
 // metadata into staging buffer b (completing on bar).  Items of rules with
-// equalities only are emitted on the spot.  Positions come from the warp's
-// chunk [*cv, *cv_end), refilled by one atomic.  Once the work list is
-// exhausted or the cycle budget has run out, *stop is set and this and every
-// later claim leave c_n[b] = 0.
+// equalities only are emitted on the spot.  Items come from the warp's
+// claimed descriptors C->desc[*d_pos, *d_n), refilled by claim_chunk.  Once
+// the work list is exhausted or the cycle budget has run out, *stop is set
+// and this and every later claim leave c_n[b] = 0.
 __device__ __forceinline__ void claim_item(const EvalParams& P, WarpCtl* C, uint32_t b,
                                            uint32_t* buf, uint64_t* bar, unsigned long long n_work,
-                                           long long t_start, bool* stop, unsigned long long* cv,
-                                           unsigned long long* cv_end, unsigned long long* done) {
+                                           uint32_t chunk, long long t_start, bool* stop,
+                                           uint32_t* d_pos, uint32_t* d_n,
+                                           unsigned long long* done) {
   const int lane = threadIdx.x & 31;
   while (!*stop) {
-    if (*cv >= *cv_end) {
-      unsigned long long v0 = 0;
-      if (lane == 0) v0 = atomicAdd(&P.ctr->work_next, (unsigned long long)kClaimChunk);
-      v0 = __shfl_sync(kFull, v0, 0);
-      if (v0 >= n_work) {
+    if (*d_pos >= *d_n) {
+      *d_n = claim_chunk(P, C, n_work, chunk);
+      *d_pos = 0;
+      if (*d_n == 0) {
         *stop = true;
         break;
       }
-      *cv = v0;
-      *cv_end = min(v0 + kClaimChunk, n_work);
     }
-    const unsigned long long v = (*cv)++;
     if (P.watchdog_cycles && (unsigned long long)(clock64() - t_start) > P.watchdog_cycles) {
       if (lane == 0) atomicAdd(&P.ctr->watchdog_trips, 1ull);
       *stop = true;
       break;
     }
-    const unsigned long long it = P.n_seg ? seg_item(P, v) : v;
-    uint32_t r = 0;
-    while (r + 1 < P.n_rules && P.rule_item_base[r + 1] <= it) r++;
-    const Rule& R = P.rules[r];
-    const unsigned long long local = it - P.rule_item_base[r];
-    unsigned long long lo = C->k_lo;
-    uint32_t nl = C->k_nl, offl = C->k_offl, offr = C->k_offr, endr = C->k_endr;
-    if (r != C->k_rule || local < lo || local >= C->k_hi) {
-      const uint32_t jl = find_key(R.item_off, R.domain_l, local);  // (word class, join key)
-      const uint32_t key = jl % R.domain;                           // join key
-      lo = R.item_off[jl];
-      const unsigned long long hi = R.item_off[jl + 1];
-      nl = R.cnt_l[jl];
-      offl = R.off_l[jl];
-      offr = R.off_r[key];
-      endr = offr + R.cnt_r[key];
-      __syncwarp();
-      C->k_rule = r;
-      C->k_key = jl;
-      C->k_lo = lo;
-      C->k_hi = hi;
-      C->k_nl = nl;
-      C->k_offl = offl;
-      C->k_offr = offr;
-      C->k_endr = endr;
-    }
-    const unsigned long long in_key = local - lo;
-    const uint32_t ri = (uint32_t)(in_key / nl);
-    const uint32_t li = (uint32_t)(in_key - (unsigned long long)ri * nl);
-    const uint32_t lrow = R.sorted_l[offl + li];
-    const uint32_t rb0 = offr + ri * P.tile_right;
-    const uint32_t rb1 = min(rb0 + P.tile_right, endr);
-    if (R.n_sim == 0) {  // equalities only: every candidate matches
-      for (uint32_t rb = rb0; rb < rb1; rb += 32) {
-        const uint32_t idx = rb + (uint32_t)lane;
-        const uint32_t rrow = idx < rb1 ? R.sorted_r[idx] : 0u;
-        emit(P, idx < rb1, lrow, rrow, lane);
+    const ItemDesc d = C->desc[(*d_pos)++];
+    if (d.n_sim == 0) {  // equalities only: every candidate matches
+      for (uint32_t e = 0; e < d.n; e += 32) {
+        const uint32_t k = e + (uint32_t)lane;
+        const uint32_t rrow = k < d.n ? d.rows_src[d.shift + k] : 0u;
+        emit(P, k < d.n, d.lrow, rrow, lane);
       }
       (*done)++;
       continue;
     }
-    const uint32_t a0 = rb0 & ~3u;
     if (lane == 0) {
-      const uint32_t mbytes = (rb1 - rb0) * (uint32_t)sizeof(StrMeta);
-      const uint32_t rbytes = ((rb1 - a0) * 4u + 15u) & ~15u;
-      const StrMeta* lm = P.L.str_meta + (size_t)R.sim_l[0] * P.L.n_rows + lrow;
+      const uint32_t mbytes = d.n * (uint32_t)sizeof(StrMeta);
+      const uint32_t rbytes = ((d.n + d.shift) * 4u + 15u) & ~15u;
       // earlier reads of this buffer are done (__syncwarp before the claim);
       // order them before the asynchronous writes
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       mbar_expect_tx(bar, mbytes + rbytes + (uint32_t)sizeof(StrMeta));
-      bulk_g2s(buf, R.sorted_meta_r + rb0, mbytes, bar);
-      bulk_g2s(buf + P.buf_rows_off, R.sorted_r + a0, rbytes, bar);
-      bulk_g2s(buf + P.buf_lmeta_off, lm, (uint32_t)sizeof(StrMeta), bar);
+      bulk_g2s(buf, d.meta_src, mbytes, bar);
+      bulk_g2s(buf + P.buf_rows_off, d.rows_src, rbytes, bar);
+      bulk_g2s(buf + P.buf_lmeta_off, d.lm_src, (uint32_t)sizeof(StrMeta), bar);
     }
-    C->c_rule[b] = r;
-    C->c_lrow[b] = lrow;
-    C->c_n[b] = rb1 - rb0;
-    C->c_shift[b] = rb0 - a0;
+    C->c_rule[b] = d.rule;
+    C->c_lrow[b] = d.lrow;
+    C->c_n[b] = d.n;
+    C->c_shift[b] = d.shift;
+    C->c_more[b] = d.n_sim > 1 ? 1u : 0u;
+    C->c_thr[b] = d.thr0;
     return;
   }
   C->c_n[b] = 0;
@@ -1116,17 +1165,17 @@ __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
   WarpCtl* C = reinterpret_cast<WarpCtl*>(region + P.ctl_off);
   uint64_t* bar0 = reinterpret_cast<uint64_t*>(region + P.mbar_off);
   const long long t_start = clock64();
-  if (lane == 0) {
-    C->k_rule = 0xffffffffu;
-    C->k_lo = 1ull;
-    C->k_hi = 0ull;
-  }
-  __syncwarp();
+  // work positions per claim: every warp gets about eight claims, at most
+  // kMaxClaimChunk items each
+  const unsigned long long n_warps = (unsigned long long)gridDim.x * kWarpsPerCta;
+  const uint32_t chunk =
+      (uint32_t)max(1ull, min((unsigned long long)kMaxClaimChunk, n_work / (n_warps * 8ull)));
   bool stop = false;
-  unsigned long long cv = 0, cv_end = 0;  // the warp's claimed work positions
-  claim_item(P, C, 0, region + P.buf_off0, bar0, n_work, t_start, &stop, &cv, &cv_end, done);
-  claim_item(P, C, 1, region + P.buf_off1, bar0 + 1, n_work, t_start, &stop, &cv, &cv_end, done);
-  uint32_t cb = 0;      // buffer of the current item (the other holds the next)
+  uint32_t d_pos = 0, d_n = 0;  // the warp's claimed descriptors not yet taken
+  for (uint32_t b = 0; b < P.n_bufs; b++)
+    claim_item(P, C, b, region + P.buf_off + b * P.buf_words, bar0 + b, n_work, chunk, t_start,
+               &stop, &d_pos, &d_n, done);
+  uint32_t cb = 0;      // buffer of the current item (buffer cb + k holds the k-th next)
   uint32_t phs = 0;     // bit b: mbarrier phase of buffer b
   bool active = false;  // current item waited for and being filtered
   uint32_t in_pos = 0, cur_n = C->c_n[0];
@@ -1149,7 +1198,7 @@ __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
     const uint32_t n_idle = __popc(idle);
     // refill the ring until it holds a pair for every idle lane
     while (tail - head < n_idle && tail - head <= kRing - 32) {
-      uint32_t* buf = region + (cb ? P.buf_off1 : P.buf_off0);
+      uint32_t* buf = region + P.buf_off + cb * P.buf_words;
       if (active) {
         if (in_pos < cur_n) {
           tail += filter_batch(P, C, reinterpret_cast<const StrMeta*>(buf + P.buf_lmeta_off),
@@ -1161,9 +1210,9 @@ __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
         // the item is filtered: its buffer takes the item after the next one
         active = false;
         __syncwarp();
-        claim_item(P, C, cb, buf, bar0 + cb, n_work, t_start, &stop, &cv, &cv_end, done);
-        cb ^= 1u;
-        buf = region + (cb ? P.buf_off1 : P.buf_off0);
+        claim_item(P, C, cb, buf, bar0 + cb, n_work, chunk, t_start, &stop, &d_pos, &d_n, done);
+        cb = cb + 1u == P.n_bufs ? 0u : cb + 1u;
+        buf = region + P.buf_off + cb * P.buf_words;
         cur_n = C->c_n[cb];
       }
       if (cur_n == 0) break;  // no work left (claims run in order)
@@ -1171,24 +1220,24 @@ __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
       phs ^= 1u << cb;
       if (!__all_sync(kFull, ok)) {
         // a copy never completed: report, wait once more (bounded) for it
-        // and for the other buffer's copies, stop
+        // and for the other buffers' copies, stop
         if (lane == 0) atomicAdd(&P.ctr->watchdog_trips, 1ull);
         mbar_wait(bar0 + cb, ((phs >> cb) & 1u) ^ 1u);
-        if (C->c_n[cb ^ 1u]) mbar_wait(bar0 + (cb ^ 1u), (phs >> (cb ^ 1u)) & 1u);
+        for (uint32_t b = 0; b < P.n_bufs; b++)
+          if (b != cb && C->c_n[b]) mbar_wait(bar0 + b, (phs >> b) & 1u);
         return;
       }
       active = true;
       in_pos = 0;
       (*done)++;
       const StrMeta* lm = reinterpret_cast<const StrMeta*>(buf + P.buf_lmeta_off);
-      const uint32_t ir = C->c_rule[cb];
-      const Rule& R = P.rules[ir];
-      const uint32_t il = C->c_lrow[cb];
+      const uint32_t ir = C->c_rule[cb], il = C->c_lrow[cb], more = C->c_more[cb];
+      const float thr = C->c_thr[cb];
       const uint32_t la = lm->loc.y;
       C->i_rule = ir;
       C->i_lrow = il;
-      C->i_thr = R.thr[0];
-      C->i_more = R.n_sim > 1 ? 1u : 0u;
+      C->i_thr = thr;
+      C->i_more = more;
       C->i_fast = has_table(P, la) ? 1u : 0u;
     }
     // idle lanes take the next queued pairs
@@ -1251,8 +1300,7 @@ __device__ __forceinline__ void eval_body(const EvalParams& P) {
   uint32_t* region = smem + (size_t)warp * P.warp_words;
   if (lane == 0) {
     uint64_t* bar = reinterpret_cast<uint64_t*>(region + P.mbar_off);
-    mbar_init(bar);
-    mbar_init(bar + 1);
+    for (uint32_t b = 0; b < P.n_bufs; b++) mbar_init(bar + b);
   }
   __syncwarp();
   unsigned long long n_work = 0;  // length of this launch's work list

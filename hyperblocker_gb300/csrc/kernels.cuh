@@ -159,30 +159,43 @@ inline PeqShape peq_shape(uint32_t max_len, uint32_t n_symbols) {
 }
 
 // Shared memory of one warp of k_eval, in 32-bit words: the ring of pairs
-// waiting for a scan (kRingEntries x kRingWords), two staging buffers (while
-// the warp filters one work item, the bulk copies of the next one fill the
-// other) and two mbarriers.  A staging buffer holds the item's right-row
+// waiting for a scan (kRingEntries x kRingWords), n_bufs staging buffers
+// (while the warp filters one work item, the bulk copies of the next
+// n_bufs - 1 fill the others) and one mbarrier per buffer.  A staging buffer holds the item's right-row
 // metadata (tile_right StrMeta records), its right rows (tile_right + 8: a
 // 16-byte-aligned copy starts up to 3 rows early and rounds up) and the
 // metadata of its left string.  Every offset is a multiple of 4 words (16
 // bytes) when tile_right is a multiple of 32.  A control block of
 // kWarpCtlWords words follows.
+constexpr uint32_t kMaxStageBufs = 4;
 struct WarpLayout {
-  uint32_t buf_off[2], buf_rows_off, buf_lmeta_off, mbar_off, ctl_off, warp_words;
+  uint32_t n_bufs, buf_off, buf_words, buf_rows_off, buf_lmeta_off, mbar_off, ctl_off, warp_words;
 };
-constexpr uint32_t kWarpCtlWords = 40;  // the warp's control block (kernels.cu: WarpCtl)
+constexpr uint32_t kWarpCtlWords = 224;  // the warp's control block (kernels.cu: WarpCtl)
 
-inline WarpLayout warp_layout(uint32_t tile_right) {
+inline WarpLayout warp_layout(uint32_t tile_right, uint32_t n_bufs) {
   WarpLayout w;
+  w.n_bufs = n_bufs < 2 ? 2 : (n_bufs > kMaxStageBufs ? kMaxStageBufs : n_bufs);
   const uint32_t meta_words = (uint32_t)(sizeof(StrMeta) / 4) * tile_right;
   w.buf_rows_off = meta_words;
   w.buf_lmeta_off = meta_words + (tile_right + 8 + 3) / 4 * 4;
-  const uint32_t buf_words = w.buf_lmeta_off + (uint32_t)(sizeof(StrMeta) / 4);
-  w.buf_off[0] = kRingWords * kRingEntries;
-  w.buf_off[1] = w.buf_off[0] + buf_words;
-  w.mbar_off = w.buf_off[1] + buf_words;
-  w.ctl_off = w.mbar_off + 4;
+  w.buf_words = w.buf_lmeta_off + (uint32_t)(sizeof(StrMeta) / 4);
+  w.buf_off = kRingWords * kRingEntries;
+  w.mbar_off = w.buf_off + w.n_bufs * w.buf_words;
+  w.ctl_off = w.mbar_off + (2 * w.n_bufs + 3) / 4 * 4;
   w.warp_words = w.ctl_off + kWarpCtlWords;
+  return w;
+}
+
+// The deepest staging (up to kMaxStageBufs buffers) that keeps two blocks of
+// kWarpsPerCta warps on an SM within smem_cap bytes of shared memory per
+// block; two buffers at least.
+inline WarpLayout warp_layout_fit(uint32_t tile_right, size_t smem_cap) {
+  WarpLayout w = warp_layout(tile_right, 2);
+  for (uint32_t n = kMaxStageBufs; n > 2; n--) {
+    const WarpLayout c = warp_layout(tile_right, n);
+    if ((size_t)c.warp_words * 4 * kWarpsPerCta * 2 <= smem_cap) return c;
+  }
   return w;
 }
 
@@ -220,7 +233,7 @@ struct EvalParams {
   unsigned long long seg_end[kMaxSegments];
   uint32_t tile_right;  // TR
   // shared-memory words per warp and offsets inside a warp's region (warp_layout)
-  uint32_t warp_words, buf_off0, buf_off1, buf_rows_off, buf_lmeta_off, mbar_off, ctl_off;
+  uint32_t warp_words, n_bufs, buf_off, buf_words, buf_rows_off, buf_lmeta_off, mbar_off, ctl_off;
   // Peq tables of the left strings (PeqShape): [left string slot][left row]
   const uint32_t* peq;
   uint32_t peq_w, tab_words, fast_max;
@@ -237,8 +250,9 @@ struct EvalParams {
 // Host: the shared-memory layout and Peq tables of a launch.
 inline void set_layout(EvalParams* P, const WarpLayout& w, const PeqShape& s, const uint32_t* peq) {
   P->warp_words = w.warp_words;
-  P->buf_off0 = w.buf_off[0];
-  P->buf_off1 = w.buf_off[1];
+  P->n_bufs = w.n_bufs;
+  P->buf_off = w.buf_off;
+  P->buf_words = w.buf_words;
   P->buf_rows_off = w.buf_rows_off;
   P->buf_lmeta_off = w.buf_lmeta_off;
   P->mbar_off = w.mbar_off;

@@ -517,7 +517,7 @@ void open_server(hbx_server* S, const hbx_plan* const* plans, int32_t n_plans, c
   const dev::EvalKernel kern = dev::eval_kernel(S->variant);
   const size_t smem_cap = std::min<size_t>(C->smem_optin, 200 * 1024);
   const uint32_t cap_warp_words = (uint32_t)(smem_cap / 4 / dev::kWarpsPerCta) / 4 * 4;
-  S->wl = dev::warp_layout(S->tile_right);
+  S->wl = dev::warp_layout_fit(S->tile_right, smem_cap);
   if (S->wl.warp_words > cap_warp_words) fail(HBX_ERR_INVALID_ARG, "tile_right too large");
   S->smem_bytes = (size_t)S->wl.warp_words * 4 * dev::kWarpsPerCta;
 

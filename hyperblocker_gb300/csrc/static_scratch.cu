@@ -186,7 +186,7 @@ void place(Carve& c, const hbx::Encoded& E, uint64_t capacity, size_t smem_cap, 
     Y->nb_l[r] = (d.domain_l + dev::kScanChunk - 1) / dev::kScanChunk;
     max_nb = std::max(max_nb, std::max(Y->nb[r], Y->nb_l[r]));
   }
-  Y->wl = dev::warp_layout(Y->tile_right);
+  Y->wl = dev::warp_layout_fit(Y->tile_right, smem_cap);
   if ((size_t)Y->wl.warp_words * 4 * dev::kWarpsPerCta > smem_cap)
     hbx::fail(HBX_ERR_INVALID_ARG, "tile_right too large");
   Y->shape = dev::peq_shape(max_len, E.n_symbols);
