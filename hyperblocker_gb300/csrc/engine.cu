@@ -66,6 +66,7 @@ struct hbx_session {
   hbx::DBuf<hbx::dev::Rule> d_rules;
   hbx::DBuf<unsigned long long> d_rule_base;
   hbx::DBuf<hbx::dev::Counters> d_ctr;
+  hbx::dev::Counters* h_ctr = nullptr;  // page-locked copy of d_ctr, written by each run
   hbx::DBuf<uint32_t> out_l, out_r;
   hbx::DBuf<unsigned long long> seen;  // reported-pair set (plans with several rules)
   // key histograms and scatter cursors of every rule, one block: one memset
@@ -91,6 +92,7 @@ struct hbx_session {
   hbx_stats stats{};
   ~hbx_session() {
     if (graph) cudaGraphExecDestroy(graph);
+    if (h_ctr) cudaFreeHost(h_ctr);
     for (cudaEvent_t e : {ev0, ev1, ev_eval0, ev_eval1})
       if (e) cudaEventDestroy(e);
   }
@@ -276,6 +278,7 @@ void setup_session(hbx_session* S, uint64_t h2d_tables) {
   S->d_rules.alloc(E.rules.size());
   S->d_rule_base.alloc(E.rules.size() + 1);
   S->d_ctr.alloc(1);
+  if (!S->h_ctr) HBX_CUDA(cudaHostAlloc(&S->h_ctr, sizeof(dev::Counters), cudaHostAllocPortable));
   const uint32_t tile = C->opts.tile_right > 0 ? (uint32_t)C->opts.tile_right : 64u;
   const int variant = C->opts.eval_variant > 0 ? C->opts.eval_variant - 1 : 1;
   configure(S, tile, variant);
@@ -416,6 +419,8 @@ uint32_t enqueue_batched(hbx_session* S, cudaStream_t st) {
   dev::eval_kernel(S->variant)<<<grid, kThreads, S->smem_bytes, st>>>(P);
   launch_check("k_eval");
   HBX_CUDA(cudaEventRecordWithFlags(S->ev_eval1, st, rec_flags));
+  // the counters travel back inside the run (a graph node when captured)
+  HBX_CUDA(cudaMemcpyAsync(S->h_ctr, S->d_ctr.p, sizeof(dev::Counters), cudaMemcpyDeviceToHost, st));
   return launches + 1;
 }
 
@@ -444,10 +449,9 @@ uint64_t needed_capacity(const hbx_session* S, const dev::Counters& c) {
 }
 
 dev::Counters read_counters(hbx_session* S, cudaStream_t st) {
-  dev::Counters c{};
-  HBX_CUDA(cudaMemcpyAsync(&c, S->d_ctr.p, sizeof c, cudaMemcpyDeviceToHost, st));
+  HBX_CUDA(cudaMemcpyAsync(S->h_ctr, S->d_ctr.p, sizeof(dev::Counters), cudaMemcpyDeviceToHost, st));
   HBX_CUDA(cudaStreamSynchronize(st));
-  return c;
+  return *S->h_ctr;
 }
 
 // One run into the session's own output buffers; returns the counters.
@@ -477,7 +481,8 @@ dev::Counters run_once(hbx_session* S, hbx_mode mode, cudaStream_t st, uint32_t*
     } else {
       *launches = enqueue_batched(S, st);
     }
-    return read_counters(S, st);
+    HBX_CUDA(cudaStreamSynchronize(st));
+    return *S->h_ctr;
   }
   // PLAIN: join, then one launch per (partition, rule)
   uint32_t n = enqueue_join(S, st);
