@@ -279,7 +279,7 @@ void setup_session(hbx_session* S, uint64_t h2d_tables) {
   S->d_rule_base.alloc(E.rules.size() + 1);
   S->d_ctr.alloc(1);
   if (!S->h_ctr) HBX_CUDA(cudaHostAlloc(&S->h_ctr, sizeof(dev::Counters), cudaHostAllocPortable));
-  const uint32_t tile = C->opts.tile_right > 0 ? (uint32_t)C->opts.tile_right : 64u;
+  const uint32_t tile = C->opts.tile_right > 0 ? (uint32_t)C->opts.tile_right : 128u;
   const int variant = C->opts.eval_variant > 0 ? C->opts.eval_variant - 1 : 1;
   configure(S, tile, variant);
 

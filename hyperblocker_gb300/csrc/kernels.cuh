@@ -175,7 +175,7 @@ constexpr uint32_t kWarpCtlWords = 224;  // the warp's control block (kernels.cu
 
 inline WarpLayout warp_layout(uint32_t tile_right, uint32_t n_bufs) {
   WarpLayout w;
-  w.n_bufs = n_bufs < 2 ? 2 : (n_bufs > kMaxStageBufs ? kMaxStageBufs : n_bufs);
+  w.n_bufs = n_bufs < 1 ? 1 : (n_bufs > kMaxStageBufs ? kMaxStageBufs : n_bufs);
   const uint32_t meta_words = (uint32_t)(sizeof(StrMeta) / 4) * tile_right;
   w.buf_rows_off = meta_words;
   w.buf_lmeta_off = meta_words + (tile_right + 8 + 3) / 4 * 4;
@@ -188,15 +188,15 @@ inline WarpLayout warp_layout(uint32_t tile_right, uint32_t n_bufs) {
 }
 
 // The deepest staging (up to kMaxStageBufs buffers) that keeps two blocks of
-// kWarpsPerCta warps on an SM within smem_cap bytes of shared memory per
-// block; two buffers at least.
+// kWarpsPerCta warps on an SM within smem_cap bytes of shared memory; one
+// buffer when none does (with one buffer the next item's copies start once
+// the current item is filtered, and other warps cover their latency).
 inline WarpLayout warp_layout_fit(uint32_t tile_right, size_t smem_cap) {
-  WarpLayout w = warp_layout(tile_right, 2);
-  for (uint32_t n = kMaxStageBufs; n > 2; n--) {
+  for (uint32_t n = kMaxStageBufs; n > 1; n--) {
     const WarpLayout c = warp_layout(tile_right, n);
     if ((size_t)c.warp_words * 4 * kWarpsPerCta * 2 <= smem_cap) return c;
   }
-  return w;
+  return warp_layout(tile_right, 1);
 }
 
 __host__ __device__ inline uint32_t word_class(uint32_t len) {

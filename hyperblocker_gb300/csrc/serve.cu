@@ -292,7 +292,7 @@ struct hbx_server {
   bool any_multi_rule = false;
   uint64_t resident_bytes = 0;
   // kernel configuration
-  uint32_t tile_right = 64;
+  uint32_t tile_right = 128;
   int variant = 1;
   dev::WarpLayout wl{};
   size_t smem_bytes = 0;
@@ -511,7 +511,7 @@ void open_server(hbx_server* S, const hbx_plan* const* plans, int32_t n_plans, c
   S->side_r = dev::Side{S->R.bucket.p, S->R.eq.p, S->R.comp.p, S->R.arena.p, S->R.meta.p, nR};
 
   // ---- kernel configuration
-  S->tile_right = S->opts.tile_right > 0 ? (uint32_t)S->opts.tile_right : 64u;
+  S->tile_right = S->opts.tile_right > 0 ? (uint32_t)S->opts.tile_right : 128u;
   S->tile_right = std::min<uint32_t>(512, std::max<uint32_t>(32, (S->tile_right + 31) / 32 * 32));
   S->variant = S->opts.eval_variant == 1 ? 0 : 1;
   const dev::EvalKernel kern = dev::eval_kernel(S->variant);

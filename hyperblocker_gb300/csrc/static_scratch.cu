@@ -123,7 +123,7 @@ struct Layout {
   hbx::dev::WarpLayout wl{};
   hbx::dev::PeqShape shape{};
   uint32_t* peq = nullptr;
-  uint32_t tile_right = 64;
+  uint32_t tile_right = 128;
 };
 
 // Places every buffer; with c.base == nullptr it only measures.
