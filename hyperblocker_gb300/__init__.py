@@ -136,6 +136,8 @@ SIGNATURES = {
     "hbx_block": (ctypes.c_int, [_VP, _VP, _VP, _VP, ctypes.c_uint64, ctypes.c_int64, ctypes.c_int,
                                  ctypes.POINTER(Pairs), ctypes.POINTER(Stats)]),
     "hbx_write_pairs": (ctypes.c_int, [_VP, _VP, _VP, _VP, _VP, ctypes.c_uint64, ctypes.c_char_p]),
+    "hbx_write_pairs_device": (ctypes.c_int, [_VP, _VP, _VP, _VP, _VP, ctypes.c_uint64,
+                                              ctypes.c_char_p]),
     "hbx_run_cli": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_char_p)]),
     "hbx_block_static": (ctypes.c_int, [ctypes.c_int, _VP, _VP, _VP, ctypes.c_uint64,
                                         ctypes.c_int64, ctypes.POINTER(Pairs), _VP,
@@ -501,6 +503,14 @@ def write_pairs(left: Table, right: Table, pairs: np.ndarray, path: str,
     c = ctx.h if ctx else None
     _check(lib().hbx_write_pairs(c, left.h, right.h, l.ctypes.data, r.ctypes.data, len(pairs),
                                  path.encode()), c)
+
+
+def write_pairs_device(ctx: Context, left: Table, right: Table, l_row_ptr: int, r_row_ptr: int,
+                       n: int, path: str) -> None:
+    """Appends the id lines of n pairs held in DEVICE memory (two uint32
+    arrays given by address), formatted on the device."""
+    _check(lib().hbx_write_pairs_device(ctx.h, left.h, right.h, l_row_ptr, r_row_ptr, n,
+                                        path.encode()), ctx.h)
 
 
 def run_cli(argv: Sequence[str]) -> int:

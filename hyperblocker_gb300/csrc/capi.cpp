@@ -29,6 +29,12 @@ extern "C" const char* hbx_last_error(const hbx_ctx* ctx);
 // this accessor, which engine.cu does not need.
 struct hbx_ctx;
 extern "C" void hbx_internal_set_error(hbx_ctx* ctx, const char* msg);
+// writer.cu: the same lines formatted on the device
+extern "C" hbx_status hbx_internal_write_pairs_via_device(hbx_ctx* ctx, const hbx_table* left,
+                                                          const hbx_table* right,
+                                                          const uint32_t* l_row,
+                                                          const uint32_t* r_row, uint64_t n,
+                                                          const char* path);
 
 namespace {
 
@@ -151,6 +157,10 @@ hbx_status hbx_write_pairs(hbx_ctx* ctx, const hbx_table* left, const hbx_table*
                            const uint32_t* l_row, const uint32_t* r_row, uint64_t n,
                            const char* path) {
   if (!left || !right || !path || (n && (!l_row || !r_row))) return HBX_ERR_INVALID_ARG;
+  // with a context, many pairs are formatted on its device
+  constexpr uint64_t kDeviceMin = 1 << 16;
+  if (ctx && n >= kDeviceMin)
+    return hbx_internal_write_pairs_via_device(ctx, left, right, l_row, r_row, n, path);
   return guard_host(ctx, [&] {
     if (left->t.n_cols() == 0 || right->t.n_cols() == 0)
       hbx::fail(HBX_ERR_INVALID_ARG, "table without an id column");

@@ -173,10 +173,20 @@ hbx_status hbx_block(hbx_ctx* ctx, const hbx_plan* plan, const hbx_table* left,
                      hbx_mode mode, hbx_pairs* out, hbx_stats* stats);
 
 /* Appends "<id_l>,<id_r>\n" lines (column 0 of each table), like
- * host_reducer.h:80-90.  Pairs are written in the order given. */
+ * host_reducer.h:80-90.  Pairs are written in the order given.  With a
+ * context and at least 65,536 pairs the lines are formatted on its device
+ * (hbx_write_pairs_device); the bytes are the same. */
 hbx_status hbx_write_pairs(hbx_ctx* ctx, const hbx_table* left, const hbx_table* right,
                            const uint32_t* l_row, const uint32_t* r_row, uint64_t n,
                            const char* path);
+
+/* hbx_write_pairs for pairs in DEVICE memory (l_row, r_row: device arrays of
+ * n rows), formatted on the device: the same bytes as hbx_write_pairs, in
+ * chunks of at most 64 MiB of text, each appended to path while the next is
+ * formatted (replaces host_reducer.h:80-90 for large outputs). */
+hbx_status hbx_write_pairs_device(hbx_ctx* ctx, const hbx_table* left, const hbx_table* right,
+                                  const uint32_t* l_row, const uint32_t* r_row, uint64_t n,
+                                  const char* path);
 
 /* hbx_block for tables whose encoding need not fit the device at once (the
  * reference's per-partition pipeline, host_producer.h:75-104, with a memory
