@@ -127,6 +127,7 @@ SIGNATURES = {
     "hbx_table_ingest": (ctypes.c_int, [_VP, ctypes.POINTER(Columns), ctypes.POINTER(_VP)]),
     "hbx_table_n_rows": (ctypes.c_int64, [_VP]),
     "hbx_table_n_cols": (ctypes.c_int32, [_VP]),
+    "hbx_table_column": (ctypes.c_int, [_VP, ctypes.c_int32, ctypes.POINTER(_VP), ctypes.POINTER(_VP)]),
     "hbx_table_destroy": (ctypes.c_int, [_VP]),
     "hbx_session_create": (ctypes.c_int, [_VP, _VP, _VP, _VP, ctypes.c_uint64, ctypes.c_int64,
                                           ctypes.POINTER(_VP)]),
@@ -282,6 +283,18 @@ class Table:
     @property
     def n_cols(self) -> int:
         return lib().hbx_table_n_cols(self.h)
+
+    def column(self, c: int):
+        """Column c as parsed: (cell bytes back to back as uint8, int64
+        offsets of n_rows + 1), copies."""
+        b, o = _VP(), _VP()
+        _check(lib().hbx_table_column(self.h, c, ctypes.byref(b), ctypes.byref(o)), None)
+        n = self.n_rows
+        off = np.ctypeslib.as_array(ctypes.cast(o, ctypes.POINTER(ctypes.c_int64)), (n + 1,)).copy()
+        nb = int(off[-1])
+        data = (np.ctypeslib.as_array(ctypes.cast(b, ctypes.POINTER(ctypes.c_uint8)), (nb,)).copy()
+                if nb else np.zeros(0, np.uint8))
+        return data, off
 
     def __del__(self):
         if getattr(self, "h", None):

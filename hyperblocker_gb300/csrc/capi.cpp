@@ -128,7 +128,7 @@ hbx_status hbx_table_from_csv(hbx_ctx* ctx, const char* path, char sep, hbx_tabl
   *out = nullptr;
   auto t = std::make_unique<hbx_table>();
   t->uid = hbx::next_table_uid();
-  hbx_status s = guard_host(ctx, [&] { t->t = hbx::table_from_csv(path, sep ? sep : ','); });
+  hbx_status s = guard_host(ctx, [&] { t->t = hbx::table_from_csv(path, sep ? sep : ',', ctx); });
   if (s == HBX_OK) *out = t.release();
   return s;
 }
@@ -145,6 +145,15 @@ hbx_status hbx_table_ingest(hbx_ctx* ctx, const hbx_columns* cols, hbx_table** o
 
 int64_t hbx_table_n_rows(const hbx_table* t) { return t ? t->t.n_rows : -1; }
 int32_t hbx_table_n_cols(const hbx_table* t) { return t ? t->t.n_cols() : -1; }
+
+hbx_status hbx_table_column(const hbx_table* t, int32_t c, const char** bytes,
+                            const int64_t** offsets) {
+  if (!t || !bytes || !offsets || c < 0 || c >= t->t.n_cols()) return HBX_ERR_INVALID_ARG;
+  const hbx::Column& col = t->t.cols[(size_t)c];
+  *bytes = col.bytes.data();
+  *offsets = col.off.data();
+  return HBX_OK;
+}
 
 hbx_status hbx_table_destroy(hbx_table* t) {
   if (!t) return HBX_ERR_INVALID_ARG;

@@ -114,11 +114,33 @@ Table table_from_buffer(const char* data, size_t n, char sep) {
   return t;
 }
 
-Table table_from_csv(const std::string& path, char sep) {
-  std::ifstream f(path, std::ios::binary);
-  if (!f) fail(HBX_ERR_IO, "cannot open " + path);
-  std::vector<char> buf((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+Table table_from_csv(const std::string& path, char sep, hbx_ctx* ctx) {
+  std::vector<char> buf;
+  {
+    FILE* f = std::fopen(path.c_str(), "rb");
+    if (!f) fail(HBX_ERR_IO, "cannot open " + path);
+    // one read of the whole file (grown if the file grows meanwhile)
+    std::fseek(f, 0, SEEK_END);
+    const long size = std::ftell(f);
+    std::fseek(f, 0, SEEK_SET);
+    buf.resize(size > 0 ? (size_t)size : 0);
+    size_t got = buf.empty() ? 0 : std::fread(buf.data(), 1, buf.size(), f);
+    for (char tmp[65536];;) {
+      const size_t k = std::fread(tmp, 1, sizeof tmp, f);
+      if (k == 0) break;
+      buf.insert(buf.begin() + (long)got, tmp, tmp + k);
+      got += k;
+    }
+    const bool err = std::ferror(f) != 0;
+    std::fclose(f);
+    if (err) fail(HBX_ERR_IO, "cannot read " + path);
+    buf.resize(got);
+  }
   try {
+    if (ctx && buf.size() >= kDeviceCsvMin) {
+      Table t;
+      if (table_from_buffer_device(ctx, buf.data(), buf.size(), sep, &t)) return t;
+    }
     return table_from_buffer(buf.data(), buf.size(), sep);
   } catch (const Error& e) {
     fail(e.status, path + ": " + e.what());

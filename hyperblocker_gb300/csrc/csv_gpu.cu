@@ -1,0 +1,310 @@
+// csv_gpu.cu -- the CSV tokenization of csv.cpp (rapidcsv 8.x with the
+// reference's parameters, core/components/data_mngr.h:48-51) on the device.
+//
+// A line break always ends a row (no quoted line breaks), so rows are the
+// spans between '\n' bytes and tokenize independently: one thread per row
+// walks its bytes with the host loop's state machine (a '"' toggles the quote
+// state when it is the first kept byte of the cell or the cell began with
+// '"'; the separator ends a cell outside quotes; '\r' is dropped), first to
+// measure every cell after unquoting ("..." -> ..., "" -> "), then, after a
+// scan of the lengths per column, to write the cells into column-major
+// arenas.  The table is then copied back into host columns, byte for byte
+// what table_from_buffer builds.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "context.h"
+#include "device_buffers.h"
+#include "hbx_core.h"
+#include "ingest.h"
+
+namespace hbx {
+namespace csvd {
+
+constexpr uint32_t kChunk = 64;  // bytes per thread when finding line breaks
+
+// Line breaks per 64-byte chunk of the buffer.
+__global__ void k_nl_count(const uint8_t* buf, uint64_t n, uint32_t n_chunks, uint32_t* cnt) {
+  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < n_chunks; c += gridDim.x * blockDim.x) {
+    const uint64_t a = (uint64_t)c * kChunk, b = min(a + kChunk, n);
+    uint32_t k = 0;
+    for (uint64_t i = a; i < b; i++) k += buf[i] == '\n';
+    cnt[c] = k;
+  }
+}
+
+// Positions of the line breaks, in order.
+__global__ void k_nl_write(const uint8_t* buf, uint64_t n, uint32_t n_chunks, const uint32_t* off,
+                           uint64_t* pos) {
+  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < n_chunks; c += gridDim.x * blockDim.x) {
+    const uint64_t a = (uint64_t)c * kChunk, b = min(a + kChunk, n);
+    uint32_t k = off[c];
+    for (uint64_t i = a; i < b; i++)
+      if (buf[i] == '\n') pos[k++] = i;
+  }
+}
+
+// The cells of one row [s, e), '\r' bytes dropped, in the host loop's order.
+// For every cell up to n_cols: visit(cell index, first byte, end) with the
+// cell's raw span (still holding '\r' bytes).  Returns the cell count.
+template <class F>
+__device__ __forceinline__ uint32_t for_cells(const uint8_t* buf, uint64_t s, uint64_t e,
+                                              uint8_t sep, F&& visit) {
+  uint32_t c = 0;
+  uint64_t cs = s;
+  bool quoted = false, empty = true, first_quote = false;
+  for (uint64_t i = s; i < e; i++) {
+    const uint8_t ch = buf[i];
+    if (ch == '"') {
+      if (empty || first_quote) quoted = !quoted;
+      if (empty) first_quote = true;
+      empty = false;
+    } else if (ch == sep) {
+      if (!quoted) {
+        visit(c++, cs, i);
+        cs = i + 1;
+        empty = true;
+        first_quote = false;
+      } else {
+        empty = false;
+      }
+    } else if (ch == '\r') {
+      // dropped
+    } else {
+      empty = false;
+    }
+  }
+  visit(c++, cs, e);
+  return c;
+}
+
+// Kept (non-'\r') bytes of a raw cell: count, first and last.
+__device__ __forceinline__ void kept(const uint8_t* buf, uint64_t a, uint64_t b, uint32_t* n,
+                                     uint8_t* first, uint8_t* last) {
+  uint32_t k = 0;
+  uint8_t f = 0, l = 0;
+  for (uint64_t i = a; i < b; i++) {
+    const uint8_t ch = buf[i];
+    if (ch == '\r') continue;
+    if (k == 0) f = ch;
+    l = ch;
+    k++;
+  }
+  *n = k;
+  *first = f;
+  *last = l;
+}
+
+// Unquoted bytes of a raw cell (csv.cpp push_cell): when its kept bytes are
+// "...", the interior with "" read as "; else the kept bytes.  out == null:
+// only count.
+__device__ __forceinline__ uint32_t unquote(const uint8_t* buf, uint64_t a, uint64_t b,
+                                            uint8_t* out) {
+  uint32_t n;
+  uint8_t f, l;
+  kept(buf, a, b, &n, &f, &l);
+  uint32_t w = 0;
+  if (n >= 2 && f == '"' && l == '"') {
+    // kept index j runs 1 .. n-2; a '"' followed by '"' with j + 2 < n
+    // swallows the second
+    uint32_t j = 0;
+    bool skip = false;
+    for (uint64_t i = a; i < b; i++) {
+      const uint8_t ch = buf[i];
+      if (ch == '\r') continue;
+      const uint32_t jj = j++;
+      if (jj == 0 || jj + 1 >= n) continue;  // the enclosing quotes
+      if (skip) {
+        skip = false;
+        continue;
+      }
+      if (out) out[w] = ch;
+      w++;
+      if (ch == '"' && jj + 2 < n) {
+        // look at the next kept byte
+        uint64_t k = i + 1;
+        while (k < b && buf[k] == '\r') k++;
+        if (k < b && buf[k] == '"') skip = true;
+      }
+    }
+  } else {
+    for (uint64_t i = a; i < b; i++) {
+      const uint8_t ch = buf[i];
+      if (ch == '\r') continue;
+      if (out) out[w] = ch;
+      w++;
+    }
+  }
+  return w;
+}
+
+struct Rows {
+  const uint64_t* nl;  // line-break positions
+  uint64_t n_nl;
+  uint64_t start;      // first byte of row 0 (after a BOM)
+  uint64_t end;        // end of the buffer
+  uint64_t n_rows;     // n_nl, plus one when bytes other than '\r' follow the last break
+};
+
+__device__ __forceinline__ void row_span(const Rows& R, uint64_t r, uint64_t* s, uint64_t* e) {
+  *s = r == 0 ? R.start : R.nl[r - 1] + 1;
+  *e = r < R.n_nl ? R.nl[r] : R.end;
+}
+
+// Pass 1: unquoted length of every cell [col][row]; rows with fewer cells
+// than n_cols report (row << 32 | cells) into *short_row (smallest wins).
+__global__ void k_measure(const uint8_t* buf, Rows R, uint8_t sep, uint32_t n_cols, uint32_t* len,
+                          unsigned long long* short_row) {
+  for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < R.n_rows;
+       r += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t s, e;
+    row_span(R, r, &s, &e);
+    const uint32_t cells = for_cells(buf, s, e, sep, [&](uint32_t c, uint64_t a, uint64_t b) {
+      if (c < n_cols) len[(uint64_t)c * R.n_rows + r] = unquote(buf, a, b, nullptr);
+    });
+    if (cells < n_cols) {
+      for (uint32_t c = cells; c < n_cols; c++) len[(uint64_t)c * R.n_rows + r] = 0;
+      atomicMin(short_row, ((unsigned long long)r << 32) | cells);
+    }
+  }
+}
+
+// Pass 2: the cells into their columns' arenas.
+__global__ void k_write(const uint8_t* buf, Rows R, uint8_t sep, uint32_t n_cols,
+                        const uint32_t* off, uint8_t* const* arena) {
+  for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < R.n_rows;
+       r += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t s, e;
+    row_span(R, r, &s, &e);
+    for_cells(buf, s, e, sep, [&](uint32_t c, uint64_t a, uint64_t b) {
+      if (c < n_cols) unquote(buf, a, b, arena[c] + off[(uint64_t)c * R.n_rows + r]);
+    });
+  }
+}
+
+// Exclusive u32 offsets of one column (plus its total) as int64.
+__global__ void k_widen(const uint32_t* off, const uint32_t* len, uint64_t n, int64_t* out) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i <= n;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    out[i] = i < n ? (int64_t)off[i] : (n ? (int64_t)off[n - 1] + len[n - 1] : 0);
+}
+
+}  // namespace csvd
+
+bool table_from_buffer_device(hbx_ctx* C, const char* data, size_t n, char sep, Table* out) {
+  // the same BOM rule and row count as the host loop; the header row's cell
+  // count, on the host
+  size_t skip = 0;
+  if (n >= 3 && (unsigned char)data[0] == 0xEF && (unsigned char)data[1] == 0xBB &&
+      (unsigned char)data[2] == 0xBF)
+    skip = 3;
+  const char* p = data + skip;
+  const size_t m = n - skip;
+  const char* first_nl = (const char*)std::memchr(p, '\n', m);
+  const size_t first_end = first_nl ? (size_t)(first_nl - p) : m;
+  // cells of row 0 by the host tokenizer itself
+  const Table head = table_from_buffer(p, first_end, sep);
+  const uint32_t n_cols = (uint32_t)head.n_cols();
+  if (n_cols == 0 || m > (1ull << 40)) return false;
+  HBX_CUDA(cudaSetDevice(C->device));
+  cudaStream_t st = C->stream;
+  PoolScope scope(C->pool, st);
+  DBuf<uint8_t> buf;
+  buf.alloc(std::max<size_t>(m, 16));
+  HBX_CUDA(cudaMemcpyAsync(buf.p, p, m, cudaMemcpyHostToDevice, st));
+  const uint64_t n_chunks64 = (m + csvd::kChunk - 1) / csvd::kChunk;
+  if (n_chunks64 >= (1ull << 32)) return false;
+  const uint32_t n_chunks = (uint32_t)std::max<uint64_t>(n_chunks64, 1);
+  DBuf<uint32_t> cnt, coff;
+  cnt.alloc(n_chunks);
+  coff.alloc(n_chunks);
+  HBX_CUDA(cudaMemsetAsync(cnt.p, 0, (size_t)n_chunks * 4, st));
+  const int g = grid_for(n_chunks, C->n_sm);
+  csvd::k_nl_count<<<g, 256, 0, st>>>(buf.p, m, n_chunks, cnt.p);
+  scan_u32(cnt.p, n_chunks, coff.p, st);
+  DBuf<unsigned long long> tot;
+  tot.alloc(1);
+  ing::k_scan_total<<<1, 1, 0, st>>>(coff.p, cnt.p, n_chunks, 0ull, tot.p);
+  unsigned long long n_nl = 0;
+  HBX_CUDA(cudaMemcpyAsync(&n_nl, tot.p, 8, cudaMemcpyDeviceToHost, st));
+  HBX_CUDA(cudaStreamSynchronize(st));
+  DBuf<uint64_t> nl;
+  nl.alloc(std::max<uint64_t>(n_nl, 1));
+  csvd::k_nl_write<<<g, 256, 0, st>>>(buf.p, m, n_chunks, coff.p, nl.p);
+  // a last row without a line break when any byte other than '\r' follows
+  // the last one
+  const char* last_nl = (const char*)memrchr(p, '\n', m);
+  const size_t tail = last_nl ? (size_t)(last_nl - p) + 1 : 0;
+  bool tail_row = false;
+  for (size_t i = tail; i < m && !tail_row; i++) tail_row = p[i] != '\r';
+  csvd::Rows R{nl.p, n_nl, 0, m, n_nl + (tail_row ? 1u : 0u)};
+  const uint64_t rows = R.n_rows;
+  if (rows == 0 || rows >= (1ull << 31)) return false;
+  DBuf<uint32_t> len, off;
+  len.alloc((size_t)n_cols * rows);
+  off.alloc((size_t)n_cols * rows);
+  DBuf<unsigned long long> short_row;
+  short_row.alloc(1);
+  HBX_CUDA(cudaMemsetAsync(short_row.p, 0xff, 8, st));
+  const int gr = grid_for(rows, C->n_sm);
+  csvd::k_measure<<<gr, 256, 0, st>>>(buf.p, R, (uint8_t)sep, n_cols, len.p, short_row.p);
+  check_launch("csv measure");
+  // per column: exclusive offsets and total bytes
+  std::vector<unsigned long long> totals(n_cols);
+  DBuf<unsigned long long> dtot;
+  dtot.alloc(n_cols);
+  for (uint32_t c = 0; c < n_cols; c++) {
+    scan_u32(len.p + (size_t)c * rows, (uint32_t)rows, off.p + (size_t)c * rows, st);
+    ing::k_scan_total<<<1, 1, 0, st>>>(off.p + (size_t)c * rows, len.p + (size_t)c * rows,
+                                        (uint32_t)rows, 0ull, dtot.p + c);
+  }
+  unsigned long long bad = 0;
+  HBX_CUDA(cudaMemcpyAsync(totals.data(), dtot.p, 8ull * n_cols, cudaMemcpyDeviceToHost, st));
+  HBX_CUDA(cudaMemcpyAsync(&bad, short_row.p, 8, cudaMemcpyDeviceToHost, st));
+  HBX_CUDA(cudaStreamSynchronize(st));
+  if (bad != ~0ull) {
+    char msg[160];
+    std::snprintf(msg, sizeof msg, "row %lld has %d cells, expected %d", (long long)(bad >> 32),
+                  (int)(bad & 0xffffffffu), (int)n_cols);
+    fail(HBX_ERR_PARSE, msg);
+  }
+  // a column over 4 GiB would overflow the u32 offsets: the host loop then
+  for (unsigned long long t : totals)
+    if (t >= (1ull << 32)) return false;
+  std::vector<DBuf<uint8_t>> arenas(n_cols);
+  std::vector<uint8_t*> arena_ptr(n_cols);
+  for (uint32_t c = 0; c < n_cols; c++) {
+    arenas[c].alloc(std::max<uint64_t>(totals[c], 16));
+    arena_ptr[c] = arenas[c].p;
+  }
+  DBuf<uint8_t*> d_arena;
+  d_arena.upload(arena_ptr, st);
+  csvd::k_write<<<gr, 256, 0, st>>>(buf.p, R, (uint8_t)sep, n_cols, off.p, d_arena.p);
+  check_launch("csv write");
+  DBuf<int64_t> off64;
+  off64.alloc(rows + 1);
+  Table t;
+  t.n_rows = (int64_t)rows;
+  t.cols.resize(n_cols);
+  for (uint32_t c = 0; c < n_cols; c++) {
+    Column& col = t.cols[c];
+    col.bytes.resize(totals[c]);
+    col.off.resize(rows + 1);
+    csvd::k_widen<<<grid_for(rows + 1, C->n_sm), 256, 0, st>>>(
+        off.p + (size_t)c * rows, len.p + (size_t)c * rows, rows, off64.p);
+    if (totals[c])
+      HBX_CUDA(cudaMemcpyAsync(col.bytes.data(), arenas[c].p, totals[c], cudaMemcpyDeviceToHost, st));
+    HBX_CUDA(cudaMemcpyAsync(col.off.data(), off64.p, (rows + 1) * 8, cudaMemcpyDeviceToHost, st));
+    HBX_CUDA(cudaStreamSynchronize(st));  // off64 is reused by the next column
+  }
+  check_launch("csv columns");
+  finish_table(&t);
+  *out = std::move(t);
+  return true;
+}
+
+}  // namespace hbx

@@ -81,7 +81,15 @@ Plan plan_from_docs(const std::vector<std::pair<std::string, std::string>>& name
 Plan plan_from_dir(const std::string& dir);
 
 // csv.cpp
-Table table_from_csv(const std::string& path, char sep);
+// The reference's tokenization of a CSV buffer (csv.cpp).
+Table table_from_buffer(const char* data, size_t n, char sep);
+// With a context and at least kDeviceCsvMin bytes the file is tokenized on
+// the context's device (csv_gpu.cu), into the same table.
+Table table_from_csv(const std::string& path, char sep, hbx_ctx* ctx = nullptr);
+constexpr size_t kDeviceCsvMin = 1u << 20;
+// table_from_buffer on the device; false when the input needs the host loop
+// (a first line without cells, a column of 4 GiB or more, 2^31 rows or more).
+bool table_from_buffer_device(hbx_ctx* ctx, const char* data, size_t n, char sep, Table* out);
 Table table_from_columns(const hbx_columns* cols);
 
 // Measured-selectivity ordering of similarity predicates (planner.cpp).

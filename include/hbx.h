@@ -149,6 +149,11 @@ hbx_status hbx_table_from_csv(hbx_ctx* ctx, const char* path, char sep, hbx_tabl
 hbx_status hbx_table_ingest(hbx_ctx* ctx, const hbx_columns* cols, hbx_table** out);
 int64_t hbx_table_n_rows(const hbx_table* t);
 int32_t hbx_table_n_cols(const hbx_table* t);
+/* Column c of a table as parsed: *bytes holds the cells back to back, cell i
+ * is bytes[offsets[i] .. offsets[i + 1]) (n_rows + 1 offsets); the pointers
+ * stay valid until the table is destroyed. */
+hbx_status hbx_table_column(const hbx_table* t, int32_t c, const char** bytes,
+                            const int64_t** offsets);
 hbx_status hbx_table_destroy(hbx_table* t);
 
 /* ---- blocking ------------------------------------------------------------ */
