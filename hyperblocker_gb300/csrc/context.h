@@ -15,4 +15,6 @@ struct hbx_ctx {
   cudaMemPool_t pool = nullptr;  // device memory of this context's sessions and servers
   hbx_opts opts{};
   std::string err;
+  std::string device_name;  // keys the autotuner's cache
+  void* h_ctr = nullptr;    // page-locked counters of the context's session runs
 };

@@ -66,7 +66,7 @@ struct hbx_session {
   hbx::DBuf<hbx::dev::Rule> d_rules;
   hbx::DBuf<unsigned long long> d_rule_base;
   hbx::DBuf<hbx::dev::Counters> d_ctr;
-  hbx::dev::Counters* h_ctr = nullptr;  // page-locked copy of d_ctr, written by each run
+  hbx::dev::Counters* h_ctr = nullptr;  // page-locked copy of d_ctr (the context's), written by each run
   hbx::DBuf<uint32_t> out_l, out_r;
   hbx::DBuf<unsigned long long> seen;  // reported-pair set (plans with several rules)
   // key histograms and scatter cursors of every rule, one block: one memset
@@ -92,7 +92,6 @@ struct hbx_session {
   hbx_stats stats{};
   ~hbx_session() {
     if (graph) cudaGraphExecDestroy(graph);
-    if (h_ctr) cudaFreeHost(h_ctr);
     for (cudaEvent_t e : {ev0, ev1, ev_eval0, ev_eval1})
       if (e) cudaEventDestroy(e);
   }
@@ -278,7 +277,9 @@ void setup_session(hbx_session* S, uint64_t h2d_tables) {
   S->d_rules.alloc(E.rules.size());
   S->d_rule_base.alloc(E.rules.size() + 1);
   S->d_ctr.alloc(1);
-  if (!S->h_ctr) HBX_CUDA(cudaHostAlloc(&S->h_ctr, sizeof(dev::Counters), cudaHostAllocPortable));
+  // one page-locked counter block per context: its sessions run one at a time
+  if (!C->h_ctr) HBX_CUDA(cudaHostAlloc(&C->h_ctr, sizeof(dev::Counters), cudaHostAllocPortable));
+  S->h_ctr = static_cast<dev::Counters*>(C->h_ctr);
   const uint32_t tile = C->opts.tile_right > 0 ? (uint32_t)C->opts.tile_right : 128u;
   const int variant = C->opts.eval_variant > 0 ? C->opts.eval_variant - 1 : 1;
   configure(S, tile, variant);
@@ -548,9 +549,7 @@ std::string autotune_path() {
 }
 
 std::string workload_signature(const hbx_session* S) {
-  cudaDeviceProp prop;
-  std::string sig;
-  if (cudaGetDeviceProperties(&prop, S->ctx->device) == cudaSuccess) sig = prop.name;
+  std::string sig = S->ctx->device_name;
   sig += "|k2";  // evaluation kernel generation: entries of earlier kernels do not apply
   auto bucket = [](uint64_t n) {  // power-of-two bucket
     uint32_t b = 0;
@@ -650,8 +649,9 @@ void autotune(hbx_session* S, cudaStream_t st) {
     int v = 0;
     float ms = 0;
     if (std::sscanf(hit->second.c_str(), "%u, %d, %f", &tr, &v, &ms) == 3 && tr >= 32) {
-      configure(S, o.tile_right > 0 ? (uint32_t)o.tile_right : tr,
-                o.eval_variant > 0 ? o.eval_variant - 1 : v);
+      const uint32_t want_tr = o.tile_right > 0 ? (uint32_t)o.tile_right : tr;
+      const int want_v = o.eval_variant > 0 ? o.eval_variant - 1 : v;
+      if (want_tr != S->tile_right || (want_v ? 1 : 0) != S->variant) configure(S, want_tr, want_v);
       return;
     }
   }
@@ -859,6 +859,7 @@ hbx_status hbx_ctx_create(int device, const hbx_opts* opts, hbx_ctx** out) {
     HBX_CUDA(cudaGetDeviceProperties(&prop, device));
     ctx->n_sm = prop.multiProcessorCount;
     ctx->smem_optin = prop.sharedMemPerBlockOptin;
+    ctx->device_name = prop.name;
     HBX_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
     cudaMemPoolProps props{};
     props.allocType = cudaMemAllocationTypePinned;
@@ -879,6 +880,7 @@ hbx_status hbx_ctx_destroy(hbx_ctx* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  if (ctx->h_ctr) cudaFreeHost(ctx->h_ctr);
   delete ctx;
   return HBX_OK;
 }

@@ -771,41 +771,37 @@ __device__ __forceinline__ bool scan_begin(Scan<W>& z, const uint32_t* tab, cons
   return true;
 }
 
-// One scan step of 8 symbols (the row loads of all 8 in flight at once);
-// every 16 symbols the pair stops once even
+// One scan step of 16 symbols, the chunk in hand (the next chunk was asked
+// for one step earlier); after each, the pair stops once even
 // matching every remaining symbol stays below its bound.  Returns true when
 // the pair is decided (*pass = the decision).
 template <int W>
 __device__ __forceinline__ bool scan_step(Scan<W>& z, bool* pass, Counters* ctr, WorkTally* ops) {
   constexpr int S = row_words(W);
-  if ((z.i & 15u) == 0 && z.i) {
+  if (z.i) {
     // chunk i/16 arrived one chunk ago; ask for the one after it
     z.cur = z.nxt;
     if (z.i + 16u < z.n_iter) z.nxt = __ldg(reinterpret_cast<const uint4*>(z.b + z.i + 16u));
   }
-  const uint32_t wd = z.cur.x, wd2 = z.cur.y;
-  z.cur.x = z.cur.z;
-  z.cur.y = z.cur.w;
+  const uint32_t wds[4] = {z.cur.x, z.cur.y, z.cur.z, z.cur.w};
 #pragma unroll
-  for (int c = 0; c < 4; c++)
-    bp_step<W, S>(z.tab, (wd >> (8 * c)) & 0xffu, z.win, z.mt, (z.i + (uint32_t)c) < z.h ? 1u : 0u);
+  for (int q = 0; q < 4; q++)
 #pragma unroll
-  for (int c = 0; c < 4; c++)
-    bp_step<W, S>(z.tab, (wd2 >> (8 * c)) & 0xffu, z.win, z.mt, (z.i + 4u + (uint32_t)c) < z.h ? 1u : 0u);
-  z.i += 8;
-  ops->steps += 2;
-  if (z.i >= z.n_iter || (z.i & 15u) == 0) {
-    uint32_t m = 0;
+    for (int c = 0; c < 4; c++)
+      bp_step<W, S>(z.tab, (wds[q] >> (8 * c)) & 0xffu, z.win, z.mt,
+                    (z.i + 4u * q + (uint32_t)c) < z.h ? 1u : 0u);
+  z.i += 16;
+  ops->steps += 4;
+  uint32_t m = 0;
 #pragma unroll
-    for (int k = 0; k < W; k++) m += __popc(z.mt[k]);
-    if (z.i >= z.n_iter) {
-      *pass = jw_decide(m, z.ls, z.ll, z.p, z.thr, &ctr->ambiguous);
-      return true;
-    }
-    if ((int)(z.i - m) > z.allowed) {
-      *pass = false;  // even matching every remaining symbol stays below
-      return true;
-    }
+  for (int k = 0; k < W; k++) m += __popc(z.mt[k]);
+  if (z.i >= z.n_iter) {
+    *pass = jw_decide(m, z.ls, z.ll, z.p, z.thr, &ctr->ambiguous);
+    return true;
+  }
+  if ((int)(z.i - m) > z.allowed) {
+    *pass = false;  // even matching every remaining symbol stays below
+    return true;
   }
   return false;
 }
