@@ -17,4 +17,6 @@ struct hbx_ctx {
   std::string err;
   std::string device_name;  // keys the autotuner's cache
   void* h_ctr = nullptr;    // page-locked counters of the context's session runs
+  void* h_out = nullptr;    // page-locked staging of one-shot results (grown as needed)
+  size_t h_out_n = 0;
 };

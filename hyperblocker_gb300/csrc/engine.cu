@@ -881,6 +881,7 @@ hbx_status hbx_ctx_destroy(hbx_ctx* ctx) {
   if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   if (ctx->h_ctr) cudaFreeHost(ctx->h_ctr);
+  if (ctx->h_out) cudaFreeHost(ctx->h_out);
   delete ctx;
   return HBX_OK;
 }
@@ -970,9 +971,23 @@ hbx_status hbx_block(hbx_ctx* ctx, const hbx_plan* plan, const hbx_table* left,
     if (n > out->capacity) hbx::fail(HBX_ERR_CAPACITY, "output capacity below the match count");
     if (n) {
       if (!out->l_row || !out->r_row) hbx::fail(HBX_ERR_INVALID_ARG, "null output pointer");
-      HBX_CUDA(cudaMemcpyAsync(out->l_row, s->out_l.p, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
-      HBX_CUDA(cudaMemcpyAsync(out->r_row, s->out_r.p, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+      // through the context's page-locked staging (copies at link speed)
+      const size_t bytes = n * 8;
+      if (ctx->h_out_n < bytes) {
+        if (ctx->h_out) cudaFreeHost(ctx->h_out);
+        ctx->h_out = nullptr;
+        ctx->h_out_n = 0;
+        size_t want = 1 << 20;
+        while (want < bytes) want *= 2;
+        HBX_CUDA(cudaHostAlloc(&ctx->h_out, want, cudaHostAllocPortable));
+        ctx->h_out_n = want;
+      }
+      uint32_t* hl = static_cast<uint32_t*>(ctx->h_out);
+      HBX_CUDA(cudaMemcpyAsync(hl, s->out_l.p, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+      HBX_CUDA(cudaMemcpyAsync(hl + n, s->out_r.p, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
       HBX_CUDA(cudaStreamSynchronize(ctx->stream));
+      std::memcpy(out->l_row, hl, n * 4);
+      std::memcpy(out->r_row, hl + n, n * 4);
     }
     out->n_written = n;
   });

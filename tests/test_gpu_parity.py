@@ -203,6 +203,33 @@ def test_pairs_of_many_items_share_a_warp(built, variant):
         c.close()
 
 
+def test_string_lengths_at_word_and_table_boundaries(ctx):
+    """Left and right strings of 0-300 bytes around every scan-width and
+    table boundary (32, 64, 96, 128, 256 = the longest string with a Peq
+    table), over a 3-symbol alphabet so that many pairs reach a scan, on both
+    predicates of a rule (the second one reached only by pairs that pass the
+    first)."""
+    lens = [0, 1, 2, 15, 16, 17, 31, 32, 33, 63, 64, 65, 95, 96, 97, 127, 128, 129, 160,
+            255, 256, 257, 300]
+    rng = np.random.Generator(np.random.PCG64(2024))
+
+    def table(n, prefix):
+        def s():
+            return bytes(rng.choice(list(b"abc"), size=lens[int(rng.integers(0, len(lens)))]).tolist())
+        ids = [b"id"] + [f"{prefix}{i}".encode() for i in range(n)]
+        return [ids, [b"s1"] + [s() for _ in range(n)], [b"s2"] + [s() for _ in range(n)],
+                [b"k1"] + [b"0"] * n, [b"k2"] + [b"0"] * n]
+
+    cl, cr = table(120, "l"), table(160, "r")
+    docs = [synth.rule_yaml([3], [(1, 0.62), (2, 0.6)])]
+    want = api.run_block(api.CTable(cl), api.CTable(cr), _oracle_plan(docs), 1)
+    for mode in MODES:
+        got, st = _engine_pairs(ctx, docs, cl, cr, 1, _util.INT_MAX, mode)
+        assert np.array_equal(got, want.pairs), mode
+        assert st.fma_ambiguous == 0
+    assert len(want.pairs) > 100
+
+
 def test_autotuner_choice_is_cached_and_exact(built, tmp_path, monkeypatch):
     cache = tmp_path / "tune.json"
     monkeypatch.setenv("HBX_AUTOTUNE_CACHE", str(cache))
