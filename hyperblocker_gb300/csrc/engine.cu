@@ -71,7 +71,8 @@ struct hbx_session {
   hbx::DBuf<unsigned long long> seen;  // reported-pair set (plans with several rules)
   // key histograms and scatter cursors of every rule, one block: one memset
   hbx::DBuf<uint32_t> counts;
-  bool fused_join = false;  // every key domain small: the three-kernel join
+  bool fused_join = false;  // every key domain small: the four-kernel join
+  hbx::DBuf<unsigned long long> scan_totals;  // fused join: chunk totals [rule][scan][chunk]
   hbx::DBuf<uint32_t> bound_idx;              // per rule, n_partitions + 1 key indices
   hbx::DBuf<unsigned long long> bound_val;    // item_off at those keys
   hbx::dev::Side side_l{}, side_r{};
@@ -273,6 +274,10 @@ void setup_session(hbx_session* S, uint64_t h2d_tables) {
       pos += 2ull * d.domain_l + 2ull * d.domain;
       if (d.domain_l > dev::kFusedJoinMaxDomain) S->fused_join = false;
     }
+    uint32_t max_d = 1;
+    for (const dev::Rule& d : S->h_rules) max_d = std::max(max_d, d.domain_l);
+    const uint32_t nb = (max_d + dev::kScanChunk - 1) / dev::kScanChunk;
+    if (S->fused_join) S->scan_totals.alloc((size_t)S->h_rules.size() * 3 * nb);
   }
   S->d_rules.alloc(E.rules.size());
   S->d_rule_base.alloc(E.rules.size() + 1);
@@ -349,13 +354,16 @@ uint32_t enqueue_join(hbx_session* S, cudaStream_t st) {
     for (const dev::Rule& d : S->h_rules) max_d = std::max(max_d, d.domain_l);
     const size_t smem = std::min<uint32_t>(max_d, dev::kSharedHistKeys) * sizeof(uint32_t);
     const int grid = row_grid(std::max(nL, nR), n_sm);
+    const uint32_t nb = (max_d + dev::kScanChunk - 1) / dev::kScanChunk;
     dev::k_join_count<<<grid, 256, smem, st>>>(S->side_l, S->side_r, S->d_rules.p, n_rules);
-    dev::k_join_scan<<<dim3(n_rules, 3), 1024, 0, st>>>(S->d_rules.p, S->tile_right,
-                                                        &S->d_ctr.p->comparisons);
+    dev::k_join_scan_totals<<<dim3(nb, 3, n_rules), 1024, 0, st>>>(
+        S->d_rules.p, S->tile_right, nb, S->scan_totals.p, &S->d_ctr.p->comparisons);
+    dev::k_join_scan_final<<<dim3(nb, 3, n_rules), 1024, 0, st>>>(S->d_rules.p, S->tile_right, nb,
+                                                                  S->scan_totals.p);
     dev::k_join_scatter<<<grid, 256, 0, st>>>(S->side_l, S->side_r, S->d_rules.p, n_rules,
                                                S->d_rule_base.p);
     launch_check("join kernels");
-    return 3;
+    return 4;
   }
   for (size_t r = 0; r < S->rb.size(); r++) {
     RuleBufs& b = S->rb[r];

@@ -178,8 +178,9 @@ __global__ void k_items_final(const Rule* rules, uint32_t rule, uint32_t tile_ri
 }
 
 // ---- fused join for small key domains (every rule's left key domain at most
-// kFusedJoinMaxDomain): one launch each for keys + histograms, offsets + work
-// items, and the scatter, covering every rule and both tables.
+// kFusedJoinMaxDomain): one launch for keys + histograms, two for offsets +
+// work items (chunk totals, then each chunk's scan), one for the scatter,
+// each covering every rule and both tables.
 
 // Keys and key histograms of every rule for both tables; histograms of
 // domains up to kSharedHistKeys are kept per block in shared memory.
@@ -216,62 +217,99 @@ __global__ void k_join_count(Side L, Side R, const Rule* rules, uint32_t n_rules
   }
 }
 
-// Three blocks (1024 threads) per rule (blockIdx.x), one per independent
-// scan (blockIdx.y): 0 = row offsets per left key, 1 = row offsets per right
-// key, 2 = work items per left key and the rule's pair-comparison count.
-__global__ void k_join_scan(const Rule* rules, uint32_t tile_right, unsigned long long* comparisons) {
-  __shared__ uint32_t s_w32[32];
-  __shared__ uint32_t s_t32;
+// The three independent scans of every rule -- row offsets per left key
+// (y = 0), row offsets per right key (y = 1), work items per left key with
+// the rule's pair-comparison count (y = 2) -- in chunks of kScanChunk keys,
+// one block of 1024 threads per (chunk, y, rule): k_join_scan_totals writes
+// every chunk's total, k_join_scan_final adds the totals of the earlier
+// chunks to the chunk's own exclusive scan.
+__device__ __forceinline__ uint32_t join_scan_domain(const Rule& Q, uint32_t y) {
+  return y == 1 ? Q.domain : Q.domain_l;
+}
+
+// The values of one chunk: 4 keys per thread (counts, or work items).
+__device__ __forceinline__ void join_scan_values(const Rule& Q, uint32_t y, uint32_t tile_right,
+                                                 uint32_t b, uint32_t D,
+                                                 unsigned long long (&v)[4],
+                                                 unsigned long long* pairs) {
+  const uint32_t* cnt = y == 1 ? Q.cnt_r : Q.cnt_l;
+  unsigned long long pr = 0;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    v[k] = 0;
+    if (b + k < D) {
+      if (y == 2) {
+        unsigned long long p = 0;
+        v[k] = key_items(Q, b + k, tile_right, &p);
+        pr += p;
+      } else {
+        v[k] = cnt[b + k];
+      }
+    }
+  }
+  *pairs = pr;
+}
+
+__global__ void k_join_scan_totals(const Rule* rules, uint32_t tile_right, uint32_t nb_max,
+                                   unsigned long long* totals, unsigned long long* comparisons) {
   __shared__ unsigned long long s_w64[32];
   __shared__ unsigned long long s_t64;
-  const Rule& Q = rules[blockIdx.x];
-  if (blockIdx.y < 2) {
-    const int side = (int)blockIdx.y;
-    const uint32_t D = side ? Q.domain : Q.domain_l;
-    const uint32_t* cnt = side ? Q.cnt_r : Q.cnt_l;
-    uint32_t* off = side ? Q.off_r : Q.off_l;
-    uint32_t carry = 0;
-    for (uint32_t base = 0; base < D; base += kScanChunk) {
-      const uint32_t b = base + threadIdx.x * 4u;
-      uint32_t v[4], sum = 0;
-      for (int k = 0; k < 4; k++) {
-        v[k] = b + k < D ? cnt[b + k] : 0u;
-        sum += v[k];
-      }
-      uint32_t ex = block_excl_scan<uint32_t>(sum, s_w32, &s_t32) + carry;
-      for (int k = 0; k < 4; k++) {
-        if (b + k < D) off[b + k] = ex;
-        ex += v[k];
-      }
-      carry += s_t32;
-      __syncthreads();
-    }
-    return;
+  const uint32_t c = blockIdx.x, y = blockIdx.y, r = blockIdx.z;
+  const Rule& Q = rules[r];
+  const uint32_t D = join_scan_domain(Q, y);
+  if ((unsigned long long)c * kScanChunk >= D) return;
+  unsigned long long v[4], pairs = 0;
+  join_scan_values(Q, y, tile_right, c * kScanChunk + threadIdx.x * 4u, D, v, &pairs);
+  const unsigned long long sum = v[0] + v[1] + v[2] + v[3];
+  block_excl_scan<unsigned long long>(sum, s_w64, &s_t64);
+  if (threadIdx.x == 0) totals[((size_t)r * 3 + y) * nb_max + c] = s_t64;
+  if (y == 2) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) pairs += __shfl_xor_sync(kFull, pairs, o);
+    if ((threadIdx.x & 31) == 0 && pairs) atomicAdd(comparisons, pairs);
   }
-  // work items per left key (exclusive, with the total at domain_l)
-  unsigned long long carry = 0, pairs = 0;
-  for (uint32_t base = 0; base < Q.domain_l; base += kScanChunk) {
-    const uint32_t b = base + threadIdx.x * 4u;
-    unsigned long long v[4], sum = 0, pr = 0;
+}
+
+__global__ void k_join_scan_final(const Rule* rules, uint32_t tile_right, uint32_t nb_max,
+                                  const unsigned long long* totals) {
+  __shared__ unsigned long long s_w64[32];
+  __shared__ unsigned long long s_t64;
+  __shared__ unsigned long long s_base;
+  const uint32_t c = blockIdx.x, y = blockIdx.y, r = blockIdx.z;
+  const Rule& Q = rules[r];
+  const uint32_t D = join_scan_domain(Q, y);
+  if ((unsigned long long)c * kScanChunk >= D) return;
+  const unsigned long long* tot = totals + ((size_t)r * 3 + y) * nb_max;
+  if (threadIdx.x < 32) {  // totals of the earlier chunks (at most 16 for the fused join)
+    unsigned long long t = 0;
+    for (uint32_t k = threadIdx.x; k < c; k += 32) t += tot[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(kFull, t, o);
+    if (threadIdx.x == 0) s_base = t;
+  }
+  __syncthreads();
+  const unsigned long long base = s_base;
+  const uint32_t b = c * kScanChunk + threadIdx.x * 4u;
+  unsigned long long v[4], pairs = 0;
+  join_scan_values(Q, y, tile_right, b, D, v, &pairs);
+  unsigned long long ex =
+      block_excl_scan<unsigned long long>(v[0] + v[1] + v[2] + v[3], s_w64, &s_t64) + base;
+  if (y == 2) {
+#pragma unroll
     for (int k = 0; k < 4; k++) {
-      unsigned long long p = 0;
-      v[k] = b + k < Q.domain_l ? key_items(Q, b + k, tile_right, &p) : 0ull;
-      sum += v[k];
-      pr += p;
-    }
-    unsigned long long ex = block_excl_scan<unsigned long long>(sum, s_w64, &s_t64) + carry;
-    for (int k = 0; k < 4; k++) {
-      if (b + k < Q.domain_l) Q.item_off[b + k] = ex;
+      if (b + k < D) Q.item_off[b + k] = ex;
       ex += v[k];
     }
-    carry += s_t64;
-    pairs += pr;
-    __syncthreads();
-  }
+    if ((unsigned long long)(c + 1) * kScanChunk >= D && threadIdx.x == 0)
+      Q.item_off[D] = base + s_t64;
+  } else {
+    uint32_t* off = y == 1 ? Q.off_r : Q.off_l;
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) pairs += __shfl_xor_sync(kFull, pairs, o);
-  if ((threadIdx.x & 31) == 0 && pairs) atomicAdd(comparisons, pairs);
-  if (threadIdx.x == 0) Q.item_off[Q.domain_l] = carry;
+    for (int k = 0; k < 4; k++) {
+      if (b + k < D) off[b + k] = (uint32_t)ex;
+      ex += v[k];
+    }
+  }
 }
 
 // Rows of every rule grouped by key (counting-sort scatter, right rows with

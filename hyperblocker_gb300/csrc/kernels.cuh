@@ -281,7 +281,10 @@ __global__ void k_rule_base(const Rule* rules, uint32_t n_rules, unsigned long l
 constexpr uint32_t kFusedJoinMaxDomain = 1u << 16;
 constexpr uint32_t kSharedHistKeys = 8192;
 __global__ void k_join_count(Side L, Side R, const Rule* rules, uint32_t n_rules);
-__global__ void k_join_scan(const Rule* rules, uint32_t tile_right, unsigned long long* comparisons);
+__global__ void k_join_scan_totals(const Rule* rules, uint32_t tile_right, uint32_t nb_max,
+                                   unsigned long long* totals, unsigned long long* comparisons);
+__global__ void k_join_scan_final(const Rule* rules, uint32_t tile_right, uint32_t nb_max,
+                                  const unsigned long long* totals);
 __global__ void k_join_scatter(Side L, Side R, const Rule* rules, uint32_t n_rules,
                                unsigned long long* rule_base);
 // ------------------------------------------------------------------ evaluation
