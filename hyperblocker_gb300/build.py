@@ -23,7 +23,7 @@ EXE = os.path.join(OUT, "run_hyperblocker_exec")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 CU_SOURCES = ["kernels.cu", "engine.cu", "ingest.cu", "serve.cu", "stream.cu", "static_scratch.cu",
-              "writer.cu", "csv_gpu.cu"]
+              "writer.cu", "csv_gpu.cu", "sort.cu"]
 CPP_SOURCES = ["csv.cpp", "rules.cpp", "planner.cpp", "encode.cpp", "capi.cpp", "cli.cpp"]
 
 

@@ -24,6 +24,12 @@
 
 #include "../../include/hbx.h"
 
+// engine.cu: hbx_block, the sort and hbx_write_pairs with the pairs on the device
+extern "C" hbx_status hbx_internal_block_to_file(hbx_ctx* ctx, const hbx_plan* plan,
+                                                 const hbx_table* left, const hbx_table* right,
+                                                 uint64_t n_partitions, int64_t prefix_idx,
+                                                 hbx_mode mode, const char* path, hbx_stats* stats);
+
 namespace {
 
 struct Flags {
@@ -155,42 +161,42 @@ extern "C" int hbx_run_cli(int argc, const char* const* argv) {
     }
     const auto t1 = std::chrono::steady_clock::now();
     std::printf("HyperBlocker.Initialize() elapsed: %f\n", secs(t0, t1));
-    hbx_pairs out{};
-    ol.resize(1 << 16);
-    orr.resize(1 << 16);
-    for (;;) {
-      out.l_row = ol.data();
-      out.r_row = orr.data();
-      out.capacity = ol.size();
-      s = hbx_block(ctx, plan, L, R, F.n_partitions, (int64_t)F.prefix_hash_pred_idx, mode, &out, &st);
-      if (s == HBX_ERR_CAPACITY) {
-        ol.resize(out.n_required);
-        orr.resize(out.n_required);
-        continue;
+    if (!F.o.empty()) {
+      // the pairs stay on the device: run, sort by (left row, right row),
+      // format the id lines and append them to -o
+      s = hbx_internal_block_to_file(ctx, plan, L, R, F.n_partitions,
+                                     (int64_t)F.prefix_hash_pred_idx, mode, F.o.c_str(), &st);
+      if (s != HBX_OK) {
+        die("blocking", s);
+        break;
       }
-      break;
-    }
-    if (s != HBX_OK) {
-      die("blocking", s);
-      break;
-    }
-    std::vector<uint64_t> key(out.n_written);
-    for (uint64_t i = 0; i < out.n_written; i++) key[i] = ((uint64_t)ol[i] << 32) | orr[i];
-    std::sort(key.begin(), key.end());
-    for (uint64_t i = 0; i < out.n_written; i++) {
-      ol[i] = (uint32_t)(key[i] >> 32);
-      orr[i] = (uint32_t)key[i];
+    } else {
+      hbx_pairs out{};
+      ol.resize(1 << 16);
+      orr.resize(1 << 16);
+      for (;;) {
+        out.l_row = ol.data();
+        out.r_row = orr.data();
+        out.capacity = ol.size();
+        s = hbx_block(ctx, plan, L, R, F.n_partitions, (int64_t)F.prefix_hash_pred_idx, mode, &out,
+                      &st);
+        if (s == HBX_ERR_CAPACITY) {
+          ol.resize(out.n_required);
+          orr.resize(out.n_required);
+          continue;
+        }
+        break;
+      }
+      if (s != HBX_OK) {
+        die("blocking", s);
+        break;
+      }
+      std::fprintf(stderr, "WARNING: no -o given, pairs not written\n");
     }
     std::printf("Actual number of partitions: %u\n", st.n_partitions_used);
     std::printf("pairs covered: %llu, pair comparisons: %llu, matches: %llu, device ms: %.3f\n",
                 (unsigned long long)st.pairs_covered, (unsigned long long)st.pair_comparisons,
                 (unsigned long long)st.n_matches, st.ms_last_run);
-    if (F.o.empty()) {
-      std::fprintf(stderr, "WARNING: no -o given, pairs not written\n");
-    } else if ((s = hbx_write_pairs(ctx, L, R, ol.data(), orr.data(), out.n_written, F.o.c_str())) != HBX_OK) {
-      die("output", s);
-      break;
-    }
     std::printf("HyperBlocker.Run() elapsed: %f\n", secs(t1, std::chrono::steady_clock::now()));
   } while (false);
   if (L) hbx_table_destroy(L);

@@ -29,6 +29,7 @@
 
 #include "context.h"
 #include "device_buffers.h"
+#include "engine.h"
 #include "encode.h"
 #include "hbx_core.h"
 #include "ingest.h"
@@ -998,6 +999,35 @@ hbx_status hbx_block(hbx_ctx* ctx, const hbx_plan* plan, const hbx_table* left,
       std::memcpy(out->r_row, hl + n, n * 4);
     }
     out->n_written = n;
+  });
+  S.reset();
+  return st;
+}
+
+// run_hyperblocker_exec's pipeline with the pairs kept on the device: one
+// session run, the pairs sorted by (left row, right row), their id lines
+// formatted and appended to path.
+hbx_status hbx_internal_block_to_file(hbx_ctx* ctx, const hbx_plan* plan, const hbx_table* left,
+                                      const hbx_table* right, uint64_t n_partitions,
+                                      int64_t prefix_idx, hbx_mode mode, const char* path,
+                                      hbx_stats* stats) {
+  if (!ctx || !plan || !left || !right || !path) return HBX_ERR_INVALID_ARG;
+  auto S = std::make_unique<hbx_session>();
+  S->ctx = ctx;
+  S->one_shot = true;
+  hbx_session* s = S.get();
+  hbx_status st = guard(ctx, [&] {
+    if (prefix_idx != INT_MAX && (prefix_idx < 0 || prefix_idx > INT_MAX))
+      hbx::fail(HBX_ERR_INVALID_ARG, "prefix_idx out of range");
+    HBX_CUDA(cudaSetDevice(ctx->device));
+    hbx::PoolScope scope(ctx->pool, ctx->stream);
+    hbx::create_session(s, plan, left, right, n_partitions, prefix_idx);
+    hbx::session_run(s, mode, ctx->stream);
+    const uint64_t n = s->stats.n_matches;
+    if (stats) *stats = s->stats;
+    hbx::sort_pairs_device(ctx, s->out_l.p, s->out_r.p, n, (uint32_t)left->t.n_rows,
+                           (uint32_t)right->t.n_rows);
+    hbx::write_pairs_device(ctx, left->t, right->t, s->out_l.p, s->out_r.p, n, path);
   });
   S.reset();
   return st;

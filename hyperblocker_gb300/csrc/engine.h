@@ -12,4 +12,12 @@ namespace hbx {
 // pairs, exactly sized, into host vectors.
 void run_to_host(hbx_session* s, hbx_mode mode, std::vector<uint32_t>* l, std::vector<uint32_t>* r);
 
+struct Table;
+// sort.cu: sorts n device pairs by (left row, right row) in place.
+void sort_pairs_device(hbx_ctx* ctx, uint32_t* l, uint32_t* r, uint64_t n, uint32_t n_left,
+                       uint32_t n_right);
+// writer.cu: appends the id lines of n device pairs to path.
+void write_pairs_device(hbx_ctx* ctx, const Table& left, const Table& right, const uint32_t* l_row,
+                        const uint32_t* r_row, uint64_t n, const char* path);
+
 }  // namespace hbx

@@ -91,3 +91,42 @@ def test_out_of_range_rows_are_refused(ctx, tmp_path):
     dr = torch.tensor([0, 1], dtype=torch.int32, device="cuda")
     with pytest.raises(hb.HbxError):
         hb.write_pairs_device(ctx, L, R, dl.data_ptr(), dr.data_ptr(), 2, str(tmp_path / "x.txt"))
+
+
+def test_cli_pipeline_sorts_and_writes_on_device(built, tmp_path):
+    """run_hyperblocker_exec keeps the pairs on the device: the file holds the
+    engine's pairs sorted by (left row, right row), byte for byte what the
+    host writer makes of them, across many sort tiles and row bytes."""
+    import subprocess
+
+    from hyperblocker_gb300 import synth
+    from tests import _util
+
+    cl, cr = _util.random_tables(3131, 700, 900, b"ab", 12, n_eq_values=2)
+
+    def write_csv(path, cols):
+        with open(path, "wb") as f:
+            for i in range(len(cols[0])):
+                f.write(b",".join(b'"' + c[i] + b'"' for c in cols) + b"\n")
+
+    lp, rp = tmp_path / "l.csv", tmp_path / "r.csv"
+    write_csv(lp, cl)
+    write_csv(rp, cr)
+    rules = tmp_path / "rules"
+    rules.mkdir()
+    (rules / "0.yaml").write_text(synth.rule_yaml([3], [(1, 0.55)]))
+    out = tmp_path / "pairs.csv"
+    cmd = [hb.EXE_PATH, "-data_l", str(lp), "-data_r", str(rp), "-rule_dir", str(rules),
+           "-n_partitions", "2", "-o", str(out)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    ctx = hb.Context(0)
+    plan = hb.Plan.from_rule_dir(str(rules), ctx)
+    L = hb.Table.from_csv(str(lp))
+    R = hb.Table.from_csv(str(rp))
+    pairs, _ = hb.block(ctx, plan, L, R, 2)
+    assert len(pairs) > 20_000  # many sort tiles
+    want = tmp_path / "want.csv"
+    hb.write_pairs(L, R, _util.sorted_pairs(pairs), str(want))  # host loop, row order
+    assert out.read_bytes() == want.read_bytes()
+    ctx.close()
