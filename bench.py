@@ -352,6 +352,18 @@ def bench_serving(args, ctx):
                        "arrival times"}
 
 
+def max_over_ranks(dist, values, device):
+    """Element-wise maximum over the ranks of per-rank timings: the slowest
+    replica sets the job's time (values unchanged without a process group)."""
+    if dist is None:
+        return [float(v) for v in values]
+    import torch
+
+    t = torch.tensor([float(v) for v in values], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t]
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
@@ -437,13 +449,7 @@ def run_engine(args, rank, world, local_rank):
     wall_batched = time.perf_counter() - t_wall
     clocks = sampler.stop()
     pla = timed("plain", args.steps, args.warmup)
-    total_ms = sum(bat["ms"])
-    if dist:
-        t = torch.tensor([total_ms, sum(pla["ms"])], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms, plain_ms = float(t[0]), float(t[1])
-    else:
-        plain_ms = sum(pla["ms"])
+    total_ms, plain_ms = max_over_ranks(dist, [sum(bat["ms"]), sum(pla["ms"])], dev)
     cmp_step = bat["cmp"][0]
     value = world * cmp_step * args.steps / (total_ms / 1000.0)
     plain_value = world * cmp_step * args.steps / (plain_ms / 1000.0)
