@@ -85,6 +85,9 @@ struct hbx_session {
   int variant = 0;  // evaluation kernel: 0 = k_eval, 1 = k_eval_wide
   bool tuned = false;
   bool one_shot = false;  // runs once (hbx_block): no graph is captured
+  // output slots to start with; a run needing more than cap_limit (the
+  // caller's buffer, 0 = none) returns its count without growing and rerunning
+  uint64_t out_hint = 1 << 16, cap_limit = 0;
   int blocks_per_sm = 1;
   size_t smem_bytes = 0;
   cudaGraphExec_t graph = nullptr;
@@ -284,7 +287,8 @@ void setup_session(hbx_session* S, uint64_t h2d_tables) {
   S->d_rule_base.alloc(E.rules.size() + 1);
   S->d_ctr.alloc(1);
   // one page-locked counter block per context: its sessions run one at a time
-  if (!C->h_ctr) HBX_CUDA(cudaHostAlloc(&C->h_ctr, sizeof(dev::Counters), cudaHostAllocPortable));
+  if (!C->h_ctr)  // the counters, then the total of work items (u64)
+    HBX_CUDA(cudaHostAlloc(&C->h_ctr, sizeof(dev::Counters) + 8, cudaHostAllocPortable));
   S->h_ctr = static_cast<dev::Counters*>(C->h_ctr);
   const uint32_t tile = C->opts.tile_right > 0 ? (uint32_t)C->opts.tile_right : 128u;
   const int variant = C->opts.eval_variant > 0 ? C->opts.eval_variant - 1 : 1;
@@ -319,9 +323,14 @@ void setup_session(hbx_session* S, uint64_t h2d_tables) {
       }
   S->bound_idx.upload(idx, st);
   S->bound_val.alloc(idx.size());
-  S->out_l.alloc(1 << 16);
-  S->out_r.alloc(1 << 16);
-  if (E.rules.size() > 1) S->seen.alloc(1 << 17);
+  const uint64_t cap0 = std::max<uint64_t>(1 << 16, S->out_hint);
+  S->out_l.alloc(cap0);
+  S->out_r.alloc(cap0);
+  if (E.rules.size() > 1) {
+    uint64_t slots = 1 << 17;
+    while (slots < 2 * cap0) slots *= 2;  // load factor at most one half
+    S->seen.alloc(slots);
+  }
   HBX_CUDA(cudaEventCreate(&S->ev0));
   HBX_CUDA(cudaEventCreate(&S->ev1));
   HBX_CUDA(cudaEventCreate(&S->ev_eval0));
@@ -413,6 +422,8 @@ dev::EvalParams eval_params(hbx_session* S) {
   return P;
 }
 
+void queue_counters(hbx_session* S, cudaStream_t st);
+
 uint32_t enqueue_batched(hbx_session* S, cudaStream_t st) {
   uint32_t launches = enqueue_join(S, st);
   dev::EvalParams P = eval_params(S);
@@ -429,8 +440,8 @@ uint32_t enqueue_batched(hbx_session* S, cudaStream_t st) {
   dev::eval_kernel(S->variant)<<<grid, kThreads, S->smem_bytes, st>>>(P);
   launch_check("k_eval");
   HBX_CUDA(cudaEventRecordWithFlags(S->ev_eval1, st, rec_flags));
-  // the counters travel back inside the run (a graph node when captured)
-  HBX_CUDA(cudaMemcpyAsync(S->h_ctr, S->d_ctr.p, sizeof(dev::Counters), cudaMemcpyDeviceToHost, st));
+  // the counters travel back inside the run (graph nodes when captured)
+  queue_counters(S, st);
   return launches + 1;
 }
 
@@ -458,8 +469,19 @@ uint64_t needed_capacity(const hbx_session* S, const dev::Counters& c) {
   return std::max<uint64_t>(need, S->out_l.n + 1);
 }
 
-dev::Counters read_counters(hbx_session* S, cudaStream_t st) {
+// Queues the copies of the counters and of the work-item total into the
+// context's page-locked block (a graph node each when captured).
+void queue_counters(hbx_session* S, cudaStream_t st) {
   HBX_CUDA(cudaMemcpyAsync(S->h_ctr, S->d_ctr.p, sizeof(dev::Counters), cudaMemcpyDeviceToHost, st));
+  HBX_CUDA(cudaMemcpyAsync(S->h_ctr + 1, S->d_rule_base.p + S->rb.size(), 8, cudaMemcpyDeviceToHost, st));
+}
+
+unsigned long long items_total(const hbx_session* S) {
+  return *reinterpret_cast<const unsigned long long*>(S->h_ctr + 1);
+}
+
+dev::Counters read_counters(hbx_session* S, cudaStream_t st) {
+  queue_counters(S, st);
   HBX_CUDA(cudaStreamSynchronize(st));
   return *S->h_ctr;
 }
@@ -789,17 +811,21 @@ void session_run(hbx_session* S, hbx_mode mode, cudaStream_t st) {
     S->stats.tile_right = S->tile_right;
     S->stats.n_windows = 1;
     S->stats.eval_variant = (uint32_t)S->variant + 1;
-    unsigned long long total_items = 0;
-    HBX_CUDA(cudaMemcpyAsync(&total_items, S->d_rule_base.p + S->rb.size(), sizeof total_items,
-                             cudaMemcpyDeviceToHost, st));
-    HBX_CUDA(cudaStreamSynchronize(st));
+    const unsigned long long total_items = items_total(S);  // copied with the counters
     S->stats.n_tiles = total_items;
     if (c.watchdog_trips) fail(HBX_ERR_WATCHDOG, "evaluation stopped by the watchdog budget");
     if (c.items_done != total_items)
       fail(HBX_ERR_CUDA, "evaluation finished " + std::to_string(c.items_done) + " of " +
                              std::to_string(total_items) + " work items");
     if (c.out_count <= S->out_l.n && c.seen_overflow == 0) return;
-    grow_output(S, needed_capacity(S, c));
+    const uint64_t need = needed_capacity(S, c);
+    if (S->cap_limit && need > S->cap_limit) {
+      // the caller's buffer is too small anyway: report the count (an upper
+      // bound when the duplicate set overflowed) instead of running again
+      S->stats.n_matches = c.seen_overflow ? std::max<uint64_t>(c.out_count, c.passes) : c.out_count;
+      return;
+    }
+    grow_output(S, need);
   }
   fail(HBX_ERR_CAPACITY, "output kept growing");
 }
@@ -965,6 +991,9 @@ hbx_status hbx_block(hbx_ctx* ctx, const hbx_plan* plan, const hbx_table* left,
   auto S = std::make_unique<hbx_session>();
   S->ctx = ctx;
   S->one_shot = true;
+  // the caller's buffer sizes the device output; a larger result is only counted
+  S->out_hint = out->capacity;
+  S->cap_limit = std::max<uint64_t>(out->capacity, 1);
   hbx_session* s = S.get();
   hbx_status st = guard(ctx, [&] {
     if (prefix_idx != INT_MAX && (prefix_idx < 0 || prefix_idx > INT_MAX))
