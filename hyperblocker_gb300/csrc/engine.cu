@@ -425,23 +425,26 @@ dev::EvalParams eval_params(hbx_session* S) {
 void queue_counters(hbx_session* S, cudaStream_t st);
 
 uint32_t enqueue_batched(hbx_session* S, cudaStream_t st) {
-  uint32_t launches = enqueue_join(S, st);
-  dev::EvalParams P = eval_params(S);
-  P.n_seg = 0;  // every work item of every rule
-  const int grid = S->ctx->n_sm * S->blocks_per_sm;
   // Inside stream capture a plain record would only be a capture dependency
   // marker; the external flag makes it an event-record node that can be
-  // timed (the flag is refused outside capture).
+  // timed (the flag is refused outside capture).  The run's events (start,
+  // join done, evaluation done, end) are all recorded by the run itself.
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
   HBX_CUDA(cudaStreamIsCapturing(st, &cap));
   const unsigned rec_flags =
       cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
+  HBX_CUDA(cudaEventRecordWithFlags(S->ev0, st, rec_flags));
+  uint32_t launches = enqueue_join(S, st);
+  dev::EvalParams P = eval_params(S);
+  P.n_seg = 0;  // every work item of every rule
+  const int grid = S->ctx->n_sm * S->blocks_per_sm;
   HBX_CUDA(cudaEventRecordWithFlags(S->ev_eval0, st, rec_flags));
   dev::eval_kernel(S->variant)<<<grid, kThreads, S->smem_bytes, st>>>(P);
   launch_check("k_eval");
   HBX_CUDA(cudaEventRecordWithFlags(S->ev_eval1, st, rec_flags));
   // the counters travel back inside the run (graph nodes when captured)
   queue_counters(S, st);
+  HBX_CUDA(cudaEventRecordWithFlags(S->ev1, st, rec_flags));
   return launches + 1;
 }
 
@@ -517,6 +520,7 @@ dev::Counters run_once(hbx_session* S, hbx_mode mode, cudaStream_t st, uint32_t*
     return *S->h_ctr;
   }
   // PLAIN: join, then one launch per (partition, rule)
+  HBX_CUDA(cudaEventRecord(S->ev0, st));
   uint32_t n = enqueue_join(S, st);
   const uint32_t n_rules = (uint32_t)S->rb.size();
   const uint32_t per_class = (uint32_t)S->E.n_partitions + 1;
@@ -561,7 +565,10 @@ dev::Counters run_once(hbx_session* S, hbx_mode mode, cudaStream_t st, uint32_t*
   HBX_CUDA(cudaEventRecord(S->ev_eval1, st));
   *launches = n;
   S->stats.n_launches = n;
-  return read_counters(S, st);
+  queue_counters(S, st);
+  HBX_CUDA(cudaEventRecord(S->ev1, st));
+  HBX_CUDA(cudaStreamSynchronize(st));
+  return *S->h_ctr;
 }
 
 // ---- tile-shape autotuner ---------------------------------------------------
@@ -659,9 +666,7 @@ void write_autotune_file(const std::string& path, const std::map<std::string, st
 // one-shot run or a run over inputs larger than L2 does.
 float timed_batched_run(hbx_session* S, cudaStream_t st, DBuf<uint8_t>* flush = nullptr) {
   if (flush && flush->p) HBX_CUDA(cudaMemsetAsync(flush->p, 0, flush->n, st));
-  HBX_CUDA(cudaEventRecord(S->ev0, st));
-  enqueue_batched(S, st);
-  HBX_CUDA(cudaEventRecord(S->ev1, st));
+  enqueue_batched(S, st);  // records ev0 and ev1 itself
   HBX_CUDA(cudaEventSynchronize(S->ev1));
   float ms = 0;
   HBX_CUDA(cudaEventElapsedTime(&ms, S->ev0, S->ev1));
@@ -789,10 +794,7 @@ void session_run(hbx_session* S, hbx_mode mode, cudaStream_t st) {
 
   uint32_t launches = 0;
   for (int attempt = 0; attempt < 8; attempt++) {
-    HBX_CUDA(cudaEventRecord(S->ev0, st));
-    dev::Counters c = run_once(S, mode, st, &launches);
-    HBX_CUDA(cudaEventRecord(S->ev1, st));
-    HBX_CUDA(cudaEventSynchronize(S->ev1));
+    dev::Counters c = run_once(S, mode, st, &launches);  // returns with the stream idle
     float ms = 0, ms_join = 0, ms_eval = 0;
     HBX_CUDA(cudaEventElapsedTime(&ms, S->ev0, S->ev1));
     HBX_CUDA(cudaEventElapsedTime(&ms_join, S->ev0, S->ev_eval0));
