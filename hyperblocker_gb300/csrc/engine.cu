@@ -91,7 +91,14 @@ struct hbx_session {
   int blocks_per_sm = 1;
   size_t smem_bytes = 0;
   cudaGraphExec_t graph = nullptr;
-  uint64_t graph_capacity = 0;
+  // the caller's device output (hbx_session_run), written by the kernels
+  // directly; null: the session's own buffers
+  uint32_t* ext_l = nullptr;
+  uint32_t* ext_r = nullptr;
+  uint64_t ext_cap = 0;
+  const uint32_t* graph_out = nullptr;  // output the captured graph writes
+  uint64_t graph_cap = 0;
+  uint64_t seen_pairs = 1 << 16;  // distinct pairs the duplicate set is sized for
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;      // whole run
   cudaEvent_t ev_eval0 = nullptr, ev_eval1 = nullptr;  // join ends / evaluation ends
   hbx_stats stats{};
@@ -402,6 +409,27 @@ uint32_t enqueue_join(hbx_session* S, cudaStream_t st) {
   return launches;
 }
 
+// Output slots of the next run: the caller's buffer or the session's own.
+uint64_t out_cap(const hbx_session* S) { return S->ext_l ? S->ext_cap : S->out_l.n; }
+
+void drop_graph(hbx_session* S) {
+  if (S->graph) {
+    cudaGraphExecDestroy(S->graph);
+    S->graph = nullptr;
+  }
+}
+
+// The duplicate set holds at least 2 x `pairs` slots (load at most one half).
+void fit_seen(hbx_session* S, uint64_t pairs) {
+  if (!S->seen.p) return;
+  uint64_t slots = S->seen.n;
+  while (slots < 2 * pairs) slots *= 2;
+  if (slots != S->seen.n) {
+    S->seen.alloc(slots);
+    drop_graph(S);
+  }
+}
+
 dev::EvalParams eval_params(hbx_session* S) {
   dev::EvalParams P{};
   P.L = S->side_l;
@@ -412,9 +440,9 @@ dev::EvalParams eval_params(hbx_session* S) {
   P.rule_item_base = S->d_rule_base.p;
   P.tile_right = S->tile_right;
   dev::set_layout(&P, S->wl, S->peq_shape, S->peq.p);
-  P.out_l = S->out_l.p;
-  P.out_r = S->out_r.p;
-  P.capacity = S->out_l.n;
+  P.out_l = S->ext_l ? S->ext_l : S->out_l.p;
+  P.out_r = S->ext_l ? S->ext_r : S->out_r.p;
+  P.capacity = out_cap(S);
   P.ctr = S->d_ctr.p;
   P.watchdog_cycles = S->ctx->opts.watchdog_cycles;
   P.seen = S->seen.p;
@@ -494,7 +522,11 @@ dev::Counters run_once(hbx_session* S, hbx_mode mode, cudaStream_t st, uint32_t*
   const bool use_graph = S->ctx->opts.use_graph != 0 && !S->one_shot;
   if (mode == HBX_MODE_BATCHED) {
     if (use_graph) {
+      const uint32_t* out = S->ext_l ? S->ext_l : S->out_l.p;
+      if (S->graph && (S->graph_out != out || S->graph_cap != out_cap(S))) drop_graph(S);
       if (!S->graph) {
+        S->graph_out = out;
+        S->graph_cap = out_cap(S);
         cudaGraph_t g = nullptr;
         HBX_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         uint32_t n = 0;
@@ -713,8 +745,13 @@ void autotune(hbx_session* S, cudaStream_t st) {
       configure(S, cand[k].first, cand[k].second);
       float ms = timed_batched_run(S, st, &flush);
       const dev::Counters c = read_counters(S, st);
-      if (c.out_count > S->out_l.n || c.seen_overflow) {
-        grow_output(S, needed_capacity(S, c));
+      if (S->ext_l ? (bool)c.seen_overflow : (c.out_count > S->out_l.n || c.seen_overflow)) {
+        if (S->ext_l) {
+          S->seen_pairs = std::max<uint64_t>(2 * S->seen_pairs, c.passes);
+          fit_seen(S, S->seen_pairs);
+        } else {
+          grow_output(S, needed_capacity(S, c));
+        }
         ms = timed_batched_run(S, st, &flush);
       }
       best_ms[k] = std::min(best_ms[k], ms);
@@ -793,6 +830,7 @@ void session_run(hbx_session* S, hbx_mode mode, cudaStream_t st) {
   if (!S->tuned && mode == HBX_MODE_BATCHED) autotune(S, st);
 
   uint32_t launches = 0;
+  fit_seen(S, S->seen_pairs);
   for (int attempt = 0; attempt < 8; attempt++) {
     dev::Counters c = run_once(S, mode, st, &launches);  // returns with the stream idle
     float ms = 0, ms_join = 0, ms_eval = 0;
@@ -819,7 +857,20 @@ void session_run(hbx_session* S, hbx_mode mode, cudaStream_t st) {
     if (c.items_done != total_items)
       fail(HBX_ERR_CUDA, "evaluation finished " + std::to_string(c.items_done) + " of " +
                              std::to_string(total_items) + " work items");
-    if (c.out_count <= S->out_l.n && c.seen_overflow == 0) return;
+    if (c.seen_overflow == 0)
+      S->seen_pairs = std::max<uint64_t>(S->seen_pairs, c.out_count + c.out_count / 4);
+    if (c.out_count <= out_cap(S) && c.seen_overflow == 0) return;
+    if (S->ext_l) {
+      // the caller's buffer: a result larger than it is only counted; a
+      // full duplicate set is grown and the run repeated
+      if (c.out_count > S->ext_cap || (c.seen_overflow && c.passes > S->ext_cap)) {
+        S->stats.n_matches = c.seen_overflow ? std::max<uint64_t>(c.out_count, c.passes) : c.out_count;
+        return;
+      }
+      S->seen_pairs = std::max<uint64_t>(2 * S->seen_pairs, c.passes);
+      fit_seen(S, S->seen_pairs);
+      continue;
+    }
     const uint64_t need = needed_capacity(S, c);
     if (S->cap_limit && need > S->cap_limit) {
       // the caller's buffer is too small anyway: report the count (an upper
@@ -957,17 +1008,17 @@ hbx_status hbx_session_run(hbx_session* s, hbx_mode mode, hbx_pairs* out, void* 
   return guard(s->ctx, [&] {
     cudaStream_t st = stream ? (cudaStream_t)stream : s->ctx->stream;
     hbx::PoolScope scope(s->ctx->pool, st);
+    // the kernels write the caller's device buffers directly
+    const bool ext = out->l_row && out->r_row && out->capacity > 0;
+    s->ext_l = ext ? out->l_row : nullptr;
+    s->ext_r = ext ? out->r_row : nullptr;
+    s->ext_cap = ext ? out->capacity : 0;
+    s->cap_limit = ext ? 0 : 1;  // no buffer: count only
     hbx::session_run(s, mode, st);
     const uint64_t n = s->stats.n_matches;
     out->n_required = n;
     out->n_written = 0;
     if (n > out->capacity) hbx::fail(HBX_ERR_CAPACITY, "output capacity below the match count");
-    if (n) {
-      if (!out->l_row || !out->r_row) hbx::fail(HBX_ERR_INVALID_ARG, "null output pointer");
-      HBX_CUDA(cudaMemcpyAsync(out->l_row, s->out_l.p, n * 4, cudaMemcpyDeviceToDevice, st));
-      HBX_CUDA(cudaMemcpyAsync(out->r_row, s->out_r.p, n * 4, cudaMemcpyDeviceToDevice, st));
-      HBX_CUDA(cudaStreamSynchronize(st));
-    }
     out->n_written = n;
   });
 }

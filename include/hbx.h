@@ -44,7 +44,7 @@ typedef enum hbx_status {
   HBX_ERR_INVALID_ARG = 1,
   HBX_ERR_CUDA = 2,
   HBX_ERR_OOM = 3,
-  HBX_ERR_CAPACITY = 4,   /* output buffer too small; n_required is set, nothing partial */
+  HBX_ERR_CAPACITY = 4,   /* output buffer too small; n_required is set, n_written is 0 */
   HBX_ERR_WATCHDOG = 5,   /* a device loop exceeded its time budget and stopped */
   HBX_ERR_PARSE = 6,      /* malformed CSV or YAML rule */
   HBX_ERR_IO = 7,         /* file could not be read or written */
@@ -89,8 +89,9 @@ typedef struct hbx_columns {
   const int64_t* const* offsets;
 } hbx_columns;
 
-/* Output pair buffer.  hbx_session_run takes device pointers, hbx_block
- * host pointers. */
+/* Output pair buffer.  hbx_session_run takes device pointers, which the
+ * kernels write directly (after HBX_ERR_CAPACITY their contents are
+ * undefined); hbx_block takes host pointers, untouched on HBX_ERR_CAPACITY. */
 typedef struct hbx_pairs {
   uint32_t* l_row;
   uint32_t* r_row;

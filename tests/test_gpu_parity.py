@@ -126,7 +126,7 @@ def test_session_reuse_and_modes_agree(ctx, tmp_path):
         results.append(_util.sorted_pairs(p))
     for r in results[1:]:
         assert np.array_equal(r, results[0])
-    # too small a device buffer: CAPACITY with the required count, nothing partial
+    # too small a device buffer: CAPACITY with the required count, nothing reported written
     with pytest.raises(hb.HbxError) as e:
         s.run_device("batched", ol.data_ptr(), orr.data_ptr(), 3)
     assert e.value.status == hb.ERR_CAPACITY
