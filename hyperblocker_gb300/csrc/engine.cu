@@ -294,8 +294,7 @@ void setup_session(hbx_session* S, uint64_t h2d_tables) {
   S->d_rule_base.alloc(E.rules.size() + 1);
   S->d_ctr.alloc(1);
   // one page-locked counter block per context: its sessions run one at a time
-  if (!C->h_ctr)  // the counters, then the total of work items (u64)
-    HBX_CUDA(cudaHostAlloc(&C->h_ctr, sizeof(dev::Counters) + 8, cudaHostAllocPortable));
+  if (!C->h_ctr) HBX_CUDA(cudaHostAlloc(&C->h_ctr, sizeof(dev::Counters), cudaHostAllocPortable));
   S->h_ctr = static_cast<dev::Counters*>(C->h_ctr);
   const uint32_t tile = C->opts.tile_right > 0 ? (uint32_t)C->opts.tile_right : 128u;
   const int variant = C->opts.eval_variant > 0 ? C->opts.eval_variant - 1 : 1;
@@ -360,9 +359,12 @@ __global__ void k_gather_bounds(const dev::Rule* rules, uint32_t n_rules, uint32
 // Enqueues counter reset + the joins of every rule.  Returns launches.
 uint32_t enqueue_join(hbx_session* S, cudaStream_t st) {
   uint32_t launches = 0;
-  HBX_CUDA(cudaMemsetAsync(S->d_ctr.p, 0, sizeof(dev::Counters), st));
-  if (S->seen.p) HBX_CUDA(cudaMemsetAsync(S->seen.p, 0xff, S->seen.n * sizeof(unsigned long long), st));
-  HBX_CUDA(cudaMemsetAsync(S->counts.p, 0, S->counts.n * sizeof(uint32_t), st));
+  {  // counters, histograms and the duplicate set, one launch
+    const uint64_t n_seen = S->seen.p ? S->seen.n : 0;
+    const uint64_t n = std::max<uint64_t>(std::max<uint64_t>(S->counts.n, n_seen), 32);
+    dev::k_reset<<<row_grid(n, S->ctx->n_sm), 256, 0, st>>>(S->d_ctr.p, S->counts.p, S->counts.n,
+                                                            S->seen.p, n_seen);
+  }
   const uint32_t nL = S->side_l.n_rows, nR = S->side_r.n_rows;
   const int n_sm = S->ctx->n_sm;
   const uint32_t n_rules = (uint32_t)S->rb.size();
@@ -378,7 +380,7 @@ uint32_t enqueue_join(hbx_session* S, cudaStream_t st) {
     dev::k_join_scan_final<<<dim3(nb, 3, n_rules), 1024, 0, st>>>(S->d_rules.p, S->tile_right, nb,
                                                                   S->scan_totals.p);
     dev::k_join_scatter<<<grid, 256, 0, st>>>(S->side_l, S->side_r, S->d_rules.p, n_rules,
-                                               S->d_rule_base.p);
+                                               S->d_rule_base.p, &S->d_ctr.p->items_total);
     launch_check("join kernels");
     return 4;
   }
@@ -403,7 +405,8 @@ uint32_t enqueue_join(hbx_session* S, cudaStream_t st) {
     if (nR) dev::k_scatter<<<row_grid(nR, n_sm), 256, 0, st>>>(S->side_r, S->d_rules.p, (uint32_t)r, 1);
     launches += 9 + (nL ? 2 : 0) + (nR ? 2 : 0);
   }
-  dev::k_rule_base<<<1, 32, 0, st>>>(S->d_rules.p, n_rules, S->d_rule_base.p);
+  dev::k_rule_base<<<1, 32, 0, st>>>(S->d_rules.p, n_rules, S->d_rule_base.p,
+                                     &S->d_ctr.p->items_total);
   launches++;
   launch_check("join kernels");
   return launches;
@@ -500,16 +503,13 @@ uint64_t needed_capacity(const hbx_session* S, const dev::Counters& c) {
   return std::max<uint64_t>(need, S->out_l.n + 1);
 }
 
-// Queues the copies of the counters and of the work-item total into the
-// context's page-locked block (a graph node each when captured).
+// Queues the copy of the counters (with the run's work-item total) into the
+// context's page-locked block (a graph node when captured).
 void queue_counters(hbx_session* S, cudaStream_t st) {
   HBX_CUDA(cudaMemcpyAsync(S->h_ctr, S->d_ctr.p, sizeof(dev::Counters), cudaMemcpyDeviceToHost, st));
-  HBX_CUDA(cudaMemcpyAsync(S->h_ctr + 1, S->d_rule_base.p + S->rb.size(), 8, cudaMemcpyDeviceToHost, st));
 }
 
-unsigned long long items_total(const hbx_session* S) {
-  return *reinterpret_cast<const unsigned long long*>(S->h_ctr + 1);
-}
+unsigned long long items_total(const hbx_session* S) { return S->h_ctr->items_total; }
 
 dev::Counters read_counters(hbx_session* S, cudaStream_t st) {
   queue_counters(S, st);

@@ -315,7 +315,7 @@ __global__ void k_join_scan_final(const Rule* rules, uint32_t tile_right, uint32
 // Rows of every rule grouped by key (counting-sort scatter, right rows with
 // their first similarity column's metadata), and the rules' item bases.
 __global__ void k_join_scatter(Side L, Side R, const Rule* rules, uint32_t n_rules,
-                               unsigned long long* rule_base) {
+                               unsigned long long* rule_base, unsigned long long* items_total) {
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     unsigned long long acc = 0;
     for (uint32_t r = 0; r < n_rules; r++) {
@@ -323,6 +323,7 @@ __global__ void k_join_scatter(Side L, Side R, const Rule* rules, uint32_t n_rul
       acc += rules[r].item_off[rules[r].domain_l];
     }
     rule_base[n_rules] = acc;
+    if (items_total) *items_total = acc;
   }
   const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x;
@@ -342,7 +343,8 @@ __global__ void k_join_scatter(Side L, Side R, const Rule* rules, uint32_t n_rul
   }
 }
 
-__global__ void k_rule_base(const Rule* rules, uint32_t n_rules, unsigned long long* base) {
+__global__ void k_rule_base(const Rule* rules, uint32_t n_rules, unsigned long long* base,
+                            unsigned long long* items_total) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
     unsigned long long acc = 0;
     for (uint32_t r = 0; r < n_rules; r++) {
@@ -350,7 +352,18 @@ __global__ void k_rule_base(const Rule* rules, uint32_t n_rules, unsigned long l
       acc += rules[r].item_off[rules[r].domain_l];
     }
     base[n_rules] = acc;
+    if (items_total) *items_total = acc;
   }
+}
+
+__global__ void k_reset(Counters* ctr, uint32_t* counts, uint64_t n_counts,
+                        unsigned long long* seen, uint64_t n_seen) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t t0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  constexpr uint64_t kCtrWords = sizeof(Counters) / 8;
+  for (uint64_t i = t0; i < kCtrWords; i += stride) reinterpret_cast<unsigned long long*>(ctr)[i] = 0;
+  for (uint64_t i = t0; i < n_counts; i += stride) counts[i] = 0;
+  for (uint64_t i = t0; i < n_seen; i += stride) seen[i] = ~0ull;
 }
 
 // =====================================================================

@@ -217,6 +217,7 @@ struct Counters {
   unsigned long long passes;  // rule-level passes before de-duplication (plans with several rules)
   unsigned long long scans;       // pairs that reached a bit-parallel scan
   unsigned long long scan_steps;  // scan steps of 4 symbols
+  unsigned long long items_total; // work items of the run (written by the join)
 };
 
 struct EvalParams {
@@ -275,7 +276,12 @@ __global__ void k_items_partial(const Rule* rules, uint32_t rule, uint32_t tile_
 __global__ void k_scan_top_u64(unsigned long long* partial, uint32_t nb);
 __global__ void k_items_final(const Rule* rules, uint32_t rule, uint32_t tile_right,
                               const unsigned long long* partial);
-__global__ void k_rule_base(const Rule* rules, uint32_t n_rules, unsigned long long* base);
+__global__ void k_rule_base(const Rule* rules, uint32_t n_rules, unsigned long long* base,
+                            unsigned long long* items_total);
+// One launch for a run's resets: the counters and histograms to 0, the
+// duplicate set (n_seen slots, may be 0) to empty.
+__global__ void k_reset(Counters* ctr, uint32_t* counts, uint64_t n_counts,
+                        unsigned long long* seen, uint64_t n_seen);
 // fused join (every rule's left key domain <= kFusedJoinMaxDomain); k_join_count
 // takes min(max domain, kSharedHistKeys) * 4 bytes of dynamic shared memory
 constexpr uint32_t kFusedJoinMaxDomain = 1u << 16;
@@ -286,7 +292,7 @@ __global__ void k_join_scan_totals(const Rule* rules, uint32_t tile_right, uint3
 __global__ void k_join_scan_final(const Rule* rules, uint32_t tile_right, uint32_t nb_max,
                                   const unsigned long long* totals);
 __global__ void k_join_scatter(Side L, Side R, const Rule* rules, uint32_t n_rules,
-                               unsigned long long* rule_base);
+                               unsigned long long* rule_base, unsigned long long* items_total);
 // ------------------------------------------------------------------ evaluation
 // Peq tables of every left string of n_slots string slots (PeqShape).
 __global__ void k_peq_build(Side L, uint32_t n_slots, PeqShape shape, uint32_t* peq);

@@ -786,7 +786,7 @@ void launch_batch(hbx_server* S, Slot& B) {
     dev::k_items_final<<<I.nb_l, 1024, 0, st>>>(B.d_rules.p, i, S->tile_right, I.part_u64.p);
     if (n) k_scatter_left<<<grid_for(n, C->n_sm), 256, 0, st>>>(B.d_rules.p, i, row0, n, I.key_l.p);
   }
-  dev::k_rule_base<<<1, 32, 0, st>>>(B.d_rules.p, ni, B.d_base.p);
+  dev::k_rule_base<<<1, 32, 0, st>>>(B.d_rules.p, ni, B.d_base.p, nullptr);
   check_launch("serving batch join");
 
   B.capacity = std::max<uint64_t>(1 << 16, 2ull * N);

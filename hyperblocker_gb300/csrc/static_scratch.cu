@@ -287,7 +287,7 @@ void run_static(int device, const hbx_plan* plan, const hbx_table* left, const h
     if (nL) dev::k_scatter<<<grid_for(nL), 256, 0, st>>>(Y.L, Y.d_rules, ru, 0);
     if (nR) dev::k_scatter<<<grid_for(nR), 256, 0, st>>>(Y.R, Y.d_rules, ru, 1);
   }
-  dev::k_rule_base<<<1, 32, 0, st>>>(Y.d_rules, (uint32_t)Y.rules.size(), Y.rule_base);
+  dev::k_rule_base<<<1, 32, 0, st>>>(Y.d_rules, (uint32_t)Y.rules.size(), Y.rule_base, nullptr);
   const uint32_t n_slots = (uint32_t)E.L.str_maxlen.size();
   if (n_slots && nL)
     dev::k_peq_build<<<grid_for((uint32_t)std::min<uint64_t>((uint64_t)n_slots * nL * 32, 1u << 30)), 256, 0,
