@@ -883,6 +883,12 @@ void session_run(hbx_session* S, hbx_mode mode, cudaStream_t st) {
   fail(HBX_ERR_CAPACITY, "output kept growing");
 }
 
+void reserve_output(hbx_session* S, uint64_t pairs) {
+  PoolScope scope(S->ctx->pool, S->ctx->stream);
+  if (pairs > S->out_l.n) grow_output(S, pairs);
+  S->seen_pairs = std::max<uint64_t>(S->seen_pairs, pairs);
+}
+
 void run_to_host(hbx_session* S, hbx_mode mode, std::vector<uint32_t>* l, std::vector<uint32_t>* r) {
   cudaStream_t st = S->ctx->stream;
   S->one_shot = true;  // no graph for a single run

@@ -11,6 +11,10 @@ namespace hbx {
 // Runs a session (batched or plain) on its context's stream and copies its
 // pairs, exactly sized, into host vectors.
 void run_to_host(hbx_session* s, hbx_mode mode, std::vector<uint32_t>* l, std::vector<uint32_t>* r);
+// Grows a session's own output (and duplicate set) to at least `pairs`
+// slots before a run, so that a run expected to produce that many pairs
+// does not overflow and repeat.
+void reserve_output(hbx_session* s, uint64_t pairs);
 
 struct Table;
 // sort.cu: sorts n device pairs by (left row, right row) in place.

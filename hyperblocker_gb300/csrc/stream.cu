@@ -195,6 +195,9 @@ extern "C" hbx_status hbx_block_streamed(hbx_ctx* ctx, const hbx_plan* plan, con
     // ---- two workers, each with its own context and stream
     std::atomic<size_t> next{0};
     std::mutex mu;
+    // matches per pair covered in the windows done so far: sizes the next
+    // windows' output so that their runs do not overflow and repeat
+    double density = -1.0;
     hbx_status err = HBX_OK;
     std::string err_text;
     auto worker = [&](int id) {
@@ -242,6 +245,18 @@ extern "C" hbx_status hbx_block_streamed(hbx_ctx* ctx, const hbx_plan* plan, con
         hbx_stats ws{};
         if (st == HBX_OK) {
           try {
+            double d;
+            {
+              std::lock_guard<std::mutex> lock(mu);
+              d = density;
+            }
+            if (d >= 0) {
+              hbx_stats pre{};
+              hbx_session_stats(s, &pre);
+              const double want = 1.5 * d * (double)pre.pairs_covered + 4096.0;
+              const uint64_t cap = std::max<uint64_t>(window_bytes / 8, 1 << 16);
+              reserve_output(s, (uint64_t)std::min<double>(want, (double)cap));
+            }
             run_to_host(s, mode, &l, &r);
             hbx_session_stats(s, &ws);
           } catch (const Error& e) {
@@ -262,6 +277,8 @@ extern "C" hbx_status hbx_block_streamed(hbx_ctx* ctx, const hbx_plan* plan, con
           res_l.push_back(il[l[i]]);
           res_r.push_back(ir[r[i]]);
         }
+        if (ws.pairs_covered)
+          density = std::max(density, (double)l.size() / (double)ws.pairs_covered);
         agg.pair_comparisons += ws.pair_comparisons;
         agg.fma_ambiguous += ws.fma_ambiguous;
         agg.long_string_pairs += ws.long_string_pairs;
