@@ -2,8 +2,11 @@
 // reference's parameters, core/components/data_mngr.h:48-51) on the device.
 //
 // A line break always ends a row (no quoted line breaks), so rows are the
-// spans between '\n' bytes and tokenize independently: one thread per row
-// walks its bytes with the host loop's state machine (a '"' toggles the quote
+// spans between '\n' bytes and tokenize independently.  A warp takes 32
+// consecutive rows -- one contiguous span of the file -- and copies it into
+// shared memory with 16-byte loads (a span longer than the warp's staging
+// area is read from device memory instead); each lane then walks its row's
+// bytes with the host loop's state machine (a '"' toggles the quote
 // state when it is the first kept byte of the cell or the cell began with
 // '"'; the separator ends a cell outside quotes; '\r' is dropped), first to
 // measure every cell after unquoting ("..." -> ..., "" -> "), then, after a
@@ -26,6 +29,19 @@ namespace hbx {
 namespace csvd {
 
 constexpr uint32_t kChunk = 64;  // bytes per thread when finding line breaks
+constexpr uint32_t kRowThreads = 256;   // threads per block of the row kernels
+constexpr uint32_t kStageBytes = 8192;  // shared memory per warp for its rows' bytes
+
+// Byte source of the row walks: position `a` at s[0] -- the file in device
+// memory (a = 0) or a warp's staged copy of its rows (a = the first staged
+// position).  Bytes are read one at a time: a per-lane register window of
+// 16 bytes was slower, since the lanes of a warp cross their window
+// boundaries at different bytes and reload on nearly every step.
+struct Src {
+  const uint8_t* s;
+  uint64_t a;
+  __device__ __forceinline__ uint8_t operator()(uint64_t i) const { return s[i - a]; }
+};
 
 // Line breaks per 64-byte chunk of the buffer.
 __global__ void k_nl_count(const uint8_t* buf, uint64_t n, uint32_t n_chunks, uint32_t* cnt) {
@@ -52,13 +68,13 @@ __global__ void k_nl_write(const uint8_t* buf, uint64_t n, uint32_t n_chunks, co
 // For every cell up to n_cols: visit(cell index, first byte, end) with the
 // cell's raw span (still holding '\r' bytes).  Returns the cell count.
 template <class F>
-__device__ __forceinline__ uint32_t for_cells(const uint8_t* buf, uint64_t s, uint64_t e,
-                                              uint8_t sep, F&& visit) {
+__device__ __forceinline__ uint32_t for_cells(const Src& buf, uint64_t s, uint64_t e, uint8_t sep,
+                                              F&& visit) {
   uint32_t c = 0;
   uint64_t cs = s;
   bool quoted = false, empty = true, first_quote = false;
   for (uint64_t i = s; i < e; i++) {
-    const uint8_t ch = buf[i];
+    const uint8_t ch = buf(i);
     if (ch == '"') {
       if (empty || first_quote) quoted = !quoted;
       if (empty) first_quote = true;
@@ -83,12 +99,12 @@ __device__ __forceinline__ uint32_t for_cells(const uint8_t* buf, uint64_t s, ui
 }
 
 // Kept (non-'\r') bytes of a raw cell: count, first and last.
-__device__ __forceinline__ void kept(const uint8_t* buf, uint64_t a, uint64_t b, uint32_t* n,
+__device__ __forceinline__ void kept(const Src& buf, uint64_t a, uint64_t b, uint32_t* n,
                                      uint8_t* first, uint8_t* last) {
   uint32_t k = 0;
   uint8_t f = 0, l = 0;
   for (uint64_t i = a; i < b; i++) {
-    const uint8_t ch = buf[i];
+    const uint8_t ch = buf(i);
     if (ch == '\r') continue;
     if (k == 0) f = ch;
     l = ch;
@@ -102,19 +118,20 @@ __device__ __forceinline__ void kept(const uint8_t* buf, uint64_t a, uint64_t b,
 // Unquoted bytes of a raw cell (csv.cpp push_cell): when its kept bytes are
 // "...", the interior with "" read as "; else the kept bytes.  out == null:
 // only count.
-__device__ __forceinline__ uint32_t unquote(const uint8_t* buf, uint64_t a, uint64_t b,
-                                            uint8_t* out) {
+__device__ __forceinline__ uint32_t unquote(const Src& buf, uint64_t a, uint64_t b, uint8_t* out) {
   uint32_t n;
   uint8_t f, l;
   kept(buf, a, b, &n, &f, &l);
+  const bool enclosed = n >= 2 && f == '"' && l == '"';
+  if (!enclosed && !out) return n;  // the kept bytes as they are
   uint32_t w = 0;
-  if (n >= 2 && f == '"' && l == '"') {
+  if (enclosed) {
     // kept index j runs 1 .. n-2; a '"' followed by '"' with j + 2 < n
     // swallows the second
     uint32_t j = 0;
     bool skip = false;
     for (uint64_t i = a; i < b; i++) {
-      const uint8_t ch = buf[i];
+      const uint8_t ch = buf(i);
       if (ch == '\r') continue;
       const uint32_t jj = j++;
       if (jj == 0 || jj + 1 >= n) continue;  // the enclosing quotes
@@ -127,13 +144,13 @@ __device__ __forceinline__ uint32_t unquote(const uint8_t* buf, uint64_t a, uint
       if (ch == '"' && jj + 2 < n) {
         // look at the next kept byte
         uint64_t k = i + 1;
-        while (k < b && buf[k] == '\r') k++;
-        if (k < b && buf[k] == '"') skip = true;
+        while (k < b && buf(k) == '\r') k++;
+        if (k < b && buf(k) == '"') skip = true;
       }
     }
   } else {
     for (uint64_t i = a; i < b; i++) {
-      const uint8_t ch = buf[i];
+      const uint8_t ch = buf(i);
       if (ch == '\r') continue;
       if (out) out[w] = ch;
       w++;
@@ -155,35 +172,75 @@ __device__ __forceinline__ void row_span(const Rows& R, uint64_t r, uint64_t* s,
   *e = r < R.n_nl ? R.nl[r] : R.end;
 }
 
+// Copies the bytes of rows [r0, r0 + 32) -- positions [*a, ...) rounded out
+// to 16 bytes -- into the warp's staging area; false (nothing copied) when
+// they do not fit.  The file buffer is padded to a multiple of 16 bytes.
+__device__ __forceinline__ bool stage_rows(const uint8_t* buf, const Rows& R, uint64_t r0,
+                                           uint32_t lane, uint8_t* stage, uint64_t* a) {
+  const uint64_t r1 = min(r0 + 32, R.n_rows) - 1;
+  uint64_t s0, e0, s1, e1;
+  row_span(R, r0, &s0, &e0);
+  row_span(R, r1, &s1, &e1);
+  const uint64_t lo = s0 & ~15ull, hi = (e1 + 15) & ~15ull;
+  if (hi - lo > kStageBytes) return false;
+  const uint4* src = reinterpret_cast<const uint4*>(buf + lo);
+  uint4* dst = reinterpret_cast<uint4*>(stage);
+  for (uint32_t k = lane; k < (uint32_t)((hi - lo) >> 4); k += 32) dst[k] = src[k];
+  __syncwarp();
+  *a = lo;
+  return true;
+}
+
+// Warps over groups of 32 rows: f(source, row) for every row, from the
+// staged copy when it fits.
+template <class F>
+__device__ __forceinline__ void for_row_groups(const uint8_t* buf, const Rows& R, F&& f) {
+  extern __shared__ uint4 s_stage[];
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  uint8_t* stage = reinterpret_cast<uint8_t*>(s_stage) + (size_t)warp * kStageBytes;
+  const uint64_t n_warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+  for (uint64_t w = (uint64_t)blockIdx.x * (blockDim.x >> 5) + warp; w * 32 < R.n_rows;
+       w += n_warps) {
+    const uint64_t r = w * 32 + lane;
+    uint64_t a = 0;
+    if (stage_rows(buf, R, w * 32, lane, stage, &a)) {
+      if (r < R.n_rows) f(Src{stage, a}, r);
+    } else if (r < R.n_rows) {
+      f(Src{buf, 0}, r);
+    }
+    __syncwarp();  // the staging area is rewritten next
+  }
+}
+
 // Pass 1: unquoted length of every cell [col][row]; rows with fewer cells
 // than n_cols report (row << 32 | cells) into *short_row (smallest wins).
-__global__ void k_measure(const uint8_t* buf, Rows R, uint8_t sep, uint32_t n_cols, uint32_t* len,
-                          unsigned long long* short_row) {
-  for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < R.n_rows;
-       r += (uint64_t)gridDim.x * blockDim.x) {
+__global__ void __launch_bounds__(kRowThreads) k_measure(const uint8_t* buf, Rows R, uint8_t sep,
+                                                         uint32_t n_cols, uint32_t* len,
+                                                         unsigned long long* short_row) {
+  for_row_groups(buf, R, [&](const Src& B, uint64_t r) {
     uint64_t s, e;
     row_span(R, r, &s, &e);
-    const uint32_t cells = for_cells(buf, s, e, sep, [&](uint32_t c, uint64_t a, uint64_t b) {
-      if (c < n_cols) len[(uint64_t)c * R.n_rows + r] = unquote(buf, a, b, nullptr);
+    const uint32_t cells = for_cells(B, s, e, sep, [&](uint32_t c, uint64_t a, uint64_t b) {
+      if (c < n_cols) len[(uint64_t)c * R.n_rows + r] = unquote(B, a, b, nullptr);
     });
     if (cells < n_cols) {
       for (uint32_t c = cells; c < n_cols; c++) len[(uint64_t)c * R.n_rows + r] = 0;
       atomicMin(short_row, ((unsigned long long)r << 32) | cells);
     }
-  }
+  });
 }
 
 // Pass 2: the cells into their columns' arenas.
-__global__ void k_write(const uint8_t* buf, Rows R, uint8_t sep, uint32_t n_cols,
-                        const uint32_t* off, uint8_t* const* arena) {
-  for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < R.n_rows;
-       r += (uint64_t)gridDim.x * blockDim.x) {
+__global__ void __launch_bounds__(kRowThreads) k_write(const uint8_t* buf, Rows R, uint8_t sep,
+                                                       uint32_t n_cols, const uint32_t* off,
+                                                       uint8_t* const* arena) {
+  for_row_groups(buf, R, [&](const Src& B, uint64_t r) {
     uint64_t s, e;
     row_span(R, r, &s, &e);
-    for_cells(buf, s, e, sep, [&](uint32_t c, uint64_t a, uint64_t b) {
-      if (c < n_cols) unquote(buf, a, b, arena[c] + off[(uint64_t)c * R.n_rows + r]);
+    for_cells(B, s, e, sep, [&](uint32_t c, uint64_t a, uint64_t b) {
+      if (c < n_cols) unquote(B, a, b, arena[c] + off[(uint64_t)c * R.n_rows + r]);
     });
-  }
+  });
 }
 
 // Exclusive u32 offsets of one column (plus its total) as int64.
@@ -214,7 +271,7 @@ bool table_from_buffer_device(hbx_ctx* C, const char* data, size_t n, char sep, 
   cudaStream_t st = C->stream;
   PoolScope scope(C->pool, st);
   DBuf<uint8_t> buf;
-  buf.alloc(std::max<size_t>(m, 16));
+  buf.alloc(((m + 15) & ~(size_t)15) + 16);  // the row kernels read whole 16-byte words
   HBX_CUDA(cudaMemcpyAsync(buf.p, p, m, cudaMemcpyHostToDevice, st));
   const uint64_t n_chunks64 = (m + csvd::kChunk - 1) / csvd::kChunk;
   if (n_chunks64 >= (1ull << 32)) return false;
@@ -250,8 +307,14 @@ bool table_from_buffer_device(hbx_ctx* C, const char* data, size_t n, char sep, 
   DBuf<unsigned long long> short_row;
   short_row.alloc(1);
   HBX_CUDA(cudaMemsetAsync(short_row.p, 0xff, 8, st));
-  const int gr = grid_for(rows, C->n_sm);
-  csvd::k_measure<<<gr, 256, 0, st>>>(buf.p, R, (uint8_t)sep, n_cols, len.p, short_row.p);
+  const size_t stage_smem = (size_t)(csvd::kRowThreads / 32) * csvd::kStageBytes;
+  for (const void* k : {(const void*)csvd::k_measure, (const void*)csvd::k_write})
+    HBX_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)stage_smem));
+  const int gr = (int)std::max<uint64_t>(
+      1, std::min<uint64_t>((rows + csvd::kRowThreads - 1) / csvd::kRowThreads,
+                            (uint64_t)C->n_sm * 3));
+  csvd::k_measure<<<gr, csvd::kRowThreads, stage_smem, st>>>(buf.p, R, (uint8_t)sep, n_cols, len.p,
+                                                            short_row.p);
   check_launch("csv measure");
   // per column: exclusive offsets and total bytes
   std::vector<unsigned long long> totals(n_cols);
@@ -283,7 +346,8 @@ bool table_from_buffer_device(hbx_ctx* C, const char* data, size_t n, char sep, 
   }
   DBuf<uint8_t*> d_arena;
   d_arena.upload(arena_ptr, st);
-  csvd::k_write<<<gr, 256, 0, st>>>(buf.p, R, (uint8_t)sep, n_cols, off.p, d_arena.p);
+  csvd::k_write<<<gr, csvd::kRowThreads, stage_smem, st>>>(buf.p, R, (uint8_t)sep, n_cols, off.p,
+                                                          d_arena.p);
   check_launch("csv write");
   DBuf<int64_t> off64;
   off64.alloc(rows + 1);

@@ -358,7 +358,7 @@ __global__ void k_gather_bounds(const dev::Rule* rules, uint32_t n_rules, uint32
 
 // Enqueues counter reset + the joins of every rule.  Returns launches.
 uint32_t enqueue_join(hbx_session* S, cudaStream_t st) {
-  uint32_t launches = 0;
+  uint32_t launches = 1;  // k_reset
   {  // counters, histograms and the duplicate set, one launch
     const uint64_t n_seen = S->seen.p ? S->seen.n : 0;
     const uint64_t n = std::max<uint64_t>(std::max<uint64_t>(S->counts.n, n_seen), 32);
@@ -372,17 +372,25 @@ uint32_t enqueue_join(hbx_session* S, cudaStream_t st) {
     uint32_t max_d = 1;
     for (const dev::Rule& d : S->h_rules) max_d = std::max(max_d, d.domain_l);
     const size_t smem = std::min<uint32_t>(max_d, dev::kSharedHistKeys) * sizeof(uint32_t);
-    const int grid = row_grid(std::max(nL, nR), n_sm);
+    // rows per block row: each (rule, table) pair gets its own blocks
+    const dim3 grid(row_grid(std::max(nL, nR), n_sm), n_rules, 2);
     const uint32_t nb = (max_d + dev::kScanChunk - 1) / dev::kScanChunk;
-    dev::k_join_count<<<grid, 256, smem, st>>>(S->side_l, S->side_r, S->d_rules.p, n_rules);
-    dev::k_join_scan_totals<<<dim3(nb, 3, n_rules), 1024, 0, st>>>(
-        S->d_rules.p, S->tile_right, nb, S->scan_totals.p, &S->d_ctr.p->comparisons);
-    dev::k_join_scan_final<<<dim3(nb, 3, n_rules), 1024, 0, st>>>(S->d_rules.p, S->tile_right, nb,
-                                                                  S->scan_totals.p);
+    unsigned long long* comparisons = &S->d_ctr.p->comparisons;
+    dev::k_join_count<<<grid, 256, smem, st>>>(S->side_l, S->side_r, S->d_rules.p);
+    const bool two_pass = nb > dev::kJoinScanLoopChunks;
+    if (two_pass) {
+      dev::k_join_scan_totals<<<dim3(nb, 3, n_rules), 1024, 0, st>>>(
+          S->d_rules.p, S->tile_right, nb, S->scan_totals.p, comparisons);
+      dev::k_join_scan_final<<<dim3(nb, 3, n_rules), 1024, 0, st>>>(
+          S->d_rules.p, S->tile_right, nb, S->scan_totals.p, nullptr);
+    } else {  // one block per (y, rule) walks the chunks
+      dev::k_join_scan_final<<<dim3(1, 3, n_rules), 1024, 0, st>>>(S->d_rules.p, S->tile_right, nb,
+                                                                   nullptr, comparisons);
+    }
     dev::k_join_scatter<<<grid, 256, 0, st>>>(S->side_l, S->side_r, S->d_rules.p, n_rules,
                                                S->d_rule_base.p, &S->d_ctr.p->items_total);
     launch_check("join kernels");
-    return 4;
+    return launches + (two_pass ? 4 : 3);
   }
   for (size_t r = 0; r < S->rb.size(); r++) {
     RuleBufs& b = S->rb[r];

@@ -178,42 +178,42 @@ __global__ void k_items_final(const Rule* rules, uint32_t rule, uint32_t tile_ri
 }
 
 // ---- fused join for small key domains (every rule's left key domain at most
-// kFusedJoinMaxDomain): one launch for keys + histograms, two for offsets +
-// work items (chunk totals, then each chunk's scan), one for the scatter,
-// each covering every rule and both tables.
+// kFusedJoinMaxDomain): one launch for keys + histograms, one or two for
+// offsets + work items (chunk totals when a domain spans several chunks,
+// then each chunk's scan), one for the scatter, each covering every rule
+// and both tables.  The row kernels run one block row per (rule, table)
+// (blockIdx.y = rule, blockIdx.z = table), so the rules' and tables'
+// dependent load -> atomic -> store chains run side by side.
 
 // Keys and key histograms of every rule for both tables; histograms of
 // domains up to kSharedHistKeys are kept per block in shared memory.
-__global__ void k_join_count(Side L, Side R, const Rule* rules, uint32_t n_rules) {
+__global__ void k_join_count(Side L, Side R, const Rule* rules) {
   extern __shared__ uint32_t s_cnt[];
+  const int side = blockIdx.z;
+  const Side& S = side ? R : L;
+  if ((unsigned long long)blockIdx.x * blockDim.x >= S.n_rows) return;  // whole block
   const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x;
-  for (uint32_t r = 0; r < n_rules; r++) {
-    const Rule& Q = rules[r];
-    for (int side = 0; side < 2; side++) {
-      const Side& S = side ? R : L;
-      const uint32_t D = side ? Q.domain : Q.domain_l;
-      uint32_t* keys = side ? Q.key_r : Q.key_l;
-      uint32_t* cnt = side ? Q.cnt_r : Q.cnt_l;
-      const bool split = !side && Q.n_wclass > 1;
-      const bool sh = D <= kSharedHistKeys;
-      if (sh) {
-        for (uint32_t k = threadIdx.x; k < D; k += blockDim.x) s_cnt[k] = 0;
-        __syncthreads();
-      }
-      for (uint32_t row = t0; row < S.n_rows; row += stride) {
-        uint32_t k = row_key(S, Q, row);
-        if (split) k += Q.domain * word_class(S.str_meta[(size_t)Q.wclass_slot * S.n_rows + row].loc.y);
-        keys[row] = k;
-        atomicAdd(sh ? s_cnt + k : cnt + k, 1u);
-      }
-      if (sh) {
-        __syncthreads();
-        for (uint32_t k = threadIdx.x; k < D; k += blockDim.x)
-          if (s_cnt[k]) atomicAdd(cnt + k, s_cnt[k]);
-        __syncthreads();
-      }
-    }
+  const Rule& Q = rules[blockIdx.y];
+  const uint32_t D = side ? Q.domain : Q.domain_l;
+  uint32_t* keys = side ? Q.key_r : Q.key_l;
+  uint32_t* cnt = side ? Q.cnt_r : Q.cnt_l;
+  const bool split = !side && Q.n_wclass > 1;
+  const bool sh = D <= kSharedHistKeys;
+  if (sh) {
+    for (uint32_t k = threadIdx.x; k < D; k += blockDim.x) s_cnt[k] = 0;
+    __syncthreads();
+  }
+  for (uint32_t row = t0; row < S.n_rows; row += stride) {
+    uint32_t k = row_key(S, Q, row);
+    if (split) k += Q.domain * word_class(S.str_meta[(size_t)Q.wclass_slot * S.n_rows + row].loc.y);
+    keys[row] = k;
+    atomicAdd(sh ? s_cnt + k : cnt + k, 1u);
+  }
+  if (sh) {
+    __syncthreads();
+    for (uint32_t k = threadIdx.x; k < D; k += blockDim.x)
+      if (s_cnt[k]) atomicAdd(cnt + k, s_cnt[k]);
   }
 }
 
@@ -222,7 +222,10 @@ __global__ void k_join_count(Side L, Side R, const Rule* rules, uint32_t n_rules
 // the rule's pair-comparison count (y = 2) -- in chunks of kScanChunk keys,
 // one block of 1024 threads per (chunk, y, rule): k_join_scan_totals writes
 // every chunk's total, k_join_scan_final adds the totals of the earlier
-// chunks to the chunk's own exclusive scan.
+// chunks to the chunk's own exclusive scan.  When every domain spans at most
+// kJoinScanLoopChunks chunks the totals pass is left out: one block per
+// (y, rule) scans the chunks in turn, carrying the running total, and also
+// sums the pair-comparison count.
 __device__ __forceinline__ uint32_t join_scan_domain(const Rule& Q, uint32_t y) {
   return y == 1 ? Q.domain : Q.domain_l;
 }
@@ -271,44 +274,62 @@ __global__ void k_join_scan_totals(const Rule* rules, uint32_t tile_right, uint3
 }
 
 __global__ void k_join_scan_final(const Rule* rules, uint32_t tile_right, uint32_t nb_max,
-                                  const unsigned long long* totals) {
+                                  const unsigned long long* totals,
+                                  unsigned long long* comparisons) {
   __shared__ unsigned long long s_w64[32];
   __shared__ unsigned long long s_t64;
   __shared__ unsigned long long s_base;
-  const uint32_t c = blockIdx.x, y = blockIdx.y, r = blockIdx.z;
+  const uint32_t y = blockIdx.y, r = blockIdx.z;
   const Rule& Q = rules[r];
   const uint32_t D = join_scan_domain(Q, y);
+  const bool loop = totals == nullptr;  // one block per (y, rule) takes every chunk in turn
+  uint32_t c = loop ? 0u : blockIdx.x;
   if ((unsigned long long)c * kScanChunk >= D) return;
-  const unsigned long long* tot = totals + ((size_t)r * 3 + y) * nb_max;
-  if (threadIdx.x < 32) {  // totals of the earlier chunks (at most 16 for the fused join)
-    unsigned long long t = 0;
-    for (uint32_t k = threadIdx.x; k < c; k += 32) t += tot[k];
+  unsigned long long base = 0;
+  if (!loop) {
+    const unsigned long long* tot = totals + ((size_t)r * 3 + y) * nb_max;
+    if (threadIdx.x < 32) {  // totals of the earlier chunks (at most 16 for the fused join)
+      unsigned long long t = 0;
+      for (uint32_t k = threadIdx.x; k < c; k += 32) t += tot[k];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(kFull, t, o);
-    if (threadIdx.x == 0) s_base = t;
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(kFull, t, o);
+      if (threadIdx.x == 0) s_base = t;
+    }
+    __syncthreads();
+    base = s_base;
   }
-  __syncthreads();
-  const unsigned long long base = s_base;
-  const uint32_t b = c * kScanChunk + threadIdx.x * 4u;
-  unsigned long long v[4], pairs = 0;
-  join_scan_values(Q, y, tile_right, b, D, v, &pairs);
-  unsigned long long ex =
-      block_excl_scan<unsigned long long>(v[0] + v[1] + v[2] + v[3], s_w64, &s_t64) + base;
-  if (y == 2) {
+  unsigned long long pairs_sum = 0;
+  for (;; c++) {
+    const uint32_t b = c * kScanChunk + threadIdx.x * 4u;
+    unsigned long long v[4], pairs = 0;
+    join_scan_values(Q, y, tile_right, b, D, v, &pairs);
+    pairs_sum += pairs;
+    unsigned long long ex =
+        block_excl_scan<unsigned long long>(v[0] + v[1] + v[2] + v[3], s_w64, &s_t64) + base;
+    const unsigned long long chunk_total = s_t64;
+    const bool last = (unsigned long long)(c + 1) * kScanChunk >= D;
+    if (y == 2) {
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
-      if (b + k < D) Q.item_off[b + k] = ex;
-      ex += v[k];
-    }
-    if ((unsigned long long)(c + 1) * kScanChunk >= D && threadIdx.x == 0)
-      Q.item_off[D] = base + s_t64;
-  } else {
-    uint32_t* off = y == 1 ? Q.off_r : Q.off_l;
+      for (int k = 0; k < 4; k++) {
+        if (b + k < D) Q.item_off[b + k] = ex;
+        ex += v[k];
+      }
+      if (last && threadIdx.x == 0) Q.item_off[D] = base + chunk_total;
+    } else {
+      uint32_t* off = y == 1 ? Q.off_r : Q.off_l;
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
-      if (b + k < D) off[b + k] = (uint32_t)ex;
-      ex += v[k];
+      for (int k = 0; k < 4; k++) {
+        if (b + k < D) off[b + k] = (uint32_t)ex;
+        ex += v[k];
+      }
     }
+    base += chunk_total;
+    if (!loop || last) break;
+  }
+  if (y == 2 && comparisons) {  // no totals pass ran: the comparison count is summed here
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) pairs_sum += __shfl_xor_sync(kFull, pairs_sum, o);
+    if ((threadIdx.x & 31) == 0 && pairs_sum) atomicAdd(comparisons, pairs_sum);
   }
 }
 
@@ -316,7 +337,7 @@ __global__ void k_join_scan_final(const Rule* rules, uint32_t tile_right, uint32
 // their first similarity column's metadata), and the rules' item bases.
 __global__ void k_join_scatter(Side L, Side R, const Rule* rules, uint32_t n_rules,
                                unsigned long long* rule_base, unsigned long long* items_total) {
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+  if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0) {
     unsigned long long acc = 0;
     for (uint32_t r = 0; r < n_rules; r++) {
       rule_base[r] = acc;
@@ -327,12 +348,13 @@ __global__ void k_join_scatter(Side L, Side R, const Rule* rules, uint32_t n_rul
   }
   const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x;
-  for (uint32_t r = 0; r < n_rules; r++) {
-    const Rule& Q = rules[r];
+  const Rule& Q = rules[blockIdx.y];
+  if (blockIdx.z == 0) {
     for (uint32_t row = t0; row < L.n_rows; row += stride) {
       const uint32_t k = Q.key_l[row];
       Q.sorted_l[Q.off_l[k] + atomicAdd(Q.cur_l + k, 1u)] = row;
     }
+  } else {
     const StrMeta* meta_in = R.str_meta + (size_t)Q.sim_r[0] * R.n_rows;
     for (uint32_t row = t0; row < R.n_rows; row += stride) {
       const uint32_t k = Q.key_r[row];

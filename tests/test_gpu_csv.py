@@ -66,6 +66,24 @@ def test_device_tokenizer_equals_host(ctx, tmp_path, sep, bom, tail):
         assert np.array_equal(hb_, db)
 
 
+def test_long_rows_read_from_device_memory(ctx, tmp_path):
+    """Groups of 32 rows longer than a warp's 8 KB staging area are walked
+    in device memory; they sit between short groups that are staged."""
+    rng = np.random.Generator(np.random.PCG64(11))
+    rows = _csv(rng, 40_000, 4, b",").split(b"\n")
+    for r in list(range(3200, 3264)) + list(range(20_031, 20_040)) + [39_999]:
+        long = b'"' + b"x," * int(rng.integers(200, 700)) + b'""y"'
+        rows[r] = long + b',"a,b",c\r,' + str(r).encode()
+    p = tmp_path / "t.csv"
+    p.write_bytes(b"\n".join(rows))
+    host = hb.Table.from_csv(str(p))
+    dev = hb.Table.from_csv(str(p), ",", ctx)
+    assert dev.n_rows == host.n_rows and dev.n_cols == host.n_cols
+    for (hb_, ho), (db, do) in zip(_columns(host), _columns(dev)):
+        assert np.array_equal(ho, do)
+        assert np.array_equal(hb_, db)
+
+
 def test_tail_of_carriage_returns_is_no_row(ctx, tmp_path):
     rng = np.random.Generator(np.random.PCG64(3))
     data = _csv(rng, 40_000, 3, b",") + b"\r\r"

@@ -108,6 +108,23 @@ def test_random_tables_against_oracle(ctx, seed):
         assert st.pairs_covered == want.pairs_covered
 
 
+@pytest.mark.parametrize("n_values", [500, 1500, 3000, 40000])
+def test_key_domains_across_scan_chunks(ctx, n_values):
+    """Left key domains (2 partitions x codes x 5 length classes) of 3, 8
+    and 15 scan chunks (chunk totals, then each chunk's scan) and beyond the
+    fused join's limit (per-rule join kernels); one-chunk domains are the
+    other tests' tables."""
+    cl, cr = _util.random_tables(7000 + n_values, 2000, 100_000, b"abc", 12, n_eq_values=n_values)
+    docs = [synth.rule_yaml([3], [(1, 0.6)]), synth.rule_yaml([3, 4], [(2, 0.7)])]
+    want = api.run_block(api.CTable(cl), api.CTable(cr), _oracle_plan(docs), 2, _util.INT_MAX)
+    assert len(want.pairs) > 100
+    for mode in MODES:
+        got, st = _engine_pairs(ctx, docs, cl, cr, 2, _util.INT_MAX, mode)
+        assert np.array_equal(got, want.pairs), mode
+        assert st.pair_comparisons == want.pair_comparisons
+        assert st.pairs_covered == want.pairs_covered
+
+
 def test_session_reuse_and_modes_agree(ctx, tmp_path):
     w, paths, _ = _util.materialize("c1", str(tmp_path))
     plan = hb.Plan.from_rule_dir(paths["rules"], ctx)
