@@ -6,13 +6,17 @@
 // consecutive rows -- one contiguous span of the file -- and copies it into
 // shared memory with 16-byte loads (a span longer than the warp's staging
 // area is read from device memory instead); each lane then walks its row's
-// bytes with the host loop's state machine (a '"' toggles the quote
+// bytes once with the host loop's state machine (a '"' toggles the quote
 // state when it is the first kept byte of the cell or the cell began with
-// '"'; the separator ends a cell outside quotes; '\r' is dropped), first to
-// measure every cell after unquoting ("..." -> ..., "" -> "), then, after a
-// scan of the lengths per column, to write the cells into column-major
-// arenas.  The table is then copied back into host columns, byte for byte
-// what table_from_buffer builds.
+// '"'; a separator other than '"' ends a cell outside quotes; '\r' is
+// dropped) and, in the same pass, keeps what unquoting needs: a cell whose
+// kept bytes are "..." reads as its interior with every run of k '"' in it
+// reading as ceil(k/2) of them (csv.cpp push_cell pairs "" -> " from the
+// left).  The first walk (k_measure) gives every cell's unquoted length
+// and whether it is enclosed; after a scan of the lengths per column the
+// second (k_write) writes the cells into column-major arenas.  The table is
+// then copied back into host columns, byte for byte what table_from_buffer
+// builds.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -62,101 +66,6 @@ __global__ void k_nl_write(const uint8_t* buf, uint64_t n, uint32_t n_chunks, co
     for (uint64_t i = a; i < b; i++)
       if (buf[i] == '\n') pos[k++] = i;
   }
-}
-
-// The cells of one row [s, e), '\r' bytes dropped, in the host loop's order.
-// For every cell up to n_cols: visit(cell index, first byte, end) with the
-// cell's raw span (still holding '\r' bytes).  Returns the cell count.
-template <class F>
-__device__ __forceinline__ uint32_t for_cells(const Src& buf, uint64_t s, uint64_t e, uint8_t sep,
-                                              F&& visit) {
-  uint32_t c = 0;
-  uint64_t cs = s;
-  bool quoted = false, empty = true, first_quote = false;
-  for (uint64_t i = s; i < e; i++) {
-    const uint8_t ch = buf(i);
-    if (ch == '"') {
-      if (empty || first_quote) quoted = !quoted;
-      if (empty) first_quote = true;
-      empty = false;
-    } else if (ch == sep) {
-      if (!quoted) {
-        visit(c++, cs, i);
-        cs = i + 1;
-        empty = true;
-        first_quote = false;
-      } else {
-        empty = false;
-      }
-    } else if (ch == '\r') {
-      // dropped
-    } else {
-      empty = false;
-    }
-  }
-  visit(c++, cs, e);
-  return c;
-}
-
-// Kept (non-'\r') bytes of a raw cell: count, first and last.
-__device__ __forceinline__ void kept(const Src& buf, uint64_t a, uint64_t b, uint32_t* n,
-                                     uint8_t* first, uint8_t* last) {
-  uint32_t k = 0;
-  uint8_t f = 0, l = 0;
-  for (uint64_t i = a; i < b; i++) {
-    const uint8_t ch = buf(i);
-    if (ch == '\r') continue;
-    if (k == 0) f = ch;
-    l = ch;
-    k++;
-  }
-  *n = k;
-  *first = f;
-  *last = l;
-}
-
-// Unquoted bytes of a raw cell (csv.cpp push_cell): when its kept bytes are
-// "...", the interior with "" read as "; else the kept bytes.  out == null:
-// only count.
-__device__ __forceinline__ uint32_t unquote(const Src& buf, uint64_t a, uint64_t b, uint8_t* out) {
-  uint32_t n;
-  uint8_t f, l;
-  kept(buf, a, b, &n, &f, &l);
-  const bool enclosed = n >= 2 && f == '"' && l == '"';
-  if (!enclosed && !out) return n;  // the kept bytes as they are
-  uint32_t w = 0;
-  if (enclosed) {
-    // kept index j runs 1 .. n-2; a '"' followed by '"' with j + 2 < n
-    // swallows the second
-    uint32_t j = 0;
-    bool skip = false;
-    for (uint64_t i = a; i < b; i++) {
-      const uint8_t ch = buf(i);
-      if (ch == '\r') continue;
-      const uint32_t jj = j++;
-      if (jj == 0 || jj + 1 >= n) continue;  // the enclosing quotes
-      if (skip) {
-        skip = false;
-        continue;
-      }
-      if (out) out[w] = ch;
-      w++;
-      if (ch == '"' && jj + 2 < n) {
-        // look at the next kept byte
-        uint64_t k = i + 1;
-        while (k < b && buf(k) == '\r') k++;
-        if (k < b && buf(k) == '"') skip = true;
-      }
-    }
-  } else {
-    for (uint64_t i = a; i < b; i++) {
-      const uint8_t ch = buf(i);
-      if (ch == '\r') continue;
-      if (out) out[w] = ch;
-      w++;
-    }
-  }
-  return w;
 }
 
 struct Rows {
@@ -212,34 +121,132 @@ __device__ __forceinline__ void for_row_groups(const uint8_t* buf, const Rows& R
   }
 }
 
-// Pass 1: unquoted length of every cell [col][row]; rows with fewer cells
-// than n_cols report (row << 32 | cells) into *short_row (smallest wins).
+// The host loop's cell rule, byte by byte: true when ch (not '\r') ends the
+// current cell; otherwise ch is one of the cell's kept bytes.
+struct CellRule {
+  bool quoted = false, empty = true, first_quote = false;
+  __device__ __forceinline__ bool ends_cell(uint8_t ch, uint8_t sep) {
+    if (ch != '"' && ch == sep && !quoted) {
+      empty = true;
+      first_quote = false;
+      return true;
+    }
+    if (ch == '"') {
+      if (empty || first_quote) quoted = !quoted;
+      if (empty) first_quote = true;
+    }
+    empty = false;
+    return false;
+  }
+};
+
+// Pass 1: unquoted length of every cell [col][row] and whether its kept
+// bytes are "..." (enclosed); rows with fewer cells than n_cols report
+// (row << 32 | cells) into *short_row (smallest wins).
 __global__ void __launch_bounds__(kRowThreads) k_measure(const uint8_t* buf, Rows R, uint8_t sep,
                                                          uint32_t n_cols, uint32_t* len,
+                                                         uint8_t* enclosed,
                                                          unsigned long long* short_row) {
   for_row_groups(buf, R, [&](const Src& B, uint64_t r) {
     uint64_t s, e;
     row_span(R, r, &s, &e);
-    const uint32_t cells = for_cells(B, s, e, sep, [&](uint32_t c, uint64_t a, uint64_t b) {
-      if (c < n_cols) len[(uint64_t)c * R.n_rows + r] = unquote(B, a, b, nullptr);
-    });
-    if (cells < n_cols) {
-      for (uint32_t c = cells; c < n_cols; c++) len[(uint64_t)c * R.n_rows + r] = 0;
-      atomicMin(short_row, ((unsigned long long)r << 32) | cells);
+    CellRule rule;
+    uint32_t c = 0;
+    // the current cell: kept bytes, first and last, the open run of '"'
+    // (and whether it began at the first kept byte), '"' swallowed by
+    // earlier runs
+    uint32_t n = 0, run = 0, swallowed = 0;
+    uint8_t first = 0, last = 0;
+    bool run_at_start = false;
+    auto end_cell = [&]() {
+      const uint64_t at = (uint64_t)c * R.n_rows + r;
+      const bool enc = n >= 2 && first == '"' && last == '"';
+      uint32_t w = n;
+      if (enc) {  // the open run holds the closing '"' (and the opening one)
+        const int k = (int)run - 1 - (run_at_start ? 1 : 0);
+        w = n - 2 - swallowed - (k > 0 ? (uint32_t)k / 2 : 0u);
+      }
+      len[at] = w;
+      enclosed[at] = enc ? 1 : 0;
+      c++;
+      n = run = swallowed = 0;
+      first = last = 0;
+      run_at_start = false;
+    };
+    for (uint64_t i = s; i < e && c < n_cols; i++) {
+      const uint8_t ch = B(i);
+      if (ch == '\r') continue;
+      if (rule.ends_cell(ch, sep)) {
+        end_cell();
+        continue;
+      }
+      if (n == 0) first = ch;
+      last = ch;
+      if (ch == '"') {
+        if (run == 0) run_at_start = n == 0;
+        run++;
+      } else if (run) {
+        swallowed += (run - (run_at_start ? 1u : 0u)) / 2;
+        run = 0;
+        run_at_start = false;
+      }
+      n++;
+    }
+    if (c < n_cols) end_cell();  // the row's last cell
+    if (c < n_cols) {
+      atomicMin(short_row, ((unsigned long long)r << 32) | c);
+      for (; c < n_cols; c++) {
+        len[(uint64_t)c * R.n_rows + r] = 0;
+        enclosed[(uint64_t)c * R.n_rows + r] = 0;
+      }
     }
   });
 }
 
-// Pass 2: the cells into their columns' arenas.
+// Pass 2: the cells into their columns' arenas: an enclosed cell's bytes
+// after the opening '"' until its length is reached, a '"' right after a
+// written '"' swallowed; any other cell's kept bytes.
 __global__ void __launch_bounds__(kRowThreads) k_write(const uint8_t* buf, Rows R, uint8_t sep,
                                                        uint32_t n_cols, const uint32_t* off,
+                                                       const uint32_t* len,
+                                                       const uint8_t* enclosed,
                                                        uint8_t* const* arena) {
   for_row_groups(buf, R, [&](const Src& B, uint64_t r) {
     uint64_t s, e;
     row_span(R, r, &s, &e);
-    for_cells(B, s, e, sep, [&](uint32_t c, uint64_t a, uint64_t b) {
-      if (c < n_cols) unquote(B, a, b, arena[c] + off[(uint64_t)c * R.n_rows + r]);
-    });
+    CellRule rule;
+    uint32_t c = 0, j = 0, w = 0, want = 0;
+    bool enc = false, pending = false;
+    uint8_t* out = nullptr;
+    auto open_cell = [&]() {
+      const uint64_t at = (uint64_t)c * R.n_rows + r;
+      out = arena[c] + off[at];
+      want = len[at];
+      enc = enclosed[at] != 0;
+      j = w = 0;
+      pending = false;
+    };
+    open_cell();
+    for (uint64_t i = s; i < e; i++) {
+      const uint8_t ch = B(i);
+      if (ch == '\r') continue;
+      if (rule.ends_cell(ch, sep)) {
+        if (++c >= n_cols) break;
+        open_cell();
+        continue;
+      }
+      const uint32_t jj = j++;
+      if (!enc) {
+        out[w++] = ch;
+      } else if (jj > 0 && w < want) {
+        if (ch == '"' && pending) {
+          pending = false;
+        } else {
+          out[w++] = ch;
+          pending = ch == '"';
+        }
+      }
+    }
   });
 }
 
@@ -304,6 +311,8 @@ bool table_from_buffer_device(hbx_ctx* C, const char* data, size_t n, char sep, 
   DBuf<uint32_t> len, off;
   len.alloc((size_t)n_cols * rows);
   off.alloc((size_t)n_cols * rows);
+  DBuf<uint8_t> encl;
+  encl.alloc((size_t)n_cols * rows);
   DBuf<unsigned long long> short_row;
   short_row.alloc(1);
   HBX_CUDA(cudaMemsetAsync(short_row.p, 0xff, 8, st));
@@ -314,7 +323,7 @@ bool table_from_buffer_device(hbx_ctx* C, const char* data, size_t n, char sep, 
       1, std::min<uint64_t>((rows + csvd::kRowThreads - 1) / csvd::kRowThreads,
                             (uint64_t)C->n_sm * 3));
   csvd::k_measure<<<gr, csvd::kRowThreads, stage_smem, st>>>(buf.p, R, (uint8_t)sep, n_cols, len.p,
-                                                            short_row.p);
+                                                            encl.p, short_row.p);
   check_launch("csv measure");
   // per column: exclusive offsets and total bytes
   std::vector<unsigned long long> totals(n_cols);
@@ -347,7 +356,7 @@ bool table_from_buffer_device(hbx_ctx* C, const char* data, size_t n, char sep, 
   DBuf<uint8_t*> d_arena;
   d_arena.upload(arena_ptr, st);
   csvd::k_write<<<gr, csvd::kRowThreads, stage_smem, st>>>(buf.p, R, (uint8_t)sep, n_cols, off.p,
-                                                          d_arena.p);
+                                                          len.p, encl.p, d_arena.p);
   check_launch("csv write");
   DBuf<int64_t> off64;
   off64.alloc(rows + 1);
