@@ -197,20 +197,30 @@ struct Inst {
   uint32_t req = 0;  // entry index within the batch
 };
 
+// Page-locked host buffer that grows by powers of two.  A buffer it
+// outgrows is kept until the slot closes: cudaFreeHost waits for the whole
+// device, which would stall every other batch in flight (and the old buffer
+// may still be the source or target of this slot's copies).  The kept
+// buffers add up to less than the current one.
 struct Pinned {
   void* p = nullptr;
   size_t n = 0;
+  std::vector<void*> retired;
+  Pinned() = default;
+  Pinned(const Pinned&) = delete;
+  Pinned& operator=(const Pinned&) = delete;
   ~Pinned() {
     if (p) cudaFreeHost(p);
+    for (void* q : retired) cudaFreeHost(q);
   }
   void ensure(size_t bytes) {
     if (bytes <= n) return;
-    if (p) cudaFreeHost(p);
-    p = nullptr;
-    n = 0;
     size_t want = 1 << 16;
     while (want < bytes) want *= 2;
-    HBX_CUDA(cudaHostAlloc(&p, want, cudaHostAllocPortable));
+    void* q = nullptr;
+    HBX_CUDA(cudaHostAlloc(&q, want, cudaHostAllocPortable));
+    if (p) retired.push_back(p);
+    p = q;
     n = want;
   }
 };
