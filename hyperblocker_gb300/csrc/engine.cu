@@ -72,7 +72,7 @@ struct hbx_session {
   hbx::DBuf<unsigned long long> seen;  // reported-pair set (plans with several rules)
   // key histograms and scatter cursors of every rule, one block: one memset
   hbx::DBuf<uint32_t> counts;
-  bool fused_join = false;  // every key domain small: the four-kernel join
+  bool fused_join = false;  // every key domain small: join kernels covering all rules
   hbx::DBuf<unsigned long long> scan_totals;  // fused join: chunk totals [rule][scan][chunk]
   hbx::DBuf<uint32_t> bound_idx;              // per rule, n_partitions + 1 key indices
   hbx::DBuf<unsigned long long> bound_val;    // item_off at those keys
