@@ -84,6 +84,28 @@ def test_long_rows_read_from_device_memory(ctx, tmp_path):
         assert np.array_equal(hb_, db)
 
 
+def test_runs_of_quotes_separators_and_carriage_returns(ctx, tmp_path):
+    """One column of cells drawn from '"', ',', '\r', 'a', 'b': runs of
+    quotes of every length, separators inside and outside quotes, carriage
+    returns between a quote and its pair; every row is valid with one
+    column (extra cells are ignored)."""
+    rng = np.random.Generator(np.random.PCG64(21))
+    alpha = np.frombuffer(b'"",\rab', dtype=np.uint8)
+    rows = [b"h"]
+    for _ in range(90_000):
+        rows.append(alpha[rng.integers(0, len(alpha), size=int(rng.integers(0, 28)))].tobytes())
+    data = b"\n".join(rows) + b"\n"
+    assert len(data) >= (1 << 20)
+    p = tmp_path / "t.csv"
+    p.write_bytes(data)
+    host = hb.Table.from_csv(str(p))
+    dev = hb.Table.from_csv(str(p), ",", ctx)
+    assert dev.n_rows == host.n_rows and dev.n_cols == host.n_cols == 1
+    (hb_, ho), (db, do) = host.column(0), dev.column(0)
+    assert np.array_equal(ho, do)
+    assert np.array_equal(hb_, db)
+
+
 def test_tail_of_carriage_returns_is_no_row(ctx, tmp_path):
     rng = np.random.Generator(np.random.PCG64(3))
     data = _csv(rng, 40_000, 3, b",") + b"\r\r"
