@@ -85,7 +85,7 @@ def test_long_rows_read_from_device_memory(ctx, tmp_path):
 
 
 def test_runs_of_quotes_separators_and_carriage_returns(ctx, tmp_path):
-    """One column of cells drawn from '"', ',', '\r', 'a', 'b': runs of
+    """One column of cells drawn from '"', ',', '\\r', 'a', 'b': runs of
     quotes of every length, separators inside and outside quotes, carriage
     returns between a quote and its pair; every row is valid with one
     column (extra cells are ignored)."""
