@@ -26,8 +26,9 @@ Jaro-Winkler pair evaluation and compaction of the matching pairs.
 At N=1 more workloads are measured and reported in the same line: ``c3``
 (1M x 1M rows, 8 rules, 64 Zipf-sized partitions: batched vs plain), ``c5``
 (long strings, one-shot vs partition windows streamed under a memory budget)
-and ``serving`` (10M resident right rows, a Poisson trace of left-record
-requests: p50/p99/p999 latency and pair-comparisons/s); ``--sections`` picks.
+``serving`` (10M resident right rows, a Poisson trace of left-record
+requests: p50/p99/p999 latency and pair-comparisons/s) and ``io`` (CSV
+tokenization and pair-file writing, device vs host); ``--sections`` picks.
 
 ``--impl reference`` times that CPU implementation alone and prints the same
 line with ``"impl": "reference"``.  With N > 1 GPUs (torchrun) every rank runs
@@ -356,6 +357,93 @@ def bench_serving(args, ctx):
                     "the trace"}
 
 
+def bench_io(args, ctx, dev):
+    """Ingest and output around the path, timed end to end (wall clock of
+    the C-ABI calls, best of args.io_reps):
+
+    * csv: a quoted CSV file of args.io_rows rows (the C3 schema, about 175
+      bytes a row) read into a table with a context (tokenized on the device,
+      csv_gpu.cu) and without one (the host tokenizer); columns compared.
+    * write: args.io_pairs (left row, right row) pairs of two tables of
+      args.io_rows rows written as id_l,id_r lines from device pairs
+      (hbx_write_pairs_device, lines formatted on the device) and from host
+      pairs by the host loop (hbx_write_pairs without a context); files
+      compared byte for byte."""
+    import numpy as np
+    import torch
+
+    import hyperblocker_gb300 as hb
+    from hyperblocker_gb300 import synth_big
+
+    reps = max(1, args.io_reps)
+
+    def best(fn):
+        ts, r = [], None
+        for _ in range(reps):
+            t = time.perf_counter()
+            r = fn()
+            ts.append(time.perf_counter() - t)
+        return min(ts), r
+
+    out = {}
+    with tempfile.TemporaryDirectory() as d:
+        w = synth_big.c3(args.io_rows, 1_000)
+        cols = w.left.cols
+        n = len(cols[0][1]) - 1
+        path = os.path.join(d, "l.csv")
+        with open(path, "wb") as f:
+            f.write(b"\n".join(b",".join(b'"' + bytes(b_[o[i]:o[i + 1]]) + b'"' for b_, o in cols)
+                               for i in range(n)) + b"\n")
+        del w, cols
+        size = os.path.getsize(path)
+        hb.Table.from_csv(path, ",", ctx)  # warm: page-in, pools
+        t_dev, D = best(lambda: hb.Table.from_csv(path, ",", ctx))
+        t_host, H = best(lambda: hb.Table.from_csv(path, ","))
+        same = D.n_rows == H.n_rows and all(
+            np.array_equal(H.column(c)[0], D.column(c)[0]) and
+            np.array_equal(H.column(c)[1], D.column(c)[1]) for c in range(H.n_cols))
+        out["csv"] = {"bytes": size, "rows": int(H.n_rows), "device_s": t_dev, "host_s": t_host,
+                      "device_gbs": size / t_dev / 1e9, "host_gbs": size / t_host / 1e9,
+                      "same_columns": bool(same)}
+        del D, H
+        os.remove(path)
+
+        m, nr = args.io_pairs, args.io_rows
+        ids = [b"id"] + [str(100_000_000 + i).encode() for i in range(nr)]
+        L = hb.Table.from_columns([ids, [b"x"] * (nr + 1)], ctx)
+        R = hb.Table.from_columns([ids, [b"x"] * (nr + 1)], ctx)
+        rng = np.random.Generator(np.random.PCG64(7))
+        pairs = np.stack([rng.integers(0, nr + 1, size=m), rng.integers(0, nr + 1, size=m)],
+                         axis=1).astype(np.uint32)
+        dl = torch.from_numpy(pairs[:, 0].astype(np.int32)).to(dev)
+        dr = torch.from_numpy(pairs[:, 1].astype(np.int32)).to(dev)
+        torch.cuda.synchronize(dev)
+        hp, dp = os.path.join(d, "host.txt"), os.path.join(d, "dev.txt")
+
+        def host_write():
+            if os.path.exists(hp):
+                os.remove(hp)
+            hb.write_pairs(L, R, pairs, hp)
+
+        def dev_write():
+            if os.path.exists(dp):
+                os.remove(dp)
+            hb.write_pairs_device(ctx, L, R, dl.data_ptr(), dr.data_ptr(), m, dp)
+
+        dev_write()  # warm
+        t_dev, _ = best(dev_write)
+        t_host, _ = best(host_write)
+        size = os.path.getsize(hp)
+        with open(hp, "rb") as fh, open(dp, "rb") as fd:
+            same = fh.read() == fd.read()
+        out["write"] = {"pairs": m, "text_bytes": size, "device_s": t_dev, "host_s": t_host,
+                        "device_gbs": size / t_dev / 1e9, "host_gbs": size / t_host / 1e9,
+                        "same_bytes": bool(same)}
+        del dl, dr
+    out["timing"] = f"wall clock of the calls, best of {reps}; files in a temporary directory"
+    return out
+
+
 def max_over_ranks(dist, values, device):
     """Element-wise maximum over the ranks of per-rank timings: the slowest
     replica sets the job's time (values unchanged without a process group)."""
@@ -514,6 +602,8 @@ def run_engine(args, rank, world, local_rank):
             extra["c5"] = bench_c5(args, ctx)
         if world == 1 and "serve" in args.sections:
             extra["serving"] = bench_serving(args, ctx)
+        if world == 1 and "io" in args.sections:
+            extra["io"] = bench_io(args, ctx, dev)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -558,7 +648,8 @@ def main():
     ap.add_argument("--sections", default="c3,serve",
                     help="extra measurements at N=1, comma separated: c3 (1M x 1M batching "
                          "workload), serve (resident-table serving trace), c5 (long strings, "
-                         "one-shot vs streamed partition windows; minutes); '' for none")
+                         "one-shot vs streamed partition windows; minutes), io (CSV "
+                         "tokenization and pair-file writing, device vs host); '' for none")
     ap.add_argument("--c3-rows", type=int, default=1_000_000)
     ap.add_argument("--c3-steps", type=int, default=2)
     ap.add_argument("--c5-rows", type=int, default=500_000)
@@ -566,6 +657,9 @@ def main():
     ap.add_argument("--serve-rows", type=int, default=10_000_000)
     ap.add_argument("--serve-requests", type=int, default=800)
     ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--io-rows", type=int, default=1_000_000)
+    ap.add_argument("--io-pairs", type=int, default=20_000_000)
+    ap.add_argument("--io-reps", type=int, default=3)
     args = ap.parse_args()
     args.sections = [x for x in args.sections.split(",") if x]
     if args.warmup < 3:
