@@ -130,3 +130,31 @@ def test_cli_rejects_unknown_flag(built):
     assert hb.run_cli(["run_hyperblocker_exec", "-no_such_flag=1"]) == 1
     assert hb.run_cli(["run_hyperblocker_exec", "-n_partitions=abc"]) == 1
     assert hb.run_cli(["run_hyperblocker_exec", "-hbx_mode=fast"]) == 1
+
+
+@pytest.mark.parametrize("argv", [
+    ["-data_l"],                               # string flag without its argument
+    ["-n_partitions"],                         # number flag without its argument
+    ["-n_partitions", "-1x"],
+    ["-read_header=maybe"],
+    ["-prefix_hash_pred_idx=3000000000"],      # above INT_MAX
+    ["-hbx_device=gpu0"],
+    ["stray_argument"],
+])
+def test_cli_flag_errors(built, argv):
+    """Malformed command lines end with exit code 1 before any device work."""
+    assert hb.run_cli(["run_hyperblocker_exec"] + argv) == 1
+
+
+@pytest.mark.parametrize("argv", [
+    ["-rule_dir", "/nonexistent/rules", "-n_partitions", "8", "-sep", ";"],
+    ["--rule_dir=/nonexistent/rules", "--n_partitions=0x10", "-read_header", "-scheduler=RR"],
+    ["-rule_dir=/nonexistent/rules", "-noread_header", "-prefix_hash_pred_idx", "2",
+     "-hbx_mode", "plain"],
+])
+def test_cli_accepts_gflags_forms(built, argv):
+    """-flag=value, --flag=value, -flag value, bare booleans and -noflag all
+    parse (gflags syntax, examples/run_hyperblocker.cu:22-31); the run then
+    stops at the missing rule directory (or at the context where there is
+    no GPU) with exit code 2, not at the flags."""
+    assert hb.run_cli(["run_hyperblocker_exec"] + argv) == 2
