@@ -184,6 +184,24 @@ def test_cli_drop_in(built, golden, tmp_path):
     assert len(open(out, "rb").read().splitlines()) == 2 * len(lines)  # append mode
 
 
+def test_reference_class_shape_writes_what_the_cli_writes(built, golden, tmp_path):
+    """hb.HyperBlocker(rule_dir, data_l, data_r, output, n_partitions).Run(),
+    the reference's class (core/hyperblocker.cuh:45-131), appends the same
+    lines as run_hyperblocker_exec: the golden pair set, in row order."""
+    w, paths, _ = _util.materialize("c1", str(tmp_path))
+    out_cls, out_cli = str(tmp_path / "cls.csv"), str(tmp_path / "cli.csv")
+    pairs = hb.HyperBlocker(paths["rules"], paths["left"], paths["right"], out_cls, 1).Run()
+    assert len(pairs) > 0
+    cmd = [hb.EXE_PATH, "-data_l", paths["left"], "-data_r", paths["right"], "-rule_dir",
+           paths["rules"], "-n_partitions", "1", "-o", out_cli]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = open(out_cls, "rb").read()
+    assert got == open(out_cli, "rb").read()
+    lines = sorted(tuple(x.split(b",", 1)) for x in got.splitlines())
+    assert _util.digest(lines) == golden["c1_order_0"]["sha256"]
+
+
 @pytest.mark.parametrize("tile", [32, 64, 128])
 @pytest.mark.parametrize("variant", [1, 2])
 def test_tile_shapes_and_kernel_variants_agree(built, tile, variant):
