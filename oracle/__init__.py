@@ -1,8 +1,8 @@
 """CPU oracle for the rule-based blocking hot path -- TEST INFRASTRUCTURE ONLY.
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline and
-reference legs import this package, and only as the checker or the timed CPU
-baseline.  The product (``hyperblocker_gb300``) never imports it.
+reference legs import this package, and only to check the engine's results or
+as the timed CPU baseline.  The product (``hyperblocker_gb300``) never imports it.
 
 Contents
 --------
