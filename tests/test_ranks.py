@@ -66,3 +66,15 @@ def test_reference_arm_runs_on_rank_zero_only():
     assert len(lines) == 1  # rank 1 prints nothing
     line = json.loads(lines[0])
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
+    # the line keeps the engine arm's metric, unit and direction, and carries
+    # the CPU baseline and end-to-end blocks that describe this run
+    import bench
+
+    assert line["metric"] == bench.METRIC and line["unit"] == bench.UNIT
+    assert line["higher_is_better"] is True and line["steps"] == 1 and line["warmup"] == 3
+    assert line["config"]["workload"] == bench.WORKLOAD_DESC
+    cb = line["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == line["value"] and cb["sample"]
+    e2e = line["e2e"]
+    assert e2e["value"] == line["value"] and e2e["unit"] == line["unit"]
+    assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
