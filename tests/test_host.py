@@ -158,3 +158,27 @@ def test_cli_accepts_gflags_forms(built, argv):
     stops at the missing rule directory (or at the context where there is
     no GPU) with exit code 2, not at the flags."""
     assert hb.run_cli(["run_hyperblocker_exec"] + argv) == 2
+
+
+def test_host_writer_lines(built, tmp_path):
+    """hbx_write_pairs without a context (the host loop) appends one
+    `id_l,id_r` line per pair, each id printed as a C string -- up to its
+    first NUL -- like WriteMatch (core/components/host_reducer.h:80-90);
+    commas and quotes inside ids are written as they are; a row index past
+    the table is refused."""
+    ids_l = [b"id", b"a1", b"x\x00hidden", b'"q,1"', b""]
+    ids_r = [b"id", b"r0", b"r,1", b"\x00", b"long" * 40]
+    L = hb.Table.from_columns([ids_l, [b"c"] * len(ids_l)])
+    R = hb.Table.from_columns([ids_r, [b"c"] * len(ids_r)])
+    pairs = np.array([[1, 1], [2, 2], [3, 3], [4, 4], [0, 0], [1, 4]], dtype=np.uint32)
+    out = tmp_path / "pairs.csv"
+    hb.write_pairs(L, R, pairs, str(out))
+    cut = lambda b: b.split(b"\x00", 1)[0]
+    want = b"".join(cut(ids_l[a]) + b"," + cut(ids_r[b]) + b"\n" for a, b in pairs)
+    assert out.read_bytes() == want
+    hb.write_pairs(L, R, pairs[:2], str(out))  # append mode
+    assert out.read_bytes() == want + want[:want.index(b"\n", want.index(b"\n") + 1) + 1]
+    with pytest.raises(hb.HbxError) as e:
+        hb.write_pairs(L, R, np.array([[5, 0]], dtype=np.uint32), str(tmp_path / "bad.csv"))
+    assert e.value.status == hb.ERR_INVALID_ARG
+
