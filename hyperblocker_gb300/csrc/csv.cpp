@@ -159,6 +159,7 @@ Table table_from_columns(const hbx_columns* cols) {
     const int64_t base = off[0];
     const int64_t total = off[cols->n_rows] - base;
     if (total < 0) fail(HBX_ERR_INVALID_ARG, "hbx_columns offsets decrease");
+    if (total > 0 && !cols->data[c]) fail(HBX_ERR_INVALID_ARG, "hbx_columns has a null column");
     col.bytes.assign(cols->data[c] + base, cols->data[c] + base + total);
     col.off.resize((size_t)cols->n_rows + 1);
     for (int64_t i = 0; i <= cols->n_rows; i++) {
