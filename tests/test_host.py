@@ -182,3 +182,18 @@ def test_host_writer_lines(built, tmp_path):
         hb.write_pairs(L, R, np.array([[5, 0]], dtype=np.uint32), str(tmp_path / "bad.csv"))
     assert e.value.status == hb.ERR_INVALID_ARG
 
+
+def test_column_ingest_refuses_bad_offsets(built):
+    """hbx_table_ingest checks the caller's offsets: decreasing offsets are
+    HBX_ERR_INVALID_ARG; offsets that do not start at 0 are taken relative to
+    their first entry; columns of different lengths never reach the C ABI."""
+    blob = np.frombuffer(b"abcdef", dtype=np.uint8)
+    with pytest.raises(hb.HbxError) as e:
+        hb.Table.from_columns([(blob, np.array([0, 3, 2, 6], dtype=np.int64))])
+    assert e.value.status == hb.ERR_INVALID_ARG
+    t = hb.Table.from_columns([(blob, np.array([2, 3, 6], dtype=np.int64))])
+    b, o = t.column(0)
+    assert bytes(b) == b"cdef" and list(o) == [0, 1, 4]
+    with pytest.raises(ValueError):
+        hb.Table.from_columns([[b"a", b"b"], [b"c"]])
+
