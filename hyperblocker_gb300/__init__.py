@@ -76,7 +76,9 @@ class Stats(ctypes.Structure):
                 ("h2d_bytes", ctypes.c_uint64), ("ms_create", ctypes.c_double),
                 ("ingest_on_device", ctypes.c_uint32), ("tile_right", ctypes.c_uint32),
                 ("eval_variant", ctypes.c_uint32), ("n_windows", ctypes.c_uint32),
-                ("pairs_scanned", ctypes.c_uint64), ("scan_steps", ctypes.c_uint64)]
+                ("pairs_scanned", ctypes.c_uint64), ("scan_steps", ctypes.c_uint64),
+                ("scan_word_ops", ctypes.c_uint64), ("scan_words", ctypes.c_uint32),
+                ("reserved0", ctypes.c_uint32)]
 
     def as_dict(self) -> Dict[str, float]:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -135,7 +137,7 @@ SIGNATURES = {
     "hbx_session_stats": (ctypes.c_int, [_VP, ctypes.POINTER(Stats)]),
     "hbx_session_destroy": (ctypes.c_int, [_VP]),
     "hbx_block": (ctypes.c_int, [_VP, _VP, _VP, _VP, ctypes.c_uint64, ctypes.c_int64, ctypes.c_int,
-                                 ctypes.POINTER(Pairs), ctypes.POINTER(Stats)]),
+                                 ctypes.POINTER(Pairs), ctypes.POINTER(Stats), _VP]),
     "hbx_write_pairs": (ctypes.c_int, [_VP, _VP, _VP, _VP, _VP, ctypes.c_uint64, ctypes.c_char_p]),
     "hbx_write_pairs_device": (ctypes.c_int, [_VP, _VP, _VP, _VP, _VP, ctypes.c_uint64,
                                               ctypes.c_char_p]),
@@ -457,7 +459,8 @@ class Session:
 
 
 def block(ctx: Context, plan: Plan, left: Table, right: Table, n_partitions: int = 1,
-          prefix_idx: int = INT_MAX, mode="batched", capacity: Optional[int] = None):
+          prefix_idx: int = INT_MAX, mode="batched", capacity: Optional[int] = None,
+          stream_ptr: Optional[int] = None):
     """Host tables -> (pairs (n, 2) uint32 of (left row, right row), stats).
 
     ``hbx_block`` writes nothing when the output buffer is too small (it
@@ -473,7 +476,7 @@ def block(ctx: Context, plan: Plan, left: Table, right: Table, n_partitions: int
         p = Pairs(ol.ctypes.data, orr.ctypes.data, capacity, 0, 0)
         s = Stats()
         st = lib().hbx_block(ctx.h, plan.h, left.h, right.h, n_partitions, prefix_idx, _mode(mode),
-                             ctypes.byref(p), ctypes.byref(s))
+                             ctypes.byref(p), ctypes.byref(s), stream_ptr)
         if st == ERR_CAPACITY:
             capacity = int(p.n_required)
             ctx._capacity_hint = max(getattr(ctx, "_capacity_hint", 0), capacity + capacity // 4)

@@ -19,12 +19,14 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libhbx.so")
+PROBE_LIB = os.path.join(OUT, "libhbx_probe.so")  # measurement probes (bench.py only)
 EXE = os.path.join(OUT, "run_hyperblocker_exec")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 CU_SOURCES = ["kernels.cu", "engine.cu", "ingest.cu", "serve.cu", "stream.cu", "static_scratch.cu",
               "writer.cu", "csv_gpu.cu", "sort.cu"]
 CPP_SOURCES = ["csv.cpp", "rules.cpp", "planner.cpp", "encode.cpp", "capi.cpp", "cli.cpp"]
+PROBE_SOURCES = ["probe.cu"]
 
 
 def _nvcc() -> str:
@@ -68,6 +70,14 @@ def build(force: bool = False, verbose: bool = False) -> str:
             jobs.append([nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                          "-Xptxas", "-v" if verbose else "-O3", "--expt-relaxed-constexpr",
                          "-c", src, "-o", obj])
+    probe_objs = []
+    for f in PROBE_SOURCES:
+        src = os.path.join(CSRC, f)
+        obj = os.path.join(OUT, f + ".o")
+        probe_objs.append(obj)
+        if force or _needs(obj, [src] + hdrs):
+            jobs.append([nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+                         "-Xptxas", "-v" if verbose else "-O3", "-c", src, "-o", obj])
     for f in CPP_SOURCES:
         src = os.path.join(CSRC, f)
         obj = os.path.join(OUT, f + ".o")
@@ -85,6 +95,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
         _compile([nvcc, ARCH, "-shared", "-o", LIB + ".tmp"] + objs +
                  ["-lpthread", "-ldl", "-lrt"])
         os.replace(LIB + ".tmp", LIB)
+    if force or _needs(PROBE_LIB, probe_objs):
+        _compile([nvcc, ARCH, "-shared", "-o", PROBE_LIB + ".tmp"] + probe_objs)
+        os.replace(PROBE_LIB + ".tmp", PROBE_LIB)
     exe_src = os.path.join(CSRC, "run_hyperblocker_exec.cpp")
     if force or _needs(EXE, [LIB, exe_src]):
         _compile(["g++", "-std=c++17", "-O2", exe_src, "-o", EXE + ".tmp", "-L", OUT, "-lhbx",

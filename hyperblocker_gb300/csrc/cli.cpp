@@ -179,7 +179,7 @@ extern "C" int hbx_run_cli(int argc, const char* const* argv) {
         out.r_row = orr.data();
         out.capacity = ol.size();
         s = hbx_block(ctx, plan, L, R, F.n_partitions, (int64_t)F.prefix_hash_pred_idx, mode, &out,
-                      &st);
+                      &st, nullptr);
         if (s == HBX_ERR_CAPACITY) {
           ol.resize(out.n_required);
           orr.resize(out.n_required);

@@ -856,6 +856,10 @@ void session_run(hbx_session* S, hbx_mode mode, cudaStream_t st) {
     S->stats.n_launches = launches;
     S->stats.pairs_scanned = c.scans;
     S->stats.scan_steps = c.scan_steps;
+    // a scan step is 4 characters over peq_shape.w 32-bit mask words, 3
+    // operations per 32-bit word per character (6 per 64-bit word)
+    S->stats.scan_word_ops = c.scan_steps * 4ull * 3ull * S->peq_shape.w;
+    S->stats.scan_words = S->peq_shape.w;
     S->stats.tile_right = S->tile_right;
     S->stats.n_windows = 1;
     S->stats.eval_variant = (uint32_t)S->variant + 1;
@@ -1052,7 +1056,7 @@ hbx_status hbx_session_destroy(hbx_session* s) {
 
 hbx_status hbx_block(hbx_ctx* ctx, const hbx_plan* plan, const hbx_table* left,
                      const hbx_table* right, uint64_t n_partitions, int64_t prefix_idx,
-                     hbx_mode mode, hbx_pairs* out, hbx_stats* stats) {
+                     hbx_mode mode, hbx_pairs* out, hbx_stats* stats, void* stream) {
   if (!ctx || !out) return HBX_ERR_INVALID_ARG;
   if (!plan || !left || !right) return HBX_ERR_INVALID_ARG;
   auto S = std::make_unique<hbx_session>();
@@ -1067,8 +1071,11 @@ hbx_status hbx_block(hbx_ctx* ctx, const hbx_plan* plan, const hbx_table* left,
       hbx::fail(HBX_ERR_INVALID_ARG, "prefix_idx out of range");
     HBX_CUDA(cudaSetDevice(ctx->device));
     hbx::PoolScope scope(ctx->pool, ctx->stream);
+    // the session is encoded on the context's stream (its creation ends with
+    // that stream idle); the run and the copies go to the caller's stream
     hbx::create_session(s, plan, left, right, n_partitions, prefix_idx);
-    hbx::session_run(s, mode, ctx->stream);
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    hbx::session_run(s, mode, st);
     const uint64_t n = s->stats.n_matches;
     out->n_required = n;
     out->n_written = 0;
@@ -1088,9 +1095,9 @@ hbx_status hbx_block(hbx_ctx* ctx, const hbx_plan* plan, const hbx_table* left,
         ctx->h_out_n = want;
       }
       uint32_t* hl = static_cast<uint32_t*>(ctx->h_out);
-      HBX_CUDA(cudaMemcpyAsync(hl, s->out_l.p, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
-      HBX_CUDA(cudaMemcpyAsync(hl + n, s->out_r.p, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
-      HBX_CUDA(cudaStreamSynchronize(ctx->stream));
+      HBX_CUDA(cudaMemcpyAsync(hl, s->out_l.p, n * 4, cudaMemcpyDeviceToHost, st));
+      HBX_CUDA(cudaMemcpyAsync(hl + n, s->out_r.p, n * 4, cudaMemcpyDeviceToHost, st));
+      HBX_CUDA(cudaStreamSynchronize(st));
       std::memcpy(out->l_row, hl, n * 4);
       std::memcpy(out->r_row, hl + n, n * 4);
     }

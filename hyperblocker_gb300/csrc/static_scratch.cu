@@ -24,8 +24,11 @@
 //     several streams without ordering between them -- race and corrupt each
 //     other;
 //   * the first call on a device looks up the array's device address (once
-//     per device, with that device current); make that first call before any
-//     stream capture begins.
+//     per device and CUDA context, with that device current); make that
+//     first call before any stream capture begins.  A later call that finds
+//     another context current on the device (after cudaDeviceReset, say,
+//     which reloads the module and may move the array) looks it up again.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -48,8 +51,15 @@ constexpr int kMaxDevices = 64;
 // a device address: kernels get the address cudaGetSymbolAddress returns.
 static __device__ __align__(256) unsigned char g_scratch[kStaticScratchBytes];
 
+// The array's address on each device, with the id of the CUDA context it
+// was looked up in (0: the id could not be read; the address is then looked
+// up on every call, which allocates nothing once the module is loaded).
+struct ScratchAddr {
+  unsigned char* addr = nullptr;
+  unsigned long long ctx_id = 0;
+};
 std::mutex g_mu;
-unsigned char* g_scratch_addr[kMaxDevices] = {};
+ScratchAddr g_scratch_addr[kMaxDevices];
 thread_local std::string g_static_err;
 
 #define HBX_STATIC_CUDA(expr)                                                              \
@@ -59,15 +69,47 @@ thread_local std::string g_static_err;
       ::hbx::fail(HBX_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_));       \
   } while (0)
 
-// Device address of the scratch on the current device (looked up once).
+// Id of the current CUDA context (cuCtxGetCurrent + cuCtxGetId through the
+// runtime's driver entry points, so no link against the driver library); 0
+// when it cannot be read.
+unsigned long long current_context_id() {
+  using GetCurrent = CUresult (*)(CUcontext*);
+  using GetId = CUresult (*)(CUcontext, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static bool resolved = false;
+  if (!resolved) {  // under g_mu
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_current = (GetCurrent)f;
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_id = (GetId)f;
+    resolved = true;
+  }
+  CUcontext c = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&c) != CUDA_SUCCESS || !c) return 0;
+  if (get_id(c, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
+
+// Device address of the scratch on `device`, which is current: looked up
+// once per device and context.
 unsigned char* scratch_on(int device) {
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_scratch_addr[device]) {
+  const unsigned long long ctx = current_context_id();
+  ScratchAddr& a = g_scratch_addr[device];
+  if (!a.addr || ctx == 0 || a.ctx_id != ctx) {
     void* p = nullptr;
     HBX_STATIC_CUDA(cudaGetSymbolAddress(&p, g_scratch));
-    g_scratch_addr[device] = (unsigned char*)p;
+    a.addr = (unsigned char*)p;
+    a.ctx_id = ctx;
   }
-  return g_scratch_addr[device];
+  return a.addr;
 }
 
 // Bump allocation of 256-byte aligned pieces of the scratch.  A first pass
@@ -126,8 +168,9 @@ struct Layout {
   uint32_t tile_right = 128;
 };
 
-// Places every buffer; with c.base == nullptr it only measures.
-void place(Carve& c, const hbx::Encoded& E, uint64_t capacity, size_t smem_cap, Layout* Y,
+// Places every buffer; with c.base == nullptr it only measures.  The
+// duplicate set (plans with several rules) is placed last by place_seen.
+void place(Carve& c, const hbx::Encoded& E, size_t smem_cap, Layout* Y,
            const std::vector<hbx::dev::StrMeta>& ml, const std::vector<hbx::dev::StrMeta>& mr) {
   namespace dev = hbx::dev;
   const uint32_t nL = (uint32_t)E.L.n_rows, nR = (uint32_t)E.R.n_rows;
@@ -196,12 +239,26 @@ void place(Carve& c, const hbx::Encoded& E, uint64_t capacity, size_t smem_cap, 
   Y->d_rules = c.take<dev::Rule>(E.rules.size());
   Y->rule_base = c.take<unsigned long long>(E.rules.size() + 1);
   Y->ctr = c.take<dev::Counters>(1);
-  if (E.rules.size() > 1) {
-    unsigned long long slots = 1024;
-    while (slots < 2 * capacity) slots *= 2;
-    Y->seen_slots = slots;
-    Y->seen = c.take<unsigned long long>(slots);
-  }
+}
+
+// Slots of the duplicate set: twice the distinct pairs the call can report
+// (at most the caller's capacity, and at most the pairs the partitions hold),
+// rounded up to a power of two, but no more than what is left of the
+// scratch after the other buffers (`used` bytes).  A set that fills up
+// stops the run with HBX_ERR_CAPACITY (seen_overflow).
+unsigned long long seen_slots_for(const hbx::Encoded& E, uint64_t capacity, size_t used) {
+  if (E.rules.size() <= 1) return 0;
+  const uint64_t pairs = std::min<uint64_t>(capacity, E.pairs_covered);
+  unsigned long long slots = 1024;
+  while (slots < 2 * pairs) slots *= 2;
+  const size_t left = kStaticScratchBytes > used + 256 ? kStaticScratchBytes - used - 256 : 0;
+  while (slots > 1024 && slots * 8 > left) slots /= 2;
+  return slots;
+}
+
+void place_seen(Carve& c, Layout* Y, unsigned long long slots) {
+  Y->seen_slots = slots;
+  Y->seen = slots ? c.take<unsigned long long>(slots) : nullptr;
 }
 
 void run_static(int device, const hbx_plan* plan, const hbx_table* left, const hbx_table* right,
@@ -220,12 +277,20 @@ void run_static(int device, const hbx_plan* plan, const hbx_table* left, const h
   const uint32_t nL = (uint32_t)E.L.n_rows, nR = (uint32_t)E.R.n_rows;
   const std::vector<hbx::dev::StrMeta> ml = string_meta(E.L, nL), mr = string_meta(E.R, nR);
 
-  cudaDeviceProp prop;
-  HBX_STATIC_CUDA(cudaGetDeviceProperties(&prop, device));
-  const size_t smem_cap = std::min<size_t>(prop.sharedMemPerBlockOptin, 200 * 1024);
+  int n_sm = 0, smem_optin = 0;
+  HBX_STATIC_CUDA(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, device));
+  HBX_STATIC_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+  const size_t smem_cap = std::min<size_t>((size_t)smem_optin, 200 * 1024);
   Layout Y;
   Carve measure{nullptr};
-  place(measure, E, out->capacity, smem_cap, &Y, ml, mr);
+  place(measure, E, smem_cap, &Y, ml, mr);
+  if (measure.used > kStaticScratchBytes)
+    hbx::fail(HBX_ERR_INVALID_ARG,
+              "input needs " + std::to_string(measure.used) + " bytes of device scratch for its "
+              "encoding and join state; the static scratch holds " +
+              std::to_string(kStaticScratchBytes));
+  const unsigned long long seen_slots = seen_slots_for(E, out->capacity, measure.used);
+  place_seen(measure, &Y, seen_slots);
   if (measure.used > kStaticScratchBytes)
     hbx::fail(HBX_ERR_INVALID_ARG,
               "input needs " + std::to_string(measure.used) + " bytes of device scratch; the "
@@ -239,10 +304,23 @@ void run_static(int device, const hbx_plan* plan, const hbx_table* left, const h
     ~Restore() { cudaSetDevice(d); }
   } restore{prev};
   Carve carve{scratch_on(device)};
-  place(carve, E, out->capacity, smem_cap, &Y, ml, mr);
+  place(carve, E, smem_cap, &Y, ml, mr);
+  place_seen(carve, &Y, seen_slots);
+  // Once work is queued on the scratch, a failure waits for the stream before
+  // it returns, so the scratch is free again when the call returns.
+  struct DrainOnError {
+    cudaStream_t st;
+    bool armed = false;
+    ~DrainOnError() {
+      if (armed) cudaStreamSynchronize(st);
+    }
+  } drain{st};
 
+  uint64_t h2d = 0;
   auto up = [&](void* dst, const void* src, size_t bytes) {
+    drain.armed = true;
     if (bytes) HBX_STATIC_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
+    h2d += bytes;
   };
   auto up_side = [&](const hbx::SideEnc& se, const dev::Side& ds,
                      const std::vector<dev::StrMeta>& m) {
@@ -261,7 +339,6 @@ void run_static(int device, const hbx_plan* plan, const hbx_table* left, const h
   // counters, histograms, cursors and the duplicate set start from zero/empty
   HBX_STATIC_CUDA(cudaMemsetAsync(Y.ctr, 0, sizeof(dev::Counters), st));
   if (Y.seen) HBX_STATIC_CUDA(cudaMemsetAsync(Y.seen, 0xff, Y.seen_slots * 8, st));
-  const int n_sm = prop.multiProcessorCount;
   auto grid_for = [&](uint32_t n) {
     return (int)std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, (uint64_t)n_sm * 8));
   };
@@ -332,6 +409,7 @@ void run_static(int device, const hbx_plan* plan, const hbx_table* left, const h
   HBX_STATIC_CUDA(cudaMemcpyAsync(&total_items, Y.rule_base + Y.rules.size(), 8,
                                   cudaMemcpyDeviceToHost, st));
   HBX_STATIC_CUDA(cudaStreamSynchronize(st));
+  drain.armed = false;  // the stream is idle
   if (c.items_done != total_items) hbx::fail(HBX_ERR_CUDA, "evaluation did not finish its work");
   out->n_required = c.seen_overflow ? std::max<uint64_t>(c.out_count, c.passes) : c.out_count;
   out->n_written = 0;
@@ -347,9 +425,19 @@ void run_static(int device, const hbx_plan* plan, const hbx_table* left, const h
     stats->n_tiles = total_items;
     stats->n_partitions_used = E.n_partitions_used;
     stats->jw_word_ops = c.jw_word_ops;
-    stats->h2d_bytes = measure.used;
+    stats->pairs_scanned = c.scans;
+    stats->scan_steps = c.scan_steps;
+    stats->scan_word_ops = c.scan_steps * 4ull * 3ull * Y.shape.w;
+    stats->scan_words = Y.shape.w;
+    stats->h2d_bytes = h2d;  // bytes copied to the device by this call
+    stats->n_windows = 1;
   }
-  if (c.out_count > out->capacity || c.seen_overflow)
+  if (c.seen_overflow)
+    hbx::fail(HBX_ERR_CAPACITY,
+              "the duplicate set (" + std::to_string(Y.seen_slots) + " slots, sized from the "
+              "output capacity and the pairs the partitions hold, within the 64 MiB scratch) "
+              "filled up; at least " + std::to_string(out->n_required) + " output slots needed");
+  if (c.out_count > out->capacity)
     hbx::fail(HBX_ERR_CAPACITY, "output capacity below the match count");
   out->n_written = c.out_count;
 }

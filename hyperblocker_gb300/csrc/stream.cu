@@ -296,6 +296,8 @@ extern "C" hbx_status hbx_block_streamed(hbx_ctx* ctx, const hbx_plan* plan, con
         agg.eval_variant = ws.eval_variant;
         agg.pairs_scanned += ws.pairs_scanned;
         agg.scan_steps += ws.scan_steps;
+        agg.scan_word_ops += ws.scan_word_ops;
+        agg.scan_words = std::max(agg.scan_words, ws.scan_words);
       }
       hbx_ctx_destroy(wc);
     };

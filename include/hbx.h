@@ -121,6 +121,10 @@ typedef struct hbx_stats {
   uint32_t n_windows;         /* partition windows of the call (hbx_block_streamed), else 1 */
   uint64_t pairs_scanned;     /* JW evaluations the filters could not settle (bit-parallel scans) */
   uint64_t scan_steps;        /* steps of those scans, 4 symbols each */
+  uint64_t scan_word_ops;     /* operations those scans executed, in jw_word_ops' unit (6 per
+                                 64-bit mask word per character scanned) */
+  uint32_t scan_words;        /* 32-bit words per scan mask in the last run (1, 2, 3, 4 or 8) */
+  uint32_t reserved0;
 } hbx_stats;
 
 /* ---- context ------------------------------------------------------------ */
@@ -173,10 +177,13 @@ hbx_status hbx_session_stats(const hbx_session* s, hbx_stats* out);
 hbx_status hbx_session_destroy(hbx_session* s);
 
 /* One call from host tables to host pairs: session create + run + copy back.
- * out holds HOST pointers. */
+ * out holds HOST pointers.  The tables are encoded on the context's stream;
+ * the run and the copy of the pairs go to `stream` (a cudaStream_t, NULL =
+ * the context's stream), the stream the reference's AsyncSubmit takes
+ * (host_producer.h:109-112).  Returns when the pairs are in out. */
 hbx_status hbx_block(hbx_ctx* ctx, const hbx_plan* plan, const hbx_table* left,
                      const hbx_table* right, uint64_t n_partitions, int64_t prefix_idx,
-                     hbx_mode mode, hbx_pairs* out, hbx_stats* stats);
+                     hbx_mode mode, hbx_pairs* out, hbx_stats* stats, void* stream);
 
 /* Appends "<id_l>,<id_r>\n" lines (column 0 of each table), like
  * host_reducer.h:80-90.  Pairs are written in the order given.  With a

@@ -20,7 +20,18 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD, "libhbx_oracle.so")
 REF_LIB_PATH = os.path.join(HERE, "_ref", "libhb_ref.so")
-REFERENCE_ROOT = os.environ.get("HBX_REFERENCE_ROOT", "/root/reference")
+
+def _reference_root() -> str:
+    """The reference checkout: $HBX_REFERENCE_ROOT, else a ``reference``
+    directory beside this repository (where the build container keeps it);
+    the GPU machines have neither, and use what was built or committed."""
+    env = os.environ.get("HBX_REFERENCE_ROOT")
+    if env:
+        return env
+    return os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+
+
+REFERENCE_ROOT = _reference_root()
 
 _lib: Optional[ctypes.CDLL] = None
 _ref: Optional[ctypes.CDLL] = None
@@ -57,6 +68,9 @@ class HboStats(ctypes.Structure):
         ("n_matches", ctypes.c_int64),
         ("fma_ambiguous", ctypes.c_int64),
         ("long_string_pairs", ctypes.c_int64),
+        ("jw_evals", ctypes.c_int64),
+        ("fp64_flips", ctypes.c_int64),
+        ("fp64_max_abs_diff", ctypes.c_double),
     ]
 
 
@@ -71,6 +85,8 @@ def lib() -> ctypes.CDLL:
         L.hbo_jw.restype = ctypes.c_double
         L.hbo_jw.argtypes = [ctypes.c_char_p, ctypes.c_int64, ctypes.c_char_p, ctypes.c_int64,
                              ctypes.c_int]
+        L.hbo_jw_fp64.restype = ctypes.c_double
+        L.hbo_jw_fp64.argtypes = [ctypes.c_char_p, ctypes.c_int64, ctypes.c_char_p, ctypes.c_int64]
         L.hbo_std_hash.restype = ctypes.c_uint64
         L.hbo_std_hash.argtypes = [ctypes.c_char_p, ctypes.c_int64]
         L.hbo_sort_rules.restype = None
@@ -103,10 +119,18 @@ def ref_lib() -> ctypes.CDLL:
 
 
 class CTable:
-    """Row-major (ptr, len) cells over Python bytes, kept alive by this object."""
+    """Row-major (ptr, len) cells, kept alive by this object.
 
-    def __init__(self, cols: Sequence[Sequence[bytes]]):
+    ``cols`` is column-major: each column a sequence of bytes, or a
+    ``(blob uint8 array, int64 offsets)`` pair (n_rows + 1 offsets), the
+    layout of the large synthetic tables; blob columns are addressed in
+    place, without a Python object per cell."""
+
+    def __init__(self, cols):
         self.n_cols = len(cols)
+        if cols and all(isinstance(c, tuple) for c in cols):
+            self._init_blobs(cols)
+            return
         self.n_rows = len(cols[0]) if cols else 0
         cells = [cols[c][r] for r in range(self.n_rows) for c in range(self.n_cols)]
         self._keep = cells
@@ -116,6 +140,24 @@ class CTable:
         self.t = HboTable(self.n_rows, self.n_cols,
                           ctypes.cast(self.ptr, ctypes.POINTER(ctypes.c_char_p)),
                           ctypes.cast(self.len, ctypes.POINTER(ctypes.c_int64)))
+
+    def _init_blobs(self, cols):
+        blobs = [np.ascontiguousarray(b, dtype=np.uint8) for b, _ in cols]
+        offs = [np.ascontiguousarray(o, dtype=np.int64) for _, o in cols]
+        blobs = [b if b.size else np.zeros(1, np.uint8) for b in blobs]
+        self.n_rows = len(offs[0]) - 1
+        ptr = np.empty((self.n_rows, self.n_cols), dtype=np.uint64)
+        ln = np.empty((self.n_rows, self.n_cols), dtype=np.int64)
+        for c, (b, o) in enumerate(zip(blobs, offs)):
+            if len(o) - 1 != self.n_rows:
+                raise ValueError("columns differ in length")
+            ptr[:, c] = np.uint64(b.ctypes.data) + o[:-1].astype(np.uint64)
+            ln[:, c] = np.diff(o)
+        self._keep = (blobs, offs)
+        self.ptr, self.len = ptr, ln
+        self.t = HboTable(self.n_rows, self.n_cols,
+                          ctypes.cast(ptr.ctypes.data, ctypes.POINTER(ctypes.c_char_p)),
+                          ctypes.cast(ln.ctypes.data, ctypes.POINTER(ctypes.c_int64)))
 
 
 def _plan_arrays(plan):
@@ -133,6 +175,9 @@ class OracleResult:
     pair_comparisons: int
     fma_ambiguous: int
     long_string_pairs: int
+    jw_evals: int = 0           # JW evaluations of the run
+    fp64_flips: int = 0         # of them, threshold decisions that differ in FP64
+    fp64_max_abs_diff: float = 0.0  # max |JW reference path - JW FP64|
 
 
 def run_block(left: CTable, right: CTable, plan, n_partitions: int,
@@ -162,7 +207,7 @@ def run_block(left: CTable, right: CTable, plan, n_partitions: int,
         a[:, 0] = np.frombuffer(ol, dtype=np.uint32, count=got)
         a[:, 1] = np.frombuffer(orr, dtype=np.uint32, count=got)
     return OracleResult(a, st.pairs_covered, st.pair_comparisons, st.fma_ambiguous,
-                        st.long_string_pairs)
+                        st.long_string_pairs, st.jw_evals, st.fp64_flips, st.fp64_max_abs_diff)
 
 
 def partition(table: CTable, plan, n_partitions: int, prefix_idx: int = 2147483647) -> np.ndarray:

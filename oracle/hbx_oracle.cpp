@@ -58,6 +58,11 @@ typedef struct {
   int64_t n_matches;            // emitted pairs
   int64_t fma_ambiguous;        // JW threshold decisions that differ fma vs no-fma
   int64_t long_string_pairs;    // JW calls whose shorter string exceeds 256 bytes
+  // FP64 report: every JW evaluation is also computed with no float rounding
+  // at all (jw_fp64 below); the reference's decisions stay the ones above
+  int64_t jw_evals;             // JW evaluations (pair, similarity predicate)
+  int64_t fp64_flips;           // evaluations whose threshold decision differs in FP64
+  double fp64_max_abs_diff;     // max |JW (reference float/double path) - JW (FP64)|
 } hbo_stats;
 
 }  // extern "C"
@@ -79,15 +84,12 @@ inline bool ref_equal(const char* a, size_t la, const char* b, size_t lb) {
 // device_func.cuh:54-132, restated loop for loop.  Strings are given with
 // their strlen; s[len] reads as the terminator (never equal to a character of
 // the other string inside its own length).
-float ref_jaro(const char* term_l, size_t len_l, const char* term_r, size_t len_r) {
-  if (len_r == 0 || len_l == 0) {
-    if (len_l == 0 && len_r == 0) return 1.0f;
-    return 0.0f;
-  }
-  if (len_l > len_r) {
-    std::swap(term_l, term_r);
-    std::swap(len_l, len_r);
-  }
+//
+// Split in two: ref_jaro_matches runs the two greedy loops (65-111) and
+// returns the match count m; ref_jaro_value applies the formula (127-128).
+// Both take the strings already swapped so that the first is the shorter
+// (71-79), and non-empty.
+size_t ref_jaro_matches(const char* term_l, size_t len_l, const char* term_r, size_t len_r) {
   const size_t halflen = (len_l + 1) / 2;
   uint16_t idx[257];
   std::memset(idx, 0, sizeof(idx));
@@ -116,8 +118,12 @@ float ref_jaro(const char* term_l, size_t len_l, const char* term_r, size_t len_
       }
     }
   }
-  if (!match) return 0.0f;
   // transpositions are counted by the reference (116-126) and never used.
+  return match;
+}
+
+float ref_jaro_value(size_t match, size_t len_l, size_t len_r) {
+  if (!match) return 0.0f;
   const float md = (float)match;
   // (md / len_l + md / len_r + 1.0) / 3.0 : float quotients, float sum,
   // then double add and divide, rounded to float on return (127-128).
@@ -127,16 +133,41 @@ float ref_jaro(const char* term_l, size_t len_l, const char* term_r, size_t len_
   return (float)r;
 }
 
-// device_func.cuh:210-231.  pfweight = 0.1; the prefix is taken on the
-// unswapped strings up to min(len1, len2), without the textbook cap of 4.
-double ref_jw(const char* s1, size_t l1, const char* s2, size_t l2, int fma_mode,
-              size_t* prefix_out) {
-  double j = ref_jaro(s1, l1, s2, l2);
+// Match count m and the Jaro value of two strings given with their strlen
+// (65-69: both empty -> 1, one empty -> 0, m = 0 for those).
+float ref_jaro_m(const char* term_l, size_t len_l, const char* term_r, size_t len_r, size_t* m_out) {
+  *m_out = 0;
+  if (len_r == 0 || len_l == 0) {
+    if (len_l == 0 && len_r == 0) return 1.0f;
+    return 0.0f;
+  }
+  if (len_l > len_r) {
+    std::swap(term_l, term_r);
+    std::swap(len_l, len_r);
+  }
+  *m_out = ref_jaro_matches(term_l, len_l, term_r, len_r);
+  return ref_jaro_value(*m_out, len_l, len_r);
+}
+
+float ref_jaro(const char* term_l, size_t len_l, const char* term_r, size_t len_r) {
+  size_t m;
+  return ref_jaro_m(term_l, len_l, term_r, len_r, &m);
+}
+
+// Common prefix of the unswapped strings up to min(len1, len2), uncapped
+// (device_func.cuh:218-226).
+size_t ref_prefix(const char* s1, size_t l1, const char* s2, size_t l2) {
   const size_t m = l1 < l2 ? l1 : l2;
   size_t p = 0;
   for (p = 0; p < m; p++)
     if (s1[p] != s2[p]) break;
-  if (prefix_out) *prefix_out = p;
+  return p;
+}
+
+// device_func.cuh:227-230 from the Jaro value j and the prefix p:
+// j += (1 - j) * p * 0.1 in double (fma_mode as described in the header),
+// clamped to 1.
+double ref_jw_from(double j, size_t p, int fma_mode) {
   volatile double a = (1.0 - j) * (double)p;
   double out;
   if (fma_mode) {
@@ -145,6 +176,35 @@ double ref_jw(const char* s1, size_t l1, const char* s2, size_t l2, int fma_mode
     volatile double b = (double)a * 0.1;
     out = j + (double)b;
   }
+  return out > 1.0 ? 1.0 : out;
+}
+
+// device_func.cuh:210-231.  pfweight = 0.1; the prefix is taken on the
+// unswapped strings up to min(len1, len2), without the textbook cap of 4.
+double ref_jw(const char* s1, size_t l1, const char* s2, size_t l2, int fma_mode,
+              size_t* prefix_out) {
+  const double j = ref_jaro(s1, l1, s2, l2);
+  const size_t p = ref_prefix(s1, l1, s2, l2);
+  if (prefix_out) *prefix_out = p;
+  return ref_jw_from(j, p, fma_mode);
+}
+
+// The same Jaro-Winkler value with no float rounding anywhere: the match
+// count m, lengths and prefix of the reference's loops, then
+// j = (m / ls + m / ll + 1) / 3 and j + (1 - j) * p * 0.1 in double
+// (clamped to 1).  Not the reference's arithmetic: it is the report of how
+// far the reference's float/double path lies from a double evaluation.
+double jw_fp64(size_t m, size_t l1, size_t l2, size_t p) {
+  double j;
+  if (l1 == 0 || l2 == 0) {
+    j = (l1 == 0 && l2 == 0) ? 1.0 : 0.0;
+  } else if (m == 0) {
+    j = 0.0;
+  } else {
+    const double ls = (double)(l1 < l2 ? l1 : l2), ll = (double)(l1 < l2 ? l2 : l1);
+    j = ((double)m / ls + (double)m / ll + 1.0) / 3.0;
+  }
+  const double out = j + (1.0 - j) * (double)p * 0.1;
   return out > 1.0 ? 1.0 : out;
 }
 
@@ -208,6 +268,9 @@ struct ThreadOut {
   int64_t comparisons = 0;
   int64_t ambiguous = 0;
   int64_t long_pairs = 0;
+  int64_t jw_evals = 0;
+  int64_t fp64_flips = 0;
+  double fp64_max = 0.0;
 };
 
 // global_func.cuh:117-183 for one (l, r) pair.  Also counts the rule
@@ -249,10 +312,19 @@ bool eval_pair(const Eval& E, int64_t row_l, int64_t row_r, ThreadOut* to) {
         Cell a = cell(E.L, row_l, pl);
         Cell b = cell(E.R, row_r, pr);
         if (std::min(a.n, b.n) > 256) to->long_pairs++;
-        const double sim = ref_jw(a.p, a.n, b.p, b.n, E.fma_mode, nullptr);
-        const double other = ref_jw(a.p, a.n, b.p, b.n, !E.fma_mode, nullptr);
+        // one run of the loops (m) and of the prefix serves the FMA form,
+        // the separate form and the FP64 report
+        size_t m = 0;
+        const double j = ref_jaro_m(a.p, a.n, b.p, b.n, &m);
+        const size_t p = ref_prefix(a.p, a.n, b.p, b.n);
+        const double sim = ref_jw_from(j, p, E.fma_mode);
+        const double other = ref_jw_from(j, p, !E.fma_mode);
         const double thr = (double)E.pred_threshold[i];
         if ((sim < thr) != (other < thr)) to->ambiguous++;
+        const double wide = jw_fp64(m, a.n, b.n, p);
+        to->jw_evals++;
+        if ((wide < thr) != (sim < thr)) to->fp64_flips++;
+        to->fp64_max = std::max(to->fp64_max, std::fabs(sim - wide));
         if (sim < thr) to_skip = true;
         break;
       }
@@ -289,6 +361,14 @@ float hbo_jaro(const char* a, int64_t la, const char* b, int64_t lb) {
 // Reference Jaro-Winkler (double); fma_mode as described in the header.
 double hbo_jw(const char* a, int64_t la, const char* b, int64_t lb, int fma_mode) {
   return ref_jw(a, c_strnlen(a, la), b, c_strnlen(b, lb), fma_mode, nullptr);
+}
+
+// The FP64 restatement of Jaro-Winkler (jw_fp64) of two byte strings.
+double hbo_jw_fp64(const char* a, int64_t la, const char* b, int64_t lb) {
+  const size_t na = c_strnlen(a, la), nb = c_strnlen(b, lb);
+  size_t m = 0;
+  ref_jaro_m(a, na, b, nb, &m);
+  return jw_fp64(m, na, nb, ref_prefix(a, na, b, nb));
 }
 
 // libstdc++ std::hash<std::string> of a byte string (data_mngr.h:157).
@@ -382,6 +462,9 @@ int64_t hbo_block(const hbo_table* L, const hbo_table* R, const int* pred_index,
     s.pair_comparisons += o.comparisons;
     s.fma_ambiguous += o.ambiguous;
     s.long_string_pairs += o.long_pairs;
+    s.jw_evals += o.jw_evals;
+    s.fp64_flips += o.fp64_flips;
+    s.fp64_max_abs_diff = std::max(s.fp64_max_abs_diff, o.fp64_max);
   }
   std::sort(all.begin(), all.end());
   s.n_matches = (int64_t)all.size();

@@ -7,10 +7,14 @@
 # oracle/_ref/libhb_ref.so.  Nothing from the reference is copied into this
 # repository; the output directory is git-ignored.
 #
-# usage: oracle/ref/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# usage: oracle/ref/build_ref.sh REFERENCE_ROOT   (the reference checkout)
 set -euo pipefail
 here="$(cd "$(dirname "$0")" && pwd)"
-ref="${1:-/root/reference}"
+if [ $# -lt 1 ]; then
+  echo "usage: build_ref.sh REFERENCE_ROOT" >&2
+  exit 2
+fi
+ref="$1"
 out="$here/../_ref"
 if [ ! -f "$ref/core/gpu/global_func.cuh" ]; then
   echo "build_ref.sh: reference checkout not found at $ref" >&2

@@ -156,3 +156,71 @@ def test_partition_uses_std_hash():
     b = api.partition(api.CTable(cols), plan, 7)
     for i, cell in enumerate(cols[4]):
         assert b[i] == L.hbo_std_hash(cell, len(cell)) % 7
+
+
+def _jw_fp64_py(a: bytes, b: bytes) -> float:
+    """FP64 Jaro-Winkler from the bit-parallel match count: no float rounding."""
+    la, lb = len(a), len(b)
+    if la == 0 or lb == 0:
+        j = 1.0 if la == lb else 0.0
+    else:
+        x, y = (a, b) if la <= lb else (b, a)
+        m = _m_bitparallel(x, y)
+        j = 0.0 if m == 0 else (m / min(la, lb) + m / max(la, lb) + 1.0) / 3.0
+    p = 0
+    while p < min(la, lb) and a[p] == b[p]:
+        p += 1
+    return min(1.0, j + (1.0 - j) * p * 0.1)
+
+
+def test_fp64_restatement_and_its_distance():
+    """hbo_jw_fp64 is the double-only formula over the reference's match
+    count and prefix; the reference's float/double value lies within float
+    rounding of it (the report's max |JW_fp32path - JW_fp64|)."""
+    L = api.lib()
+    rnd = random.Random(11)
+    worst = 0.0
+    for t in range(5000):
+        alpha = rnd.choice([b"ab", b"abcd", b"abcdefghijklmnopqrstuvwxyz "])
+        la, lb = rnd.randint(0, 60), rnd.randint(0, 60)
+        a = bytes(rnd.choice(alpha) for _ in range(la))
+        b = bytes(rnd.choice(alpha) for _ in range(lb))
+        wide = L.hbo_jw_fp64(a, la, b, lb)
+        assert abs(wide - _jw_fp64_py(a, b)) < 1e-12, (a, b)
+        worst = max(worst, abs(L.hbo_jw(a, la, b, lb, 1) - wide))
+    assert 0.0 < worst < 1e-6
+
+
+def test_fp64_report_on_c2(golden):
+    """Every JW evaluation of the C2 golden run is also evaluated in FP64: the
+    report counts them, the decisions that FP64 would flip (none on C2) and
+    the largest score difference; the reference path's set is unchanged."""
+    g = golden["c2_order_01"]
+    w = synth.WORKLOADS[g["workload"]]()
+    cl, cr = synth.table_bytes(w.tables.left), synth.table_bytes(w.tables.right)
+    res = api.run_block(api.CTable(cl), api.CTable(cr),
+                        _plan([w.rules[k] for k in g["rule_order"]]), g["n_partitions"])
+    assert _util.digest(_util.id_lines(res.pairs, cl, cr)) == g["sha256"]
+    assert res.jw_evals > g["pair_comparisons"] // 2
+    assert res.fp64_flips == 0
+    assert 0.0 < res.fp64_max_abs_diff < 1e-6
+
+
+def test_blob_tables_equal_cell_tables():
+    """The oracle reads (blob, offsets) columns in place: same result as
+    per-cell bytes (the form the 1M-10M-row checks use)."""
+    cl, cr = _util.random_tables(5, 80, 120, b"abcdef ,", 30)
+
+    def blobs(cols):
+        out = []
+        for col in cols:
+            off = np.zeros(len(col) + 1, dtype=np.int64)
+            off[1:] = np.cumsum([len(x) for x in col])
+            out.append((np.frombuffer(b"".join(col) or b"\0", dtype=np.uint8), off))
+        return out
+
+    plan = _plan([synth.rule_yaml([3], [(1, 0.6)]), synth.rule_yaml([4], [(2, 0.5)])])
+    a = api.run_block(api.CTable(cl), api.CTable(cr), plan, 3)
+    b = api.run_block(api.CTable(blobs(cl)), api.CTable(blobs(cr)), plan, 3)
+    assert np.array_equal(a.pairs, b.pairs)
+    assert (a.pair_comparisons, a.pairs_covered) == (b.pair_comparisons, b.pairs_covered)
