@@ -3,47 +3,57 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
 
-Workload (default): the C2 configuration -- 2,600 x 64,263 seeded synthetic
-bibliographic rows (header line included as data, as the reference reads it),
-5k perturbed true pairs, two rules ((year eq, JW(title) >= 0.89,
-JW(authors) >= 0.85) or (venue eq, JW(title) >= 0.95)), 8 hash partitions.
-A step is one pass of the hot path over the whole workload: equality join,
-Jaro-Winkler pair evaluation and compaction of the matching pairs.
+Headline workload: C3, the configuration the batched-vs-plain target is
+quoted on -- 1,000,000 x 1,000,000 seeded synthetic bibliographic rows (header
+line included as data, as the reference reads it), 8 rules mixing 1-2
+equalities with 1-3 Jaro-Winkler predicates (thresholds U[0.80, 0.95]), 64
+hash partitions of Zipf(1.3) sizes.  A step is one pass of the hot path over
+the whole workload: equality join, Jaro-Winkler pair evaluation and
+compaction of the matching pairs.
 
 * ``value``: pair-comparisons/s of the engine's default (batched: one
   persistent work-stealing launch replayed from a CUDA graph) with the inputs
-  resident in HBM; L2 is flushed (256 MiB write) before every timed step and
-  every step is timed with CUDA events on the launching stream.
+  resident in HBM (about 200 MB a side, larger than L2; L2 is also flushed
+  with a 256 MiB write before every timed step); every step is timed with
+  CUDA events on the launching stream.
 * ``plain``: the same with one launch per (partition, rule), like the
   reference's per-partition submission.
-* ``e2e``: the same metric through the one-shot C-ABI call ``hbx_block`` from
-  host tables to host pair buffers (encode + H2D + run + D2H inside the timed
-  region).
-* ``roofline``: the pair-evaluation kernel against the INT32 issue peak (see
-  the ``roofline`` block for the conventions), ``cpu_baseline``: the oracle
-  (the reference's brute-force algorithm restated in C++) on all host cores.
+* ``e2e``: the same metric through the one-shot C-ABI call ``hbx_block``
+  from host tables to host pair buffers (encode + H2D + run + D2H inside the
+  timed region).
+* ``parity``: the engine's pairs of a stratified sample of left rows (the
+  same number from every partition) against the oracle's on the same rows;
+  the oracle run is also the ``cpu_baseline`` (all host cores).
+* ``roofline``: the pair-evaluation kernel against the measured rate of the
+  bit-parallel scan step (libhbx_probe.so), with the fraction of the
+  algorithmic count and of the scan operations actually executed.
+* ``jw_fp64``: the reference's float/double Jaro-Winkler against a
+  double-only restatement over the oracle runs (largest difference, decisions
+  it would flip); the set is the reference's either way.
 
-At N=1 more workloads are measured and reported in the same line: ``c3``
-(1M x 1M rows, 8 rules, 64 Zipf-sized partitions: batched vs plain), ``c5``
-(long strings, one-shot vs partition windows streamed under a memory budget)
-``serving`` (10M resident right rows, a Poisson trace of left-record
-requests: p50/p99/p999 latency and pair-comparisons/s) and ``io`` (CSV
-tokenization and pair-file writing, device vs host); ``--sections`` picks.
+At N=1 more workloads are reported in the same line (``--sections``): ``c2``
+(2,600 x 64,263 rows, 2 rules, 8 partitions, checked in full), ``c5`` (long
+strings: one-shot vs partition windows streamed under a memory budget,
+sampled parity), ``serve`` (10M resident right rows, a Poisson trace of
+requests: p50/p99/p999 latency, small requests checked against the oracle)
+and ``io`` (CSV tokenization and pair-file writing, device vs host).
 
-``--impl reference`` times that CPU implementation alone and prints the same
-line with ``"impl": "reference"``.  With N > 1 GPUs (torchrun) every rank runs
-an independent replica (weak scaling); the path needs no collective.
+``--impl reference`` times the CPU implementation of the path (the oracle:
+the reference's brute-force algorithm restated in C++, all host cores) on
+stratified samples of the same C3 workload and prints the same line with
+``"impl": "reference"``.  With N > 1 GPUs (torchrun) every rank runs an
+independent replica (weak scaling); the path needs no collective.
 """
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import statistics
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -51,9 +61,17 @@ sys.path.insert(0, ROOT)
 
 METRIC = "pair-comparisons/s, batched vs plain, same GPU, exact set; serving p50/p99 ms"
 UNIT = "pair-comparisons/s"
-WORKLOAD_DESC = ("c2: 2,600 x 64,263 synthetic bibliographic rows (+1 header row each), 5k true "
-                 "pairs, rules (year eq, JW(title)>=0.89, JW(authors)>=0.85) | (venue eq, "
-                 "JW(title)>=0.95), 8 partitions")
+
+
+def c3_desc(n: int) -> str:
+    return (f"c3: {n:,} x {n:,} synthetic bibliographic rows (+1 header row each), 8 rules (1-2 "
+            "equalities, 1-3 JW predicates, thresholds U[0.80,0.95]), 64 partitions keyed by a "
+            "Zipf(1.3) column")
+
+
+C2_DESC = ("c2: 2,600 x 64,263 synthetic bibliographic rows (+1 header row each), 5k true pairs, "
+           "rules (year eq, JW(title)>=0.89, JW(authors)>=0.85) | (venue eq, JW(title)>=0.95), "
+           "8 partitions")
 
 
 def _env_int(k, d):
@@ -113,8 +131,8 @@ class ClockSampler:
                     reasons.add(n)
         os.unlink(self.path)
         if sm:
-            out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                   "samples": len(sm)}
+            out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                   "reasons": sorted(reasons), "samples": len(sm)}
         return out
 
 
@@ -126,136 +144,305 @@ def _peaks():
         return {}
 
 
-def _traffic_per_launch():
-    """dram bytes of one k_eval launch on this workload from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "k_eval_c2_traffic.json")
+def _traffic_record():
+    """DRAM bytes of one evaluation launch on C3 from the committed ncu summary
+    (ncu cannot run inside the timed bench); labelled with its source."""
+    p = os.path.join(ROOT, "profiles", "k_eval_c3_traffic.json")
     try:
         with open(p) as f:
-            return json.load(f).get("dram_bytes_per_launch")
+            d = json.load(f)
+        return d.get("dram_bytes_per_launch"), f"profiles/k_eval_c3_traffic.json ({d.get('source', '')})"
     except Exception:
-        return None
+        return None, "not measured"
 
 
-def load_workload(tmpdir: str):
-    import hyperblocker_gb300 as hb
-    from hyperblocker_gb300 import synth
+# ------------------------------------------------------------------ helpers
+def oracle_plan(docs):
+    from oracle import rules
 
-    w = synth.c2()
-    paths = synth.materialize(w, tmpdir)
-    return w, paths
+    return rules.serialize(rules.sort_rules([rules.decode_rule(rules.parse_yaml(d)) for d in docs]))
 
 
-def cpu_baseline(paths, n_partitions, target_s=15.0, steps=1, warmup=0, step_fraction=None):
-    """The oracle on all host cores over a bounded sample of left rows.
-
-    Returns dict(value, cores, sample, seconds)."""
+def stratified_rows(ctable, plan_o, n_partitions, per_part, seed):
+    """A left-row filter with up to per_part rows of every partition (rows
+    drawn from PCG64(seed)); returns (uint8 filter, rows chosen)."""
     import numpy as np
 
-    from oracle import api, csvref, rules
+    from oracle import api
 
-    api.build()
-    cl = csvref.read_columns(paths["left"])
-    cr = csvref.read_columns(paths["right"])
-    plan = rules.plan_from_dir(paths["rules"])
-    L, R = api.CTable(cl), api.CTable(cr)
-    n_l = len(cl[0])
-    cores = os.cpu_count() or 1
-    # size the sample: time a small probe, then scale to ~target_s of CPU work
-    if step_fraction is None:
-        probe = np.zeros(n_l, dtype=np.uint8)
-        probe[::64] = 1
+    bucket = api.partition(ctable, plan_o, n_partitions)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    filt = np.zeros(ctable.n_rows, dtype=np.uint8)
+    for p in range(n_partitions):
+        rows = np.nonzero(bucket == p)[0]
+        if len(rows):
+            filt[rng.choice(rows, size=min(per_part, len(rows)), replace=False)] = 1
+    return filt, int(filt.sum())
+
+
+def device_pairs_of_rows(out_l, out_r, n, filt, dev):
+    """The engine's pairs (device arrays) whose left row is in filt, sorted."""
+    import numpy as np
+    import torch
+
+    from tests._util import sorted_pairs
+
+    mask = torch.from_numpy(filt).to(dev)
+    keep = torch.index_select(mask, 0, out_l[:n]).bool()
+    l = out_l[:n][keep].cpu().numpy().view(np.uint32)
+    r = out_r[:n][keep].cpu().numpy().view(np.uint32)
+    return sorted_pairs(np.stack([l, r], axis=1))
+
+
+def fp64_block(res):
+    return {"jw_evals": int(res.jw_evals), "fp64_flips": int(res.fp64_flips),
+            "max_abs_diff": float(res.fp64_max_abs_diff), "fma_ambiguous": int(res.fma_ambiguous)}
+
+
+def probe_scan_peak(device: int, words: int):
+    """Measured rate of the bit-parallel scan step (libhbx_probe.so): best over
+    CTA counts, in the roofline's unit (6 operations per 64-bit mask word per
+    character)."""
+    from hyperblocker_gb300 import build as hbuild
+
+    lib = ctypes.CDLL(hbuild.PROBE_LIB)
+    lib.hbx_probe_scan_rate.restype = ctypes.c_int
+    lib.hbx_probe_scan_rate.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_uint32,
+                                        ctypes.POINTER(ctypes.c_double),
+                                        ctypes.POINTER(ctypes.c_double)]
+    w = {1: 1, 2: 2, 3: 4, 4: 4}.get(words, 8)
+    iters = max(256, 16384 // w)
+    best, per = 0.0, {}
+    for bps in (1, 2, 3, 4, 6, 8):
+        ops, ms = ctypes.c_double(), ctypes.c_double()
+        rc = lib.hbx_probe_scan_rate(device, w, bps, iters, ctypes.byref(ops), ctypes.byref(ms))
+        if rc != 0:
+            continue
+        per[bps] = ops.value / 1e12
+        best = max(best, ops.value)
+    return {"tops": best / 1e12, "words": w, "per_ctas_per_sm": per, "iters": iters}
+
+
+# ------------------------------------------------------------------ C3 (headline)
+class C3:
+    """The C3 workload, its engine session and device output buffers."""
+
+    def __init__(self, args, ctx, dev):
+        import torch
+
+        import hyperblocker_gb300 as hb
+        from hyperblocker_gb300 import synth_big
+
+        self.n = args.c3_rows
+        self.w = synth_big.c3(self.n, self.n, max(1, self.n // 50))
+        self.plan = hb.Plan.from_yaml(self.w.rules, ctx)
+        self.L = hb.Table.from_columns(self.w.left.cols, ctx)
+        self.R = hb.Table.from_columns(self.w.right.cols, ctx)
+        self.sess = hb.Session(ctx, self.plan, self.L, self.R, self.w.n_partitions)
+        self.stream = torch.cuda.Stream(device=dev)
+        self.dev = dev
+        m = self.sess.count("batched", self.stream.cuda_stream)  # runs the autotuner too
+        self.cap = max(1, m)
+        self.out_l = torch.empty(self.cap, dtype=torch.int32, device=dev)
+        self.out_r = torch.empty(self.cap, dtype=torch.int32, device=dev)
+        self.flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def step(self, mode):
+        return self.sess.run_device(mode, self.out_l.data_ptr(), self.out_r.data_ptr(), self.cap,
+                                    self.stream.cuda_stream)
+
+    def timed(self, mode, k, warm):
+        import torch
+
+        for _ in range(warm):
+            self.step(mode)
+        rec = {"ms": [], "ms_eval": [], "ops": [], "scan_ops": [], "cmp": [], "launches": 0,
+               "matches": 0}
+        with torch.cuda.stream(self.stream):
+            for _ in range(k):
+                self.flush.zero_()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(self.stream)
+                n = self.step(mode)
+                e1.record(self.stream)
+                e1.synchronize()
+                st = self.sess.stats()
+                rec["ms"].append(e0.elapsed_time(e1))
+                rec["ms_eval"].append(st.ms_eval)
+                rec["ops"].append(st.jw_word_ops)
+                rec["scan_ops"].append(st.scan_word_ops)
+                rec["cmp"].append(st.pair_comparisons)
+                rec["launches"] += st.n_launches
+                rec["matches"] = n
+        return rec
+
+    def parity(self, args, n_matches):
+        """Sampled check against the oracle; its run is the CPU baseline."""
+        import numpy as np
+
+        from oracle import api
+
+        plan_o = oracle_plan(self.w.rules)
+        Lo, Ro = api.CTable(self.w.left.cols), api.CTable(self.w.right.cols)
+        filt, n_rows = stratified_rows(Lo, plan_o, self.w.n_partitions, args.c3_sample_per_part, 7)
+        cores = os.cpu_count() or 1
         t = time.perf_counter()
-        api.run_block(L, R, plan, n_partitions, n_threads=cores, left_row_filter=probe)
-        dt = max(time.perf_counter() - t, 1e-3)
-        frac = min(1.0, (target_s / dt) / 64.0)
-    else:
-        frac = step_fraction
-    stride = max(1, int(round(1.0 / frac)))
-    vals, secs, cmps = [], [], []
-    for k in range(warmup + steps):
-        filt = np.zeros(n_l, dtype=np.uint8)
-        filt[(k % stride)::stride] = 1
-        t = time.perf_counter()
-        res = api.run_block(L, R, plan, n_partitions, n_threads=cores, left_row_filter=filt)
+        res = api.run_block(Lo, Ro, plan_o, self.w.n_partitions, n_threads=cores,
+                            left_row_filter=filt)
         dt = time.perf_counter() - t
-        if k >= warmup:
-            vals.append(res.pair_comparisons / dt)
-            secs.append(dt)
-            cmps.append(res.pair_comparisons)
-    return {"value": sum(cmps) / sum(secs), "cores": cores, "seconds": sum(secs),
-            "sample": f"every {stride}th left row of the workload per step ({steps} step(s), "
-                      f"{sum(cmps)} pair-comparisons in {sum(secs):.2f} s)"}
+        got = device_pairs_of_rows(self.out_l, self.out_r, n_matches, filt, self.dev)
+        equal = bool(np.array_equal(got, res.pairs))
+        parity = {"sampled_left_rows": n_rows, "per_partition": args.c3_sample_per_part,
+                  "rules": len(self.w.rules), "partitions": self.w.n_partitions,
+                  "pairs": int(len(res.pairs)), "engine_pairs": int(len(got)),
+                  "pairs_covered": int(res.pairs_covered), "equal": equal}
+        cpu = {"value": res.pair_comparisons / dt, "unit": UNIT, "cores": cores, "kind": "port",
+               "seconds": dt,
+               "sample": f"{n_rows} left rows of C3 ({args.c3_sample_per_part} per partition, "
+                         f"seed 7) against their partitions' right rows: {res.pairs_covered} "
+                         f"pairs covered, {res.pair_comparisons} pair-comparisons in {dt:.2f} s"}
+        return parity, cpu, fp64_block(res)
+
+    def e2e(self, ctx, steps):
+        """hbx_block from host tables to host pairs (caller-kept host buffers)."""
+        import numpy as np
+
+        import hyperblocker_gb300 as hb
+
+        cap = self.cap + 1024
+        out = (np.zeros(cap, dtype=np.uint32), np.zeros(cap, dtype=np.uint32))  # touched once
+        hb.block(ctx, self.plan, self.L, self.R, self.w.n_partitions, hb.INT_MAX, "batched",
+                 capacity=cap, out=out)  # warm: page-locking of the tables, predicate order
+        ts = []
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            pairs, st = hb.block(ctx, self.plan, self.L, self.R, self.w.n_partitions, hb.INT_MAX,
+                                 "batched", capacity=cap, out=out)
+            ts.append(time.perf_counter() - t0)
+        s = statistics.mean(ts)
+        return {"value": st.pair_comparisons / s, "unit": UNIT,
+                "h2d_bytes_per_step": int(st.h2d_bytes),
+                "d2h_bytes_per_step": int(8 * st.n_matches + 64),
+                "ms_per_step": 1000.0 * s, "ms_create": float(st.ms_create),
+                "ms_run_device": float(st.ms_last_run), "steps": steps,
+                "ingest_on_device": int(st.ingest_on_device),
+                "includes": "session creation (H2D of the plan's columns from page-locked host "
+                            "tables, device encode: std::hash partition buckets, dictionaries, "
+                            "symbol arenas, Peq tables) + join + evaluation + D2H of the pairs "
+                            "into the caller's host arrays; the warm-up call page-locks the "
+                            "tables and memoises the measured predicate order on the plan"}
+
+    def close(self):
+        self.sess.close()
 
 
-def bench_c3(args, ctx, dev):
-    """C3: 1M x 1M rows, 8 rules, 64 Zipf-sized partitions; batched vs plain.
-
-    One untimed batched step (it also runs the tile autotuner and sizes the
-    output), then args.c3_steps timed steps of each form, CUDA events around
-    each step on the launching stream; the inputs (about 200 MB a side) are
-    larger than L2."""
+# ------------------------------------------------------------------ C2
+def bench_c2(args, ctx, dev):
+    """C2 read from CSV files: batched vs plain, end to end, and the full
+    pair set against the oracle (which is also its CPU baseline)."""
+    import numpy as np
     import torch
 
     import hyperblocker_gb300 as hb
-    from hyperblocker_gb300 import synth_big
+    from hyperblocker_gb300 import synth
+    from oracle import api, csvref, rules
+    from tests._util import sorted_pairs
 
-    n = args.c3_rows
-    w = synth_big.c3(n, n, max(1, n // 50))
-    plan = hb.Plan.from_yaml(w.rules, ctx)
-    L = hb.Table.from_columns(w.left.cols, ctx)
-    R = hb.Table.from_columns(w.right.cols, ctx)
-    sess = hb.Session(ctx, plan, L, R, w.n_partitions)
-    stream = torch.cuda.Stream(device=dev)
-    m = sess.count("batched", stream.cuda_stream)
-    cap = max(1, m)
-    out_l = torch.empty(cap, dtype=torch.int32, device=dev)
-    out_r = torch.empty(cap, dtype=torch.int32, device=dev)
-    res = {}
-    for mode in ("batched", "plain"):
-        sess.run_device(mode, out_l.data_ptr(), out_r.data_ptr(), cap, stream.cuda_stream)  # warm
-        ms, ms_eval, ops = [], [], []
-        for _ in range(args.c3_steps):
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            with torch.cuda.stream(stream):
-                e0.record(stream)
+    with tempfile.TemporaryDirectory() as d:
+        w = synth.c2()
+        paths = synth.materialize(w, d)
+        plan = hb.Plan.from_rule_dir(paths["rules"], ctx)
+        L = hb.Table.from_csv(paths["left"], ",", ctx)
+        R = hb.Table.from_csv(paths["right"], ",", ctx)
+        sess = hb.Session(ctx, plan, L, R, w.n_partitions)
+        stream = torch.cuda.Stream(device=dev)
+        cap = 1 << 20
+        out_l = torch.empty(cap, dtype=torch.int32, device=dev)
+        out_r = torch.empty(cap, dtype=torch.int32, device=dev)
+        flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+        res = {}
+        for mode in ("batched", "plain"):
+            for _ in range(3):
                 sess.run_device(mode, out_l.data_ptr(), out_r.data_ptr(), cap, stream.cuda_stream)
-                e1.record(stream)
-            e1.synchronize()
+            ms, ms_eval = [], []
+            with torch.cuda.stream(stream):
+                for _ in range(args.c2_steps):
+                    flush.zero_()
+                    e0 = torch.cuda.Event(enable_timing=True)
+                    e1 = torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                    n = sess.run_device(mode, out_l.data_ptr(), out_r.data_ptr(), cap,
+                                        stream.cuda_stream)
+                    e1.record(stream)
+                    e1.synchronize()
+                    ms.append(e0.elapsed_time(e1))
+                    ms_eval.append(sess.stats().ms_eval)
             st = sess.stats()
-            ms.append(e0.elapsed_time(e1))
-            ms_eval.append(st.ms_eval)
-            ops.append(st.jw_word_ops)
-        res[mode] = {"value": st.pair_comparisons / (statistics.mean(ms) / 1000.0),
-                     "ms_per_step": statistics.mean(ms), "ms_eval": statistics.mean(ms_eval),
-                     "launches_per_step": int(st.n_launches)}
-    st = sess.stats()
-    out = {"workload": f"c3: {n:,} x {n:,} synthetic rows (+1 header row each), 8 rules (1-2 "
-                       "equalities, 1-3 JW predicates, thresholds U[0.80,0.95]), 64 partitions "
-                       "keyed by a Zipf(1.3) column", "steps": args.c3_steps,
-           "pair_comparisons_per_step": int(st.pair_comparisons),
-           "pairs_covered_per_step": int(st.pairs_covered),
-           "matches_per_step": int(m), "unit": UNIT,
-           "batched": res["batched"], "plain": res["plain"],
-           "batched_vs_plain": res["batched"]["value"] / res["plain"]["value"],
-           "jw_word_ops_per_step": int(statistics.mean(ops)),
-           "alu_tops_eval": statistics.mean(ops) / (res["batched"]["ms_eval"] / 1000.0) / 1e12}
-    sess.close()
-    return out
+            res[mode] = {"value": st.pair_comparisons / (statistics.mean(ms) / 1000.0),
+                         "ms_per_step": statistics.mean(ms), "ms_eval": statistics.mean(ms_eval),
+                         "launches_per_step": int(st.n_launches)}
+        st = sess.stats()
+        got = sorted_pairs(np.stack([out_l[:n].cpu().numpy().view(np.uint32),
+                                     out_r[:n].cpu().numpy().view(np.uint32)], axis=1))
+        hb.block(ctx, plan, L, R, w.n_partitions, hb.INT_MAX, "batched")  # warm
+        t0 = time.perf_counter()
+        e2e_steps = 5
+        for _ in range(e2e_steps):
+            pairs, st_e2e = hb.block(ctx, plan, L, R, w.n_partitions, hb.INT_MAX, "batched")
+        e2e_s = (time.perf_counter() - t0) / e2e_steps
+        # the oracle over every pair (all host cores): parity and CPU baseline
+        cl = csvref.read_columns(paths["left"])
+        cr = csvref.read_columns(paths["right"])
+        cores = os.cpu_count() or 1
+        t = time.perf_counter()
+        o = api.run_block(api.CTable(cl), api.CTable(cr), rules.plan_from_dir(paths["rules"]),
+                          w.n_partitions, n_threads=cores)
+        dt = time.perf_counter() - t
+        sess.close()
+    return {"workload": C2_DESC, "unit": UNIT, "pair_comparisons_per_step": int(st.pair_comparisons),
+            "pairs_covered_per_step": int(st.pairs_covered), "matches_per_step": int(n),
+            "batched": res["batched"], "plain": res["plain"],
+            "batched_vs_plain": res["batched"]["value"] / res["plain"]["value"],
+            "e2e": {"value": st_e2e.pair_comparisons / e2e_s, "ms_per_step": 1000.0 * e2e_s,
+                    "h2d_bytes_per_step": int(st_e2e.h2d_bytes),
+                    "d2h_bytes_per_step": int(8 * st_e2e.n_matches + 64)},
+            "parity": {"rows": "all", "pairs": int(len(o.pairs)), "engine_pairs": int(len(got)),
+                       "equal": bool(np.array_equal(got, o.pairs) and
+                                     sorted_pairs(pairs).shape == o.pairs.shape and
+                                     np.array_equal(sorted_pairs(pairs), o.pairs)),
+                       "pair_comparisons_equal": int(o.pair_comparisons) == int(st.pair_comparisons)},
+            "cpu_baseline": {"value": o.pair_comparisons / dt, "unit": UNIT, "cores": cores,
+                             "kind": "port", "sample": f"every pair of the workload ({dt:.2f} s)"},
+            "jw_fp64": fp64_block(o)}
 
 
-def bench_c5(args, ctx):
+def c1_fp64():
+    """The oracle over C1 in full: the FP64 report of its JW evaluations."""
+    from hyperblocker_gb300 import synth
+    from oracle import api
+
+    w = synth.c1()
+    cl, cr = synth.table_bytes(w.tables.left), synth.table_bytes(w.tables.right)
+    res = api.run_block(api.CTable(cl), api.CTable(cr), oracle_plan(w.rules), w.n_partitions)
+    return fp64_block(res)
+
+
+# ------------------------------------------------------------------ C5
+def bench_c5(args, ctx, dev):
     """C5 shape at args.c5_rows x args.c5_rows: titles and authors of 64-256
     characters, a Zipf(1.0) key over 2^20 values, 3 rules, 64 partitions.
     The same job runs once through hbx_block (both tables encoded on the
     device at once) and once through hbx_block_streamed with partition windows
-    of at most args.c5_window_mb MiB (two windows in flight, each window's
-    copies and encoding overlapping the other's evaluation); both are timed
-    end to end (host tables to host pairs) and must give the same pairs."""
+    of at most args.c5_window_mb MiB (two windows in flight); both are timed
+    end to end (host tables to host pairs), must give the same pairs, and a
+    stratified sample of left rows is checked against the oracle."""
     import numpy as np
 
     import hyperblocker_gb300 as hb
     from hyperblocker_gb300 import synth_big
+    from oracle import api
+    from tests._util import sorted_pairs
 
     n = args.c5_rows
     w = synth_big.c5(n, n, max(1, n // 50))
@@ -271,37 +458,51 @@ def bench_c5(args, ctx):
     t = time.perf_counter()
     st_pairs, s2 = hb.block_streamed(ctx, plan, L, R, w.n_partitions, budget)
     t_st = time.perf_counter() - t
-    same = len(one) == len(st_pairs) and np.array_equal(
-        one[np.lexsort((one[:, 1], one[:, 0]))], st_pairs[np.lexsort((st_pairs[:, 1], st_pairs[:, 0]))])
+    one, st_pairs = sorted_pairs(one), sorted_pairs(st_pairs)
+    same = len(one) == len(st_pairs) and np.array_equal(one, st_pairs)
+    plan_o = oracle_plan(w.rules)
+    Lo, Ro = api.CTable(w.left.cols), api.CTable(w.right.cols)
+    filt, n_rows = stratified_rows(Lo, plan_o, w.n_partitions, args.c5_sample_per_part, 11)
+    o = api.run_block(Lo, Ro, plan_o, w.n_partitions, left_row_filter=filt)
+    mine = one[filt[one[:, 0]] == 1] if len(one) else one
     return {"workload": f"c5 shape: {n:,} x {n:,} rows, titles and authors 64-256 characters, "
                         "Zipf(1.0) key over 2^20 values, 3 rules, 64 partitions",
             "unit": UNIT, "pair_comparisons": int(s1.pair_comparisons),
             "matches": int(s1.n_matches), "same_pairs": bool(same),
             "long_string_pairs": int(s1.long_string_pairs),
             "one_shot": {"value": s1.pair_comparisons / t_one, "wall_ms": 1000 * t_one,
-                         "ms_eval": s1.ms_eval},
+                         "ms_eval": s1.ms_eval, "ms_create": s1.ms_create},
             "streamed": {"value": s2.pair_comparisons / t_st, "wall_ms": 1000 * t_st,
                          "windows": int(s2.n_windows), "window_mib": args.c5_window_mb,
                          "ms_eval_summed": s2.ms_eval, "ms_create_summed": s2.ms_create},
+            "streamed_vs_one_shot": t_st / t_one,
+            "parity": {"sampled_left_rows": n_rows, "per_partition": args.c5_sample_per_part,
+                       "pairs": int(len(o.pairs)), "engine_pairs": int(len(mine)),
+                       "equal": bool(np.array_equal(mine, o.pairs)),
+                       "streamed_equal_one_shot": bool(same)},
+            "jw_fp64": fp64_block(o),
             "timing": "end to end, host tables to host pairs, host clock"}
 
 
+# ------------------------------------------------------------------ serving (C4)
 def bench_serving(args, ctx):
     """C4: a resident right table of args.serve_rows rows; args.serve_requests
     requests of log-uniform 1-50k left records arriving Poisson at
     args.serve_rate per second, each naming one of 4 rules.  Requests are
     submitted at their arrival times from this thread and their results
-    polled; latency = submit -> result ready (host clock)."""
+    polled; latency = submit -> result ready (host clock).  Afterwards the
+    smallest requests' results are checked against the oracle over the whole
+    resident table."""
     import numpy as np
 
     import hyperblocker_gb300 as hb
     from hyperblocker_gb300 import synth_big
+    from oracle import api
 
     right = synth_big.c4_right(args.serve_rows)
     reqs = synth_big.c4_requests(right, args.serve_requests, rate=args.serve_rate, seed=1)
     plans = [hb.Plan.from_yaml([d], ctx) for d in synth_big.SERVE_RULES]
     R = hb.Table.from_columns(right.cols, ctx)
-    del right
     t = time.perf_counter()
     srv = hb.Server(ctx, plans, R)
     t_open = time.perf_counter() - t
@@ -337,6 +538,23 @@ def bench_serving(args, ctx):
     cmp = sum(got[i]["comparisons"] for i in range(n))
     bad = sum(1 for i in range(n) if got[i]["status"] != hb.OK)
     pct = lambda a, q: float(np.percentile(a, q)) if len(a) else None
+    # parity: the smallest requests (5-20 records if there are any) against
+    # the oracle over the whole resident table (one partition)
+    order = sorted(range(n), key=lambda i: (not (5 <= size[i] <= 20), size[i], i))
+    chk = order[:args.serve_check]
+    Ro = api.CTable(right.cols)
+    checked, equal, pairs_total, covered = [], True, 0, 0
+    for i in chk:
+        o = api.run_block(api.CTable(reqs[i].cols), Ro,
+                          oracle_plan([synth_big.SERVE_RULES[reqs[i].rule]]), 1)
+        mine = got[i]["pairs"]
+        mine = mine[np.lexsort((mine[:, 1], mine[:, 0]))] if len(mine) else mine.reshape(0, 2)
+        ok = len(mine) == len(o.pairs) and np.array_equal(mine, o.pairs)
+        equal = equal and ok
+        pairs_total += len(o.pairs)
+        covered += o.pairs_covered
+        checked.append({"request": i, "records": int(size[i]), "rule": int(reqs[i].rule),
+                        "pairs": int(len(o.pairs)), "equal": bool(ok)})
     return {"workload": f"c4: {args.serve_rows:,} resident right rows; {n} requests of "
                         "log-uniform 1-50,000 left records, Poisson arrivals at "
                         f"{args.serve_rate:g}/s, one of 4 rules (year and venue equalities, "
@@ -351,12 +569,17 @@ def bench_serving(args, ctx):
             "batches": int(s1.batches - s0.batches),
             "mean_batch_requests": float(np.mean([got[i]["batch_requests"] for i in range(n)])),
             "open_s": t_open, "resident_bytes": int(s1.resident_bytes),
+            "parity": {"requests_checked": len(checked), "pairs": pairs_total,
+                       "pairs_covered": int(covered), "equal": bool(equal),
+                       "against": f"the oracle over all {args.serve_rows + 1:,} resident rows",
+                       "requests": checked},
             "latency": "submit -> result ready, host clock; requests submitted at their "
                        "arrival times",
             "warm": f"the largest request ({reqs[big].n_rows:,} records) once per plan before "
                     "the trace"}
 
 
+# ------------------------------------------------------------------ io
 def bench_io(args, ctx, dev):
     """Ingest and output around the path, timed end to end (wall clock of
     the C-ABI calls, best of args.io_reps):
@@ -456,31 +679,54 @@ def max_over_ranks(dist, values, device):
     return [float(x) for x in t]
 
 
+# ------------------------------------------------------------------ reference arm
 def run_reference(args, rank, world):
+    """The CPU implementation of the path (the oracle, all host cores) on
+    stratified samples of C3: step k takes args.ref_per_part left rows of
+    every partition (seed 1000 + k) against their partitions' right rows."""
     if rank != 0:
         return 0
-    with tempfile.TemporaryDirectory() as d:
-        w, paths = load_workload(d)
-        # each step: 1/8 of the left rows, brute force over their partitions
-        cb = cpu_baseline(paths, w.n_partitions, steps=args.steps, warmup=args.warmup,
-                          step_fraction=1.0 / 8.0)
+    from hyperblocker_gb300 import synth_big
+    from oracle import api
+
+    api.build()
+    n = args.c3_rows
+    w = synth_big.c3(n, n, max(1, n // 50))
+    plan_o = oracle_plan(w.rules)
+    Lo, Ro = api.CTable(w.left.cols), api.CTable(w.right.cols)
+    cores = os.cpu_count() or 1
+    secs, cmps, covered, rows = 0.0, 0, 0, 0
+    for k in range(args.warmup + args.steps):
+        filt, n_rows = stratified_rows(Lo, plan_o, w.n_partitions, args.ref_per_part, 1000 + k)
+        t = time.perf_counter()
+        res = api.run_block(Lo, Ro, plan_o, w.n_partitions, n_threads=cores, left_row_filter=filt)
+        dt = time.perf_counter() - t
+        if k >= args.warmup:
+            secs += dt
+            cmps += res.pair_comparisons
+            covered += res.pairs_covered
+            rows += n_rows
+    value = cmps / secs
+    sample = (f"per step {args.ref_per_part} left rows of each of the 64 partitions (seed 1000 + "
+              f"step) against their partitions' right rows; {args.steps} steps: {rows} left rows, "
+              f"{covered} pairs covered, {cmps} pair-comparisons in {secs:.2f} s")
     line = {
-        "impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT,
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1000.0 * cb["seconds"] / max(args.steps, 1), "higher_is_better": True,
+        "ms_per_step": 1000.0 * secs / max(args.steps, 1), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u8",
-        "data": "synthetic (seeded, C2 shape)",
-        "config": {"workload": WORKLOAD_DESC, "n_partitions": w.n_partitions, "rules": 2},
-        "cpu_baseline": {"value": cb["value"], "unit": UNIT, "cores": cb["cores"], "kind": "port",
-                         "sample": cb["sample"]},
-        "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "data": "synthetic (seeded PCG64, C3 shape; no dataset download)",
+        "config": {"workload": c3_desc(n), "n_partitions": w.n_partitions, "rules": len(w.rules)},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
 
 
+# ------------------------------------------------------------------ engine arm
 def run_engine(args, rank, world, local_rank):
-    import numpy as np
     import torch
 
     import hyperblocker_gb300 as hb
@@ -492,145 +738,115 @@ def run_engine(args, rank, world, local_rank):
 
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local_rank)
-    tmp = tempfile.TemporaryDirectory()
-    w, paths = load_workload(tmp.name)
     ctx = hb.Context(local_rank)
-    plan = hb.Plan.from_rule_dir(paths["rules"], ctx)
-    L = hb.Table.from_csv(paths["left"], ",", ctx)
-    R = hb.Table.from_csv(paths["right"], ",", ctx)
-    sess = hb.Session(ctx, plan, L, R, w.n_partitions)
-    stream = torch.cuda.Stream(device=dev)
-    cap = 1 << 20
-    out_l = torch.empty(cap, dtype=torch.int32, device=dev)
-    out_r = torch.empty(cap, dtype=torch.int32, device=dev)
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-
-    def step(mode):
-        return sess.run_device(mode, out_l.data_ptr(), out_r.data_ptr(), cap, stream.cuda_stream)
-
-    def timed(mode, k, w_):
-        for _ in range(w_):
-            step(mode)
-        ms, ms_eval, ops, cmp, launches = [], [], [], [], 0
-        with torch.cuda.stream(stream):
-            for _ in range(k):
-                flush.zero_()
-                e0 = torch.cuda.Event(enable_timing=True)
-                e1 = torch.cuda.Event(enable_timing=True)
-                e0.record(stream)
-                n = step(mode)
-                e1.record(stream)
-                e1.synchronize()
-                ms.append(e0.elapsed_time(e1))
-                st = sess.stats()
-                ms_eval.append(st.ms_eval)
-                ops.append(st.jw_word_ops)
-                cmp.append(st.pair_comparisons)
-                launches += st.n_launches
-        return {"ms": ms, "ms_eval": ms_eval, "ops": ops, "cmp": cmp, "launches": launches,
-                "matches": n}
+    c3 = C3(args, ctx, dev)
 
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
     sampler = ClockSampler(local_rank)
     sampler.start()
-    t_wall = time.perf_counter()
-    bat = timed("batched", args.steps, args.warmup)
+    bat = c3.timed("batched", args.steps, args.warmup)
     torch.cuda.synchronize()
-    wall_batched = time.perf_counter() - t_wall
     clocks = sampler.stop()
-    pla = timed("plain", args.steps, args.warmup)
+    if dist:
+        dist.barrier()
+    pla = c3.timed("plain", args.c3_plain_steps, 1)
     total_ms, plain_ms = max_over_ranks(dist, [sum(bat["ms"]), sum(pla["ms"])], dev)
     cmp_step = bat["cmp"][0]
     value = world * cmp_step * args.steps / (total_ms / 1000.0)
-    plain_value = world * cmp_step * args.steps / (plain_ms / 1000.0)
-
-    # end to end through the one-shot C-ABI call (host tables -> host pairs)
-    e2e_steps = max(1, min(args.steps, 5))
-    hb.block(ctx, plan, L, R, w.n_partitions, hb.INT_MAX, "batched")  # warm
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        pairs, st_e2e = hb.block(ctx, plan, L, R, w.n_partitions, hb.INT_MAX, "batched")
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
-    e2e = {"value": world * st_e2e.pair_comparisons / e2e_s, "unit": UNIT,
-           "h2d_bytes_per_step": int(st_e2e.h2d_bytes),
-           "d2h_bytes_per_step": int(8 * st_e2e.n_matches + 64),
-           "ms_per_step": 1000.0 * e2e_s,
-           "ms_create": float(st_e2e.ms_create),
-           "ingest_on_device": int(st_e2e.ingest_on_device),
-           "includes": "session creation (H2D of the plan's columns from the page-locked "
-                       "host tables, device encode: std::hash partition buckets, "
-                       "dictionaries, symbol arenas) + join + evaluation + D2H of the pairs "
-                       "into host memory; the warm-up call page-locks the tables and "
-                       "memoises the measured predicate order on the plan"}
+    plain_value = world * cmp_step * args.c3_plain_steps / (plain_ms / 1000.0)
 
     line = None
     if rank == 0:
+        st = c3.sess.stats()
+        e2e = c3.e2e(ctx, args.e2e_steps)
+        e2e["value"] *= world
         peaks = _peaks()
-        props = torch.cuda.get_device_properties(dev)
-        n_sm = props.multi_processor_count
-        sm_max = float(peaks.get("sm_max_mhz") or clocks.get("sm_max_mhz") or 2070.0)
-        # 1 algorithmic op = one 64-bit word operation = 2 INT32 issue slots;
-        # an SM issues 128 INT32 lane-ops per cycle.
-        peak_tops = n_sm * 64 * sm_max * 1e6 / 1e12
+        peak = probe_scan_peak(local_rank, int(st.scan_words))
         ms_eval = statistics.mean(bat["ms_eval"])
         ops = statistics.mean(bat["ops"])
-        achieved = ops / (ms_eval / 1000.0) / 1e12
+        scan_ops = statistics.mean(bat["scan_ops"])
+        achieved_exec = scan_ops / (ms_eval / 1000.0) / 1e12
+        achieved_alg = ops / (ms_eval / 1000.0) / 1e12
+        traffic, traffic_src = _traffic_record()
         roofline = {
             "bound": "alu", "kernel": "k_eval (Jaro-Winkler pair evaluation)",
-            "achieved": achieved, "peak": peak_tops, "unit": "Tops/s (64-bit word ops)",
-            "frac": achieved / peak_tops,
-            "traffic": _traffic_per_launch(),
-            "ops_per_launch": ops, "ms_per_launch": ms_eval,
-            "pairs_scanned_per_launch": int(sess.stats().pairs_scanned),
-            "scan_steps_per_launch": int(sess.stats().scan_steps),
-            "tile_right": int(sess.stats().tile_right),
-            "eval_variant": int(sess.stats().eval_variant),
-            "peak_source": f"nominal: {n_sm} SMs x 128 INT32 lanes / 2 per 64-bit op x "
-                           f"{sm_max:.0f} MHz (sm_max_mhz of MEASURED_PEAKS.json); "
-                           "MEASURED_PEAKS.json has no integer-pipe figure",
+            "achieved": achieved_exec, "peak": peak["tops"],
+            "unit": "Tops/s (scan operations: 6 per 64-bit mask word per character)",
+            "frac": achieved_exec / peak["tops"] if peak["tops"] else None,
+            "traffic": traffic, "traffic_source": traffic_src,
+            "frac_executed": achieved_exec / peak["tops"] if peak["tops"] else None,
+            "frac_algorithmic": achieved_alg / peak["tops"] if peak["tops"] else None,
+            "achieved_algorithmic": achieved_alg,
+            "peak_source": ("measured: libhbx_probe.so hbx_probe_scan_rate, the scan step of the "
+                            "evaluation kernel with Peq rows in shared memory, 4 independent "
+                            f"chains per thread, {peak['words']} mask words, best of 1-8 CTAs "
+                            f"per SM ({json.dumps(peak['per_ctas_per_sm'])} Tops/s), this GPU, "
+                            "this run"),
+            "scan_word_ops_per_launch": scan_ops, "jw_word_ops_per_launch": ops,
+            "ms_per_launch": ms_eval, "scan_words": int(st.scan_words),
+            "pairs_scanned_per_launch": int(st.pairs_scanned),
+            "tile_right": int(st.tile_right), "eval_variant": int(st.eval_variant),
             "join_ms_per_step": statistics.mean([m - e for m, e in zip(bat["ms"], bat["ms_eval"])]),
+            "hbm_gbs_measured": peaks.get("hbm_gbs"),
         }
-        cb = None
-        if world == 1 and not args.no_cpu_baseline:
-            cb = cpu_baseline(paths, w.n_partitions)
-        extra = {}
-        if world == 1 and "c3" in args.sections:
-            extra["c3"] = bench_c3(args, ctx, dev)
-        if world == 1 and "c5" in args.sections:
-            extra["c5"] = bench_c5(args, ctx)
-        if world == 1 and "serve" in args.sections:
-            extra["serving"] = bench_serving(args, ctx)
-        if world == 1 and "io" in args.sections:
-            extra["io"] = bench_io(args, ctx, dev)
+        extra, cb, par, fp = {}, None, None, {}
+        if world == 1:
+            par, cb, fp["c3_sample"] = c3.parity(args, bat["matches"])
+        c3.close()
+        if world == 1:
+            fp["c1"] = c1_fp64()
+            if "c2" in args.sections:
+                extra["c2"] = bench_c2(args, ctx, dev)
+                fp["c2"] = extra["c2"].pop("jw_fp64")
+            if "c5" in args.sections:
+                extra["c5"] = bench_c5(args, ctx, dev)
+                fp["c5_sample"] = extra["c5"].pop("jw_fp64")
+            if "serve" in args.sections:
+                extra["serving"] = bench_serving(args, ctx)
+            if "io" in args.sections:
+                extra["io"] = bench_io(args, ctx, dev)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u32",
-            "data": "synthetic (seeded PCG64, C2 shape; no dataset download)",
-            "config": {"workload": WORKLOAD_DESC, "n_left_rows": L.n_rows, "n_right_rows": R.n_rows,
-                       "rules": 2, "n_partitions": w.n_partitions, "mode": "batched",
+            "data": "synthetic (seeded PCG64, C3 shape; no dataset download)",
+            "config": {"workload": c3_desc(c3.n), "n_left_rows": c3.L.n_rows,
+                       "n_right_rows": c3.R.n_rows, "rules": len(c3.w.rules),
+                       "n_partitions": c3.w.n_partitions, "mode": "batched",
                        "pair_comparisons_per_step": cmp_step,
-                       "pairs_covered_per_step": int(sess.stats().pairs_covered),
+                       "pairs_covered_per_step": int(st.pairs_covered),
                        "matches_per_step": int(bat["matches"]),
-                       "l2": "flushed before every timed step (256 MiB write, outside the events)",
+                       "l2": "inputs larger than L2 (about 200 MB a side); L2 also flushed "
+                             "before every timed step (256 MiB write, outside the events)",
                        "parallelism": f"replicas x{world}"},
-            "plain": {"value": plain_value, "ms_per_step": plain_ms / args.steps,
-                      "launches_per_step": pla["launches"] // max(args.steps, 1)},
+            "plain": {"value": plain_value, "ms_per_step": plain_ms / args.c3_plain_steps,
+                      "steps": args.c3_plain_steps,
+                      "ms_eval": statistics.mean(pla["ms_eval"]),
+                      "launches_per_step": pla["launches"] // max(args.c3_plain_steps, 1)},
             "batched_vs_plain": value / plain_value,
+            "ms_eval_batched": ms_eval,
             "gpu_launches": bat["launches"],
             "clocks": {k: clocks[k] for k in ("sm_mhz", "sm_max_mhz", "reasons")},
-            "wall_s_batched": wall_batched,
             "e2e": e2e,
             "roofline": roofline,
         }
         if cb:
-            line["cpu_baseline"] = {"value": cb["value"], "unit": UNIT, "cores": cb["cores"],
-                                    "kind": "port", "sample": cb["sample"]}
+            line["cpu_baseline"] = cb
+        if par:
+            line["parity"] = par
+        if fp:
+            line["jw_fp64"] = {"workloads": fp,
+                               "fp64_flips": sum(v["fp64_flips"] for v in fp.values()),
+                               "max_abs_diff": max(v["max_abs_diff"] for v in fp.values()),
+                               "set_unchanged": "the engine decides with the reference's "
+                                                "float/double arithmetic; parity blocks compare "
+                                                "its set with the oracle's"}
         line.update(extra)
         print(json.dumps(line), flush=True)
-    sess.close()
+    else:
+        c3.close()
     ctx.close()
     if dist:
         dist.barrier()
@@ -641,22 +857,27 @@ def run_engine(args, rank, world, local_rank):
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
-    ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--sections", default="c3,serve",
-                    help="extra measurements at N=1, comma separated: c3 (1M x 1M batching "
-                         "workload), serve (resident-table serving trace), c5 (long strings, "
-                         "one-shot vs streamed partition windows; minutes), io (CSV "
-                         "tokenization and pair-file writing, device vs host); '' for none")
+    ap.add_argument("--sections", default="c2,c5,serve",
+                    help="extra measurements at N=1, comma separated: c2 (2,600 x 64,263 rows, "
+                         "checked in full), c5 (long strings, one-shot vs streamed partition "
+                         "windows), serve (resident-table serving trace), io (CSV tokenization "
+                         "and pair-file writing, device vs host); '' for none")
     ap.add_argument("--c3-rows", type=int, default=1_000_000)
-    ap.add_argument("--c3-steps", type=int, default=2)
+    ap.add_argument("--c3-plain-steps", type=int, default=2)
+    ap.add_argument("--c3-sample-per-part", type=int, default=64)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--ref-per-part", type=int, default=16)
+    ap.add_argument("--c2-steps", type=int, default=20)
     ap.add_argument("--c5-rows", type=int, default=500_000)
     ap.add_argument("--c5-window-mb", type=int, default=512)
+    ap.add_argument("--c5-sample-per-part", type=int, default=16)
     ap.add_argument("--serve-rows", type=int, default=10_000_000)
     ap.add_argument("--serve-requests", type=int, default=800)
     ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--serve-check", type=int, default=6)
     ap.add_argument("--io-rows", type=int, default=1_000_000)
     ap.add_argument("--io-pairs", type=int, default=20_000_000)
     ap.add_argument("--io-reps", type=int, default=3)

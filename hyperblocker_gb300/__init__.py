@@ -460,19 +460,25 @@ class Session:
 
 def block(ctx: Context, plan: Plan, left: Table, right: Table, n_partitions: int = 1,
           prefix_idx: int = INT_MAX, mode="batched", capacity: Optional[int] = None,
-          stream_ptr: Optional[int] = None):
+          stream_ptr: Optional[int] = None, out=None):
     """Host tables -> (pairs (n, 2) uint32 of (left row, right row), stats).
 
     ``hbx_block`` writes nothing when the output buffer is too small (it
     reports the size needed and the call is repeated), so without an explicit
     ``capacity`` the buffer is sized from the largest result seen on this
-    context, with a quarter of headroom.
+    context, with a quarter of headroom.  ``out`` = (left rows, right rows),
+    two uint32 host arrays the caller keeps between calls, is used when it is
+    large enough (the returned pairs are then views of them).
     """
     if capacity is None:
         capacity = getattr(ctx, "_capacity_hint", 1 << 16)
     while True:
-        ol = np.empty(max(capacity, 1), dtype=np.uint32)
-        orr = np.empty(max(capacity, 1), dtype=np.uint32)
+        if out is not None and len(out[0]) >= capacity and len(out[1]) >= capacity:
+            ol, orr = out
+            capacity = min(len(ol), len(orr))
+        else:
+            ol = np.empty(max(capacity, 1), dtype=np.uint32)
+            orr = np.empty(max(capacity, 1), dtype=np.uint32)
         p = Pairs(ol.ctypes.data, orr.ctypes.data, capacity, 0, 0)
         s = Stats()
         st = lib().hbx_block(ctx.h, plan.h, left.h, right.h, n_partitions, prefix_idx, _mode(mode),

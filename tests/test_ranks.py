@@ -59,7 +59,7 @@ def test_reference_arm_runs_on_rank_zero_only():
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node=2",
            "--master-addr", "127.0.0.1", "--master-port", str(port),
            os.path.join(ROOT, "bench.py"), "--impl", "reference", "--gpus", "2", "--steps", "1",
-           "--warmup", "3"]
+           "--warmup", "3", "--c3-rows", "20000", "--ref-per-part", "4"]
     r = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=ROOT)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
@@ -72,7 +72,7 @@ def test_reference_arm_runs_on_rank_zero_only():
 
     assert line["metric"] == bench.METRIC and line["unit"] == bench.UNIT
     assert line["higher_is_better"] is True and line["steps"] == 1 and line["warmup"] == 3
-    assert line["config"]["workload"] == bench.WORKLOAD_DESC
+    assert line["config"]["workload"] == bench.c3_desc(20000)
     cb = line["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == line["value"] and cb["sample"]
     e2e = line["e2e"]
