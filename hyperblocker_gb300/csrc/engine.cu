@@ -329,7 +329,11 @@ void setup_session(hbx_session* S, uint64_t h2d_tables) {
       }
   S->bound_idx.upload(idx, st);
   S->bound_val.alloc(idx.size());
-  const uint64_t cap0 = std::max<uint64_t>(1 << 16, S->out_hint);
+  // output slots (and the duplicate set, twice as many) for the caller's
+  // capacity, but never more than the partitions can hold: a generous caller
+  // buffer does not size device buffers by itself
+  const uint64_t cap0 =
+      std::max<uint64_t>(1 << 16, std::min<uint64_t>(S->out_hint, E.pairs_covered + 1));
   S->out_l.alloc(cap0);
   S->out_r.alloc(cap0);
   if (E.rules.size() > 1) {

@@ -21,7 +21,6 @@ namespace hbx {
 namespace probe {
 
 constexpr int kThreads = 256;
-constexpr int kChains = 4;     // independent scans per thread
 constexpr int kSymbols = 128;  // Peq rows of the table
 
 __device__ __forceinline__ uint32_t mix(uint32_t x) {
@@ -33,7 +32,8 @@ __device__ __forceinline__ uint32_t mix(uint32_t x) {
   return x;
 }
 
-template <int W>
+// kChains independent scans per thread, each over W-word masks.
+template <int W, int kChains>
 __global__ void __launch_bounds__(kThreads) k_scan_rate(uint32_t iters, uint32_t seed,
                                                          uint32_t* sink) {
   constexpr int S = dev::row_words(W);
@@ -87,10 +87,11 @@ extern "C" {
 
 // Runs the scan-rate probe for W 32-bit words per mask (1, 2, 4 or 8) on
 // `device`, grid = SMs x blocks_per_sm blocks of 256 threads, each thread
-// running 4 chains of iters x 16 characters; *ops_per_s = operations of the
-// roofline's unit per second (CUDA events around the launch, after one
-// untimed launch), *ms = the launch's time.  Returns 0, or the CUDA error.
-int hbx_probe_scan_rate(int device, int words, int blocks_per_sm, uint32_t iters,
+// running `chains` (4 or 8) independent scans of iters x 16 characters;
+// *ops_per_s = operations of the roofline's unit per second (CUDA events
+// around the launch, after one untimed launch), *ms = the launch's time.
+// Returns 0, or the CUDA error.
+int hbx_probe_scan_rate(int device, int words, int chains, int blocks_per_sm, uint32_t iters,
                         double* ops_per_s, double* ms) {
   using namespace hbx::probe;
   cudaError_t e = cudaSetDevice(device);
@@ -100,11 +101,16 @@ int hbx_probe_scan_rate(int device, int words, int blocks_per_sm, uint32_t iters
   if (e != cudaSuccess) return (int)e;
   if (blocks_per_sm < 1 || blocks_per_sm > 8 || iters < 1) return (int)cudaErrorInvalidValue;
   void (*kern)(uint32_t, uint32_t, uint32_t*) = nullptr;
-  switch (words) {
-    case 1: kern = k_scan_rate<1>; break;
-    case 2: kern = k_scan_rate<2>; break;
-    case 4: kern = k_scan_rate<4>; break;
-    case 8: kern = k_scan_rate<8>; break;
+  if (chains != 4 && chains != 8) return (int)cudaErrorInvalidValue;
+  switch (words * 16 + chains) {
+    case 1 * 16 + 4: kern = k_scan_rate<1, 4>; break;
+    case 2 * 16 + 4: kern = k_scan_rate<2, 4>; break;
+    case 4 * 16 + 4: kern = k_scan_rate<4, 4>; break;
+    case 8 * 16 + 4: kern = k_scan_rate<8, 4>; break;
+    case 1 * 16 + 8: kern = k_scan_rate<1, 8>; break;
+    case 2 * 16 + 8: kern = k_scan_rate<2, 8>; break;
+    case 4 * 16 + 8: kern = k_scan_rate<4, 8>; break;
+    case 8 * 16 + 8: kern = k_scan_rate<8, 8>; break;
     default: return (int)cudaErrorInvalidValue;
   }
   const int grid = n_sm * blocks_per_sm;
@@ -126,7 +132,7 @@ int hbx_probe_scan_rate(int device, int words, int blocks_per_sm, uint32_t iters
   if (e1) cudaEventDestroy(e1);
   cudaFree(sink);
   if (e != cudaSuccess) return (int)e;
-  const double chars = (double)n_threads * kChains * (double)iters * 16.0;
+  const double chars = (double)n_threads * chains * (double)iters * 16.0;
   if (ms) *ms = t;
   if (ops_per_s) *ops_per_s = chars * 3.0 * words / (t / 1000.0);
   return 0;
