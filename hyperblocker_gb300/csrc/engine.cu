@@ -63,8 +63,10 @@ struct hbx_session {
   hbx::Encoded E;
   hbx::SideBufs L, R;
   std::vector<hbx::RuleBufs> rb;
-  std::vector<hbx::dev::Rule> h_rules;
-  hbx::DBuf<hbx::dev::Rule> d_rules;
+  // the rules, each evaluated on its own (plain form, and every join), and
+  // the same rules grouped for the batched form (group_rules)
+  std::vector<hbx::dev::Rule> h_rules, h_groups;
+  hbx::DBuf<hbx::dev::Rule> d_rules, d_groups;
   hbx::DBuf<unsigned long long> d_rule_base;
   hbx::DBuf<hbx::dev::Counters> d_ctr;
   hbx::dev::Counters* h_ctr = nullptr;  // page-locked copy of d_ctr (the context's), written by each run
@@ -155,6 +157,8 @@ void configure(hbx_session* S, uint32_t tile_right, int variant) {
   S->smem_bytes = (size_t)S->warp_words * 4 * dev::kWarpsPerCta;
   HBX_CUDA(cudaMemcpyAsync(S->d_rules.p, S->h_rules.data(), S->h_rules.size() * sizeof(dev::Rule),
                            cudaMemcpyHostToDevice, C->stream));
+  HBX_CUDA(cudaMemcpyAsync(S->d_groups.p, S->h_groups.data(), S->h_groups.size() * sizeof(dev::Rule),
+                           cudaMemcpyHostToDevice, C->stream));
   HBX_CUDA(cudaStreamSynchronize(C->stream));
   raise_smem_limit(kern, S->smem_bytes);
   int bps = 0;
@@ -203,6 +207,8 @@ uint64_t upload_host_encoding(hbx_session* S) {
   return h2d;
 }
 
+std::vector<dev::Rule> group_rules(const std::vector<dev::Rule>& singles);
+
 // Device state of a session whose side buffers hold the encoded tables.
 void setup_session(hbx_session* S, uint64_t h2d_tables) {
   hbx_ctx* C = S->ctx;
@@ -248,6 +254,7 @@ void setup_session(hbx_session* S, uint64_t h2d_tables) {
     d.n_wclass = split ? dev::kWordClasses : 1u;
     d.wclass_slot = split ? (uint32_t)re.sim_slot_l[0] : 0u;
     d.domain_l = d.n_wclass * d.domain;
+    dev::make_singleton(&d);
     RuleBufs& b = S->rb[r];
     b.key_l.alloc(nL);
     b.key_r.alloc(nR);
@@ -290,7 +297,9 @@ void setup_session(hbx_session* S, uint64_t h2d_tables) {
     const uint32_t nb = (max_d + dev::kScanChunk - 1) / dev::kScanChunk;
     if (S->fused_join) S->scan_totals.alloc((size_t)S->h_rules.size() * 3 * nb);
   }
+  S->h_groups = group_rules(S->h_rules);
   S->d_rules.alloc(E.rules.size());
+  S->d_groups.alloc(E.rules.size());
   S->d_rule_base.alloc(E.rules.size() + 1);
   S->d_ctr.alloc(1);
   // one page-locked counter block per context: its sessions run one at a time
@@ -353,6 +362,126 @@ void setup_session(hbx_session* S, uint64_t h2d_tables) {
   S->stats.n_partitions_used = E.n_partitions_used;
 }
 
+// Groups of the batched form (dev::Rule, "Group evaluation"), from the
+// rules in plan order, each a singleton: a rule joins the first group whose
+// root's equality slots it contains (its candidates are a subset of the
+// root's) and whose first similarity column it also tests, up to
+// dev::kMaxMembers members and dev::kMaxEq distinct extra slots.  Rules are
+// taken fewest equalities first, so roots are the coarsest joins.  A new root
+// puts first, among its own similarity columns, the one that the most
+// remaining rules could share.  Rules without similarity predicates stay on
+// their own.  The result keeps every rule at its index; members get
+// n_members = 0.
+std::vector<dev::Rule> group_rules(const std::vector<dev::Rule>& singles) {
+  std::vector<dev::Rule> g = singles;
+  const size_t n = g.size();
+  auto eqset = [&](size_t r) {
+    std::vector<uint32_t> v(singles[r].eq_slot, singles[r].eq_slot + singles[r].n_eq);
+    std::sort(v.begin(), v.end());
+    v.erase(std::unique(v.begin(), v.end()), v.end());
+    return v;
+  };
+  auto contains = [](const std::vector<uint32_t>& big, const std::vector<uint32_t>& small) {
+    return std::includes(big.begin(), big.end(), small.begin(), small.end());
+  };
+  auto has_col = [&](size_t r, uint32_t sl, uint32_t sr) {
+    for (uint32_t k = 0; k < singles[r].n_sim; k++)
+      if (singles[r].sim_l[k] == sl && singles[r].sim_r[k] == sr) return true;
+    return false;
+  };
+  std::vector<size_t> order(n);
+  for (size_t i = 0; i < n; i++) order[i] = i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](size_t a, size_t b) { return singles[a].n_eq < singles[b].n_eq; });
+  std::vector<int> root_of(n, -1);
+  std::vector<size_t> roots;
+  for (size_t oi = 0; oi < n; oi++) {
+    const size_t r = order[oi];
+    if (singles[r].n_sim == 0) continue;
+    const std::vector<uint32_t> er = eqset(r);
+    bool placed = false;
+    for (size_t root : roots) {
+      dev::Rule& G = g[root];
+      if (G.n_members >= dev::kMaxMembers) continue;
+      if (!contains(er, eqset(root)) || !has_col(r, G.sim_l[0], G.sim_r[0])) continue;
+      // the extra slots this member needs, added to the group's list
+      std::vector<uint32_t> er_root = eqset(root), extra;
+      std::set_difference(er.begin(), er.end(), er_root.begin(), er_root.end(),
+                          std::back_inserter(extra));
+      uint32_t nx = G.n_xslots, xmask = 0;
+      uint32_t xs[dev::kMaxEq];
+      std::copy(G.xslot, G.xslot + G.n_xslots, xs);
+      bool fits = true;
+      for (uint32_t slot : extra) {
+        uint32_t j = 0;
+        while (j < nx && xs[j] != slot) j++;
+        if (j == nx) {
+          if (nx == (uint32_t)dev::kMaxEq) {
+            fits = false;
+            break;
+          }
+          xs[nx++] = slot;
+        }
+        xmask |= 1u << j;
+      }
+      if (!fits) continue;
+      G.n_xslots = nx;
+      std::copy(xs, xs + nx, G.xslot);
+      dev::Member& M = G.mem[G.n_members++];
+      M = dev::Member{};
+      M.xmask = xmask;
+      M.thr_first = -1e30f;
+      const dev::Rule& R = singles[r];
+      for (uint32_t k = 0; k < R.n_sim; k++) {
+        if (R.sim_l[k] == G.sim_l[0] && R.sim_r[k] == G.sim_r[0]) {
+          M.thr_first = std::max(M.thr_first, R.thr[k]);  // both must hold: the larger decides
+        } else {
+          M.rest_l[M.n_rest] = R.sim_l[k];
+          M.rest_r[M.n_rest] = R.sim_r[k];
+          M.rest_thr[M.n_rest] = R.thr[k];
+          M.n_rest++;
+        }
+      }
+      G.thr_min = std::min(G.thr_min, M.thr_first);
+      g[r].n_members = 0;
+      root_of[r] = (int)root;
+      placed = true;
+      break;
+    }
+    if (placed) continue;
+    // a new root: its first column is the one most later rules could share
+    dev::Rule& G = g[r];
+    uint32_t best_k = 0, best_n = 0;
+    for (uint32_t k = 0; k < G.n_sim; k++) {
+      uint32_t cnt = 0;
+      for (size_t oj = oi + 1; oj < n; oj++) {
+        const size_t q = order[oj];
+        if (singles[q].n_sim && contains(eqset(q), er) && has_col(q, G.sim_l[k], G.sim_r[k])) cnt++;
+      }
+      if (cnt > best_n) {
+        best_n = cnt;
+        best_k = k;
+      }
+    }
+    if (best_k) {  // move that predicate to the front, the others keep their order
+      const uint32_t sl = G.sim_l[best_k], sr = G.sim_r[best_k];
+      const float t = G.thr[best_k];
+      for (uint32_t k = best_k; k > 0; k--) {
+        G.sim_l[k] = G.sim_l[k - 1];
+        G.sim_r[k] = G.sim_r[k - 1];
+        G.thr[k] = G.thr[k - 1];
+      }
+      G.sim_l[0] = sl;
+      G.sim_r[0] = sr;
+      G.thr[0] = t;
+      if (G.n_wclass > 1) G.wclass_slot = sl;
+    }
+    dev::make_singleton(&G);
+    roots.push_back(r);
+  }
+  return g;
+}
+
 __global__ void k_gather_bounds(const dev::Rule* rules, uint32_t n_rules, uint32_t per_rule,
                                 const uint32_t* idx, unsigned long long* out) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -360,8 +489,11 @@ __global__ void k_gather_bounds(const dev::Rule* rules, uint32_t n_rules, uint32
   out[i] = rules[i / per_rule].item_off[idx[i]];
 }
 
-// Enqueues counter reset + the joins of every rule.  Returns launches.
-uint32_t enqueue_join(hbx_session* S, cudaStream_t st) {
+// Enqueues counter reset + the joins of every rule, with the rule array
+// `rules` (d_rules or d_groups: the same join state; in d_groups a group's
+// first column may lead another predicate, and members have no items).
+// Returns launches.
+uint32_t enqueue_join(hbx_session* S, cudaStream_t st, const dev::Rule* rules) {
   uint32_t launches = 1;  // k_reset
   {  // counters, histograms and the duplicate set, one launch
     const uint64_t n_seen = S->seen.p ? S->seen.n : 0;
@@ -380,18 +512,18 @@ uint32_t enqueue_join(hbx_session* S, cudaStream_t st) {
     const dim3 grid(row_grid(std::max(nL, nR), n_sm), n_rules, 2);
     const uint32_t nb = (max_d + dev::kScanChunk - 1) / dev::kScanChunk;
     unsigned long long* comparisons = &S->d_ctr.p->comparisons;
-    dev::k_join_count<<<grid, 256, smem, st>>>(S->side_l, S->side_r, S->d_rules.p);
+    dev::k_join_count<<<grid, 256, smem, st>>>(S->side_l, S->side_r, rules);
     const bool two_pass = nb > dev::kJoinScanLoopChunks;
     if (two_pass) {
       dev::k_join_scan_totals<<<dim3(nb, 3, n_rules), 1024, 0, st>>>(
-          S->d_rules.p, S->tile_right, nb, S->scan_totals.p, comparisons);
+          rules, S->tile_right, nb, S->scan_totals.p, comparisons);
       dev::k_join_scan_final<<<dim3(nb, 3, n_rules), 1024, 0, st>>>(
-          S->d_rules.p, S->tile_right, nb, S->scan_totals.p, nullptr);
+          rules, S->tile_right, nb, S->scan_totals.p, nullptr);
     } else {  // one block per (y, rule) walks the chunks
-      dev::k_join_scan_final<<<dim3(1, 3, n_rules), 1024, 0, st>>>(S->d_rules.p, S->tile_right, nb,
+      dev::k_join_scan_final<<<dim3(1, 3, n_rules), 1024, 0, st>>>(rules, S->tile_right, nb,
                                                                    nullptr, comparisons);
     }
-    dev::k_join_scatter<<<grid, 256, 0, st>>>(S->side_l, S->side_r, S->d_rules.p, n_rules,
+    dev::k_join_scatter<<<grid, 256, 0, st>>>(S->side_l, S->side_r, rules, n_rules,
                                                S->d_rule_base.p, &S->d_ctr.p->items_total);
     launch_check("join kernels");
     return launches + (two_pass ? 4 : 3);
@@ -400,24 +532,24 @@ uint32_t enqueue_join(hbx_session* S, cudaStream_t st) {
     RuleBufs& b = S->rb[r];
     const uint32_t D = S->h_rules[r].domain;
     const uint32_t DL = S->h_rules[r].domain_l;
-    if (nL) dev::k_keys_hist<<<row_grid(nL, n_sm), 256, 0, st>>>(S->side_l, S->d_rules.p, (uint32_t)r, 0);
-    if (nR) dev::k_keys_hist<<<row_grid(nR, n_sm), 256, 0, st>>>(S->side_r, S->d_rules.p, (uint32_t)r, 1);
+    if (nL) dev::k_keys_hist<<<row_grid(nL, n_sm), 256, 0, st>>>(S->side_l, rules, (uint32_t)r, 0);
+    if (nR) dev::k_keys_hist<<<row_grid(nR, n_sm), 256, 0, st>>>(S->side_r, rules, (uint32_t)r, 1);
     dev::k_scan_partial_u32<<<b.nb_l, 1024, 0, st>>>(S->h_rules[r].cnt_l, DL, b.part_u32.p);
     dev::k_scan_top_u32<<<1, 1024, 0, st>>>(b.part_u32.p, b.nb_l);
     dev::k_scan_final_u32<<<b.nb_l, 1024, 0, st>>>(S->h_rules[r].cnt_l, DL, b.part_u32.p, b.off_l.p);
     dev::k_scan_partial_u32<<<b.nb, 1024, 0, st>>>(S->h_rules[r].cnt_r, D, b.part_u32.p);
     dev::k_scan_top_u32<<<1, 1024, 0, st>>>(b.part_u32.p, b.nb);
     dev::k_scan_final_u32<<<b.nb, 1024, 0, st>>>(S->h_rules[r].cnt_r, D, b.part_u32.p, b.off_r.p);
-    dev::k_items_partial<<<b.nb_l, 1024, 0, st>>>(S->d_rules.p, (uint32_t)r, S->tile_right,
+    dev::k_items_partial<<<b.nb_l, 1024, 0, st>>>(rules, (uint32_t)r, S->tile_right,
                                                   b.part_u64.p, &S->d_ctr.p->comparisons);
     dev::k_scan_top_u64<<<1, 1024, 0, st>>>(b.part_u64.p, b.nb_l);
-    dev::k_items_final<<<b.nb_l, 1024, 0, st>>>(S->d_rules.p, (uint32_t)r, S->tile_right,
+    dev::k_items_final<<<b.nb_l, 1024, 0, st>>>(rules, (uint32_t)r, S->tile_right,
                                                 b.part_u64.p);
-    if (nL) dev::k_scatter<<<row_grid(nL, n_sm), 256, 0, st>>>(S->side_l, S->d_rules.p, (uint32_t)r, 0);
-    if (nR) dev::k_scatter<<<row_grid(nR, n_sm), 256, 0, st>>>(S->side_r, S->d_rules.p, (uint32_t)r, 1);
+    if (nL) dev::k_scatter<<<row_grid(nL, n_sm), 256, 0, st>>>(S->side_l, rules, (uint32_t)r, 0);
+    if (nR) dev::k_scatter<<<row_grid(nR, n_sm), 256, 0, st>>>(S->side_r, rules, (uint32_t)r, 1);
     launches += 9 + (nL ? 2 : 0) + (nR ? 2 : 0);
   }
-  dev::k_rule_base<<<1, 32, 0, st>>>(S->d_rules.p, n_rules, S->d_rule_base.p,
+  dev::k_rule_base<<<1, 32, 0, st>>>(rules, n_rules, S->d_rule_base.p,
                                      &S->d_ctr.p->items_total);
   launches++;
   launch_check("join kernels");
@@ -445,11 +577,11 @@ void fit_seen(hbx_session* S, uint64_t pairs) {
   }
 }
 
-dev::EvalParams eval_params(hbx_session* S) {
+dev::EvalParams eval_params(hbx_session* S, const dev::Rule* rules) {
   dev::EvalParams P{};
   P.L = S->side_l;
   P.R = S->side_r;
-  P.rules = S->d_rules.p;
+  P.rules = rules;
   P.n_rules = (uint32_t)S->rb.size();
   P.n_symbols = S->E.n_symbols;
   P.rule_item_base = S->d_rule_base.p;
@@ -477,9 +609,10 @@ uint32_t enqueue_batched(hbx_session* S, cudaStream_t st) {
   const unsigned rec_flags =
       cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
   HBX_CUDA(cudaEventRecordWithFlags(S->ev0, st, rec_flags));
-  uint32_t launches = enqueue_join(S, st);
-  dev::EvalParams P = eval_params(S);
-  P.n_seg = 0;  // every work item of every rule
+  // the batched form evaluates rule groups: one join's items for several rules
+  uint32_t launches = enqueue_join(S, st, S->d_groups.p);
+  dev::EvalParams P = eval_params(S, S->d_groups.p);
+  P.n_seg = 0;  // every work item of every group
   const int grid = S->ctx->n_sm * S->blocks_per_sm;
   HBX_CUDA(cudaEventRecordWithFlags(S->ev_eval0, st, rec_flags));
   dev::eval_kernel(S->variant)<<<grid, kThreads, S->smem_bytes, st>>>(P);
@@ -565,7 +698,7 @@ dev::Counters run_once(hbx_session* S, hbx_mode mode, cudaStream_t st, uint32_t*
   }
   // PLAIN: join, then one launch per (partition, rule)
   HBX_CUDA(cudaEventRecord(S->ev0, st));
-  uint32_t n = enqueue_join(S, st);
+  uint32_t n = enqueue_join(S, st, S->d_rules.p);
   const uint32_t n_rules = (uint32_t)S->rb.size();
   const uint32_t per_class = (uint32_t)S->E.n_partitions + 1;
   const uint32_t per_rule = per_class * dev::kWordClasses;
@@ -580,7 +713,7 @@ dev::Counters run_once(hbx_session* S, hbx_mode mode, cudaStream_t st, uint32_t*
   HBX_CUDA(cudaMemcpyAsync(base.data(), S->d_rule_base.p, (n_rules + 1) * sizeof(unsigned long long),
                            cudaMemcpyDeviceToHost, st));
   HBX_CUDA(cudaStreamSynchronize(st));
-  dev::EvalParams P = eval_params(S);
+  dev::EvalParams P = eval_params(S, S->d_rules.p);
   const int max_grid = S->ctx->n_sm * S->blocks_per_sm;
   HBX_CUDA(cudaEventRecord(S->ev_eval0, st));
   for (uint64_t p = 0; p < S->E.n_partitions; p++) {
@@ -632,7 +765,7 @@ std::string autotune_path() {
 
 std::string workload_signature(const hbx_session* S) {
   std::string sig = S->ctx->device_name;
-  sig += "|k2";  // evaluation kernel generation: entries of earlier kernels do not apply
+  sig += "|k3";  // evaluation kernel generation: entries of earlier kernels do not apply
   auto bucket = [](uint64_t n) {  // power-of-two bucket
     uint32_t b = 0;
     while ((1ull << b) < n) b++;

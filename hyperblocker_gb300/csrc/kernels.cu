@@ -35,6 +35,7 @@ __global__ void k_keys_hist(Side S, const Rule* rules, uint32_t rule, int side) 
 
 __global__ void k_scatter(Side S, const Rule* rules, uint32_t rule, int side) {
   const Rule& R = rules[rule];
+  if (!R.n_members) return;  // evaluated in another rule's group: no items of its own
   const uint32_t* keys = side ? R.key_r : R.key_l;
   const uint32_t* off = side ? R.off_r : R.off_l;
   uint32_t* cur = side ? R.cur_r : R.cur_l;
@@ -342,7 +343,8 @@ __global__ void k_join_scatter(Side L, Side R, const Rule* rules, uint32_t n_rul
     unsigned long long acc = 0;
     for (uint32_t r = 0; r < n_rules; r++) {
       rule_base[r] = acc;
-      acc += rules[r].item_off[rules[r].domain_l];
+      // a rule evaluated in another rule's group has no items of its own
+      if (rules[r].n_members) acc += rules[r].item_off[rules[r].domain_l];
     }
     rule_base[n_rules] = acc;
     if (items_total) *items_total = acc;
@@ -350,6 +352,7 @@ __global__ void k_join_scatter(Side L, Side R, const Rule* rules, uint32_t n_rul
   const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x;
   const Rule& Q = rules[blockIdx.y];
+  if (!Q.n_members) return;  // evaluated in another rule's group: counted, never enumerated
   if (blockIdx.z == 0) {
     for (uint32_t row = t0; row < L.n_rows; row += stride) {
       const uint32_t k = Q.key_l[row];
@@ -372,7 +375,7 @@ __global__ void k_rule_base(const Rule* rules, uint32_t n_rules, unsigned long l
     unsigned long long acc = 0;
     for (uint32_t r = 0; r < n_rules; r++) {
       base[r] = acc;
-      acc += rules[r].item_off[rules[r].domain_l];
+      if (rules[r].n_members) acc += rules[r].item_off[rules[r].domain_l];
     }
     base[n_rules] = acc;
     if (items_total) *items_total = acc;
@@ -561,6 +564,61 @@ __device__ __noinline__ bool sim_pass_slow(const uint8_t* a, uint32_t la, const 
   return jw_exact(m, mn, max(la, lb), p, thr, &ctr->ambiguous);
 }
 
+// The match count and common prefix of one pair by the reference's own
+// loops (any lengths; 0 and 0 when a string is empty), for decisions against
+// several thresholds.  Out of line like sim_pass_slow.
+__device__ __noinline__ void sim_m_slow(const uint8_t* a, uint32_t la, const uint8_t* b,
+                                        uint32_t lb, Counters* ctr, uint32_t* m, uint32_t* p) {
+  *m = 0;
+  *p = 0;
+  if (la == 0 || lb == 0) return;
+  const uint32_t mn = min(la, lb);
+  if (mn > 256) atomicAdd(&ctr->long_pairs, 1ull);
+  *m = jaro_m_ref(a, la, b, lb);
+  *p = prefix_len(a, b, mn);
+}
+
+// Threshold decision on one similarity column of a pair from its match
+// count m and common prefix p (la, lb: left and right lengths); an empty
+// string takes the reference's rule for empty strings (device_func.cuh:65-69).
+__device__ __forceinline__ bool decide(uint32_t m, uint32_t la, uint32_t lb, uint32_t p, float thr,
+                                       unsigned long long* ambiguous) {
+  if (la == 0 || lb == 0) return jw_exact(0, la, lb, 0, thr, ambiguous);
+  return jw_decide(m, min(la, lb), max(la, lb), p, thr, ambiguous);
+}
+
+// Members of `live` whose threshold on the group's first column the pair
+// reaches.
+__device__ __forceinline__ uint32_t first_pass(const Rule* R, uint32_t live, uint32_t m,
+                                               uint32_t la, uint32_t lb, uint32_t p,
+                                               unsigned long long* ambiguous) {
+  uint32_t out = 0;
+  for (uint32_t x = live; x; x &= x - 1) {
+    const uint32_t k = (uint32_t)__ffs(x) - 1u;
+    if (decide(m, la, lb, p, R->mem[k].thr_first, ambiguous)) out |= 1u << k;
+  }
+  return out;
+}
+
+// Does a member of `pass` have no predicate left (the pair matches)?
+__device__ __forceinline__ bool member_done(const Rule* R, uint32_t pass) {
+  for (uint32_t x = pass; x; x &= x - 1)
+    if (R->mem[__ffs(x) - 1].n_rest == 0) return true;
+  return false;
+}
+
+// Smallest first-column threshold of the live members: the threshold the
+// filters and the scan's early stop use.  A NaN threshold never fails a pair
+// (the reference compares JW < thr), so it makes the bound NaN: no bound.
+__device__ __forceinline__ float live_thr(const Rule* R, uint32_t live) {
+  float t = 3.0e38f;
+  for (uint32_t x = live; x; x &= x - 1) {
+    const float u = R->mem[__ffs(x) - 1].thr_first;
+    t = (u != u || t != t) ? __int_as_float(0x7fc00000) : fminf(t, u);
+  }
+  return t;
+}
+
 __device__ __forceinline__ uint32_t find_key(const unsigned long long* item_off, uint32_t domain,
                                              unsigned long long local) {
   uint32_t lo = 0, hi = domain;  // item_off[lo] <= local < item_off[hi]
@@ -697,19 +755,26 @@ __device__ __forceinline__ const uint32_t* peq_table(const EvalParams& P, uint32
 
 // Ring of pairs waiting for a scan, kRingEntries entries of three 16-byte
 // records per warp:
-//   {right row, right offset / 16, right length, need | p << 10 | s << 15 | kAdvance?}
+//   {right row, right offset / 16, right length, tag}
 //   {first 16 symbols of the right string}
 //   {left row, left length, left offset / 16, rule}
-// for the similarity predicate s of the rule.  A kAdvance entry is a pair
-// that passed predicate s without a scan: the lane that takes it goes on
-// with predicate s + 1.
+// tag = need | p << 10 | s << 15 | kAdvance? | live << 19 | member << 27.
+// A plain entry waits for the scan of its group's first column: `live` holds
+// the members whose extra equalities hold, need the matches the smallest of
+// their thresholds needs and p the common prefix (or kPrefixUnknown).  A
+// kAdvance entry passed the first column (live = the members that passed):
+// the lane that takes it goes on with predicate s of member `member`.
 constexpr uint32_t kRing = kRingEntries;
 constexpr uint32_t kPrefixUnknown = 31u;  // common prefix longer than 16: measured at the scan
 constexpr uint32_t kAdvance = 1u << 18;
 
-__device__ __forceinline__ uint32_t ring_tag(uint32_t need, uint32_t p, uint32_t s) {
-  return need | (p << 10) | (s << 15);
+__device__ __forceinline__ uint32_t ring_tag(uint32_t need, uint32_t p, uint32_t s, uint32_t live,
+                                             uint32_t member) {
+  return need | (p << 10) | (s << 15) | (live << 19) | (member << 27);
 }
+__device__ __forceinline__ uint32_t tag_live(uint32_t t) { return (t >> 19) & 0xffu; }
+__device__ __forceinline__ uint32_t tag_member(uint32_t t) { return (t >> 27) & 7u; }
+__device__ __forceinline__ uint32_t tag_s(uint32_t t) { return (t >> 15) & 7u; }
 
 // Bit-parallel scan state of one lane: the pair's Peq table and right
 // string, the symbols in hand (cur) and the next 16 (nxt), the window and
@@ -762,11 +827,12 @@ __device__ __forceinline__ bool scan_begin(Scan<W>& z, const uint32_t* tab, cons
 }
 
 // One scan step of 16 symbols, the chunk in hand (the next chunk was asked
-// for one step earlier); after each, the pair stops once even
-// matching every remaining symbol stays below its bound.  Returns true when
-// the pair is decided (*pass = the decision).
+// for one step earlier); after each, the pair stops once even matching every
+// remaining symbol stays below its bound.  Returns 0 (not decided yet), 1
+// (the scan is complete: *m = the match count) or 2 (the pair cannot reach
+// the scan's threshold).
 template <int W>
-__device__ __forceinline__ bool scan_step(Scan<W>& z, bool* pass, Counters* ctr, WorkTally* ops) {
+__device__ __forceinline__ int scan_step(Scan<W>& z, uint32_t* m_out, WorkTally* ops) {
   constexpr int S = row_words(W);
   if (z.i) {
     // chunk i/16 arrived one chunk ago; ask for the one after it
@@ -785,64 +851,73 @@ __device__ __forceinline__ bool scan_step(Scan<W>& z, bool* pass, Counters* ctr,
   uint32_t m = 0;
 #pragma unroll
   for (int k = 0; k < W; k++) m += __popc(z.mt[k]);
-  if (z.i >= z.n_iter) {
-    *pass = jw_decide(m, z.ls, z.ll, z.p, z.thr, &ctr->ambiguous);
-    return true;
-  }
-  if ((int)(z.i - m) > z.allowed) {
-    *pass = false;  // even matching every remaining symbol stays below
-    return true;
-  }
-  return false;
+  *m_out = m;
+  if (z.i >= z.n_iter) return 1;
+  if ((int)(z.i - m) > z.allowed) return 2;  // even matching every remaining symbol stays below
+  return 0;
 }
 
-// The similarity predicates after predicate s of a pair that passed it, in
-// order, until one needs a scan (returns 2, the scan state set up and s its
-// index), one fails (0) or all pass (1).  Each predicate first goes through
-// the filters of the first one: length bound, common prefix, count
-// signatures.
+// The similarity predicates after the group's first column, for the live
+// members of a pair's group in member order, from predicate *s of member
+// *mi: until one needs a scan (returns 2, the scan state set up for (*mi,
+// *s)), a member passes all of its predicates (1: the pair matches) or no
+// member is left (0).  A member drops out at its first failing predicate.
+// Each predicate first goes through the filters of the first column: length
+// bound, common prefix, count signatures.
 template <int W>
-__device__ __forceinline__ int advance(const EvalParams& P, uint32_t rule, uint32_t* s,
-                                       uint32_t lrow, uint32_t rrow, Scan<W>& z, WorkTally* ops) {
+__device__ __forceinline__ int advance_group(const EvalParams& P, uint32_t rule, uint32_t* live,
+                                             uint32_t* mi, uint32_t* s, uint32_t lrow,
+                                             uint32_t rrow, Scan<W>& z, WorkTally* ops) {
   const Rule* R = P.rules + rule;
-  const uint32_t n_sim = R->n_sim;
-  for (uint32_t k = *s + 1; k < n_sim; k++) {
-    *s = k;
-    const uint32_t sl = R->sim_l[k], sr = R->sim_r[k];
-    const float thr = R->thr[k];
-    const StrMeta* am = P.L.str_meta + (size_t)sl * P.L.n_rows + lrow;
-    const StrMeta* bm = P.R.str_meta + (size_t)sr * P.R.n_rows + rrow;
-    const uint4 al = am->loc, bl = bm->loc;
-    const uint32_t la = al.y, lb = bl.y;
-    const uint8_t* a = P.L.arena + 16ull * al.x;
-    const uint8_t* b = P.R.arena + 16ull * bl.x;
-    if (!has_table(P, la)) {  // the reference's own loops
-      if (la && lb) ops->ops += jw_eval_ops(min(la, lb), max(la, lb));
-      if (!sim_pass_slow(a, la, b, lb, thr, P.ctr)) return 0;
-      continue;
+  while (*live) {
+    const Member* M = R->mem + *mi;
+    const uint32_t n_rest = M->n_rest;
+    uint32_t k = *s;
+    for (; k < n_rest; k++) {
+      const uint32_t sl = M->rest_l[k], sr = M->rest_r[k];
+      const float thr = M->rest_thr[k];
+      const StrMeta* am = P.L.str_meta + (size_t)sl * P.L.n_rows + lrow;
+      const StrMeta* bm = P.R.str_meta + (size_t)sr * P.R.n_rows + rrow;
+      const uint4 al = am->loc, bl = bm->loc;
+      const uint32_t la = al.y, lb = bl.y;
+      const uint8_t* a = P.L.arena + 16ull * al.x;
+      const uint8_t* b = P.R.arena + 16ull * bl.x;
+      if (!has_table(P, la)) {  // the reference's own loops
+        if (la && lb) ops->ops += jw_eval_ops(min(la, lb), max(la, lb));
+        if (!sim_pass_slow(a, la, b, lb, thr, P.ctr)) break;
+        continue;
+      }
+      if (lb == 0) {
+        if (!jw_exact(0, la, 0, 0, thr, &P.ctr->ambiguous)) break;
+        continue;
+      }
+      const uint32_t ls = min(la, lb), ll = max(la, lb);
+      ops->ops += jw_eval_ops(ls, ll);
+      const uint4 bh = bm->head;
+      const uint32_t p16 = prefix16(am->head, bh);
+      uint32_t p = kPrefixUnknown;
+      int need = 0;
+      if (!(p16 == 16u && ls > 16u)) {
+        p = min(p16, ls);
+        need = m_need_lo(ls, ll, p, thr);
+        const uint32_t n_iter = min(lb, la + ((ls + 1u) >> 1));
+        if (need > (int)min(n_iter, ls)) break;
+        if (need > 0 && (int)sig_bound(am->sig[0], am->sig[1], bm->sig[0], bm->sig[1]) < need)
+          break;
+      }
+      if (scan_begin<W>(z, peq_table(P, sl, lrow), a, b, bh, la, lb, p, need, thr, ops)) {
+        *s = k;
+        return 2;
+      }
+      break;
     }
-    if (lb == 0) {
-      if (!jw_exact(0, la, 0, 0, thr, &P.ctr->ambiguous)) return 0;
-      continue;
-    }
-    const uint32_t ls = min(la, lb), ll = max(la, lb);
-    ops->ops += jw_eval_ops(ls, ll);
-    const uint4 bh = bm->head;
-    const uint32_t p16 = prefix16(am->head, bh);
-    uint32_t p = kPrefixUnknown;
-    int need = 0;
-    if (!(p16 == 16u && ls > 16u)) {
-      p = min(p16, ls);
-      need = m_need_lo(ls, ll, p, thr);
-      const uint32_t n_iter = min(lb, la + ((ls + 1u) >> 1));
-      if (need > (int)min(n_iter, ls)) return 0;
-      if (need > 0 &&
-          (int)sig_bound(am->sig[0], am->sig[1], bm->sig[0], bm->sig[1]) < need)
-        return 0;
-    }
-    return scan_begin<W>(z, peq_table(P, sl, lrow), a, b, bh, la, lb, p, need, thr, ops) ? 2 : 0;
+    if (k >= n_rest) return 1;
+    *live &= ~(1u << *mi);  // member *mi failed predicate k
+    if (!*live) return 0;
+    *mi = (uint32_t)__ffs(*live) - 1u;
+    *s = 0;
   }
-  return 1;
+  return 0;
 }
 
 // Warp-uniform state of the evaluation loop kept in shared memory (every
@@ -850,37 +925,47 @@ __device__ __forceinline__ int advance(const EvalParams& P, uint32_t rule, uint3
 // the values were read in the same step): the work items the warp has
 // claimed, the claim in each staging buffer, and the item being filtered.
 constexpr uint32_t kMaxClaimChunk = 16;
+// Kind of a claimed item: its rule has similarity predicates, and some
+// member of its group has extra equality slots; bits 8-11 hold the group's
+// member count.
+constexpr uint32_t kItemSim = 1u, kItemExtras = 2u;
+__device__ __forceinline__ uint32_t item_members(uint32_t kind) { return (kind >> 8) & 15u; }
 // A claimed work item: the sources of its bulk copies (right-row metadata
 // from the block's first row, right rows from the 16-byte boundary at or
 // before it, the left string's metadata), left row, rule, rows, the shift of
-// the first row past the boundary, the rule's predicate count and first
-// threshold.
+// the first row past the boundary, its kind and the group's smallest
+// first-column threshold.
 struct ItemDesc {
   const StrMeta* meta_src;
   const uint32_t* rows_src;
   const StrMeta* lm_src;
-  uint32_t lrow, rule, n, shift, n_sim;
+  uint32_t lrow, rule, n, shift, kind;
   float thr0;
 };
 struct WarpCtl {
   ItemDesc desc[kMaxClaimChunk];  // claimed items not yet staged
   uint32_t c_rule[kMaxStageBufs], c_lrow[kMaxStageBufs];  // claim per staging buffer
   uint32_t c_n[kMaxStageBufs], c_shift[kMaxStageBufs];    // (n = 0: none)
-  uint32_t c_more[kMaxStageBufs];
+  uint32_t c_kind[kMaxStageBufs];
   float c_thr[kMaxStageBufs];
-  uint32_t i_rule, i_lrow, i_more, i_fast;  // the item being filtered
+  // the item being filtered; i_lcode: its left row's codes of the group's
+  // extra equality slots
+  uint32_t i_rule, i_lrow, i_kind, i_fast, i_all;
   float i_thr;
+  int32_t i_lcode[kMaxEq];
 };
 static_assert(sizeof(WarpCtl) <= kWarpCtlWords * 4, "warp control block outgrows its words");
 
-// Filter one batch of 32 right rows of the item against its first
-// similarity predicate: one staged metadata record per right row gives its
+// Filter one batch of 32 right rows of the item against its group's first
+// similarity column: first the members whose extra equalities hold for the
+// pair (live), then one staged metadata record per right row gives its
 // length and first 16 symbols, hence the common prefix p (when below 16) and
-// the match count the threshold needs, and its count signature, an upper
-// bound on the matches; pairs that cannot reach the threshold are decided
-// here, the rest go to the ring with their first 16 symbols.  Empty right
-// strings are decided here too.  lm: the item's left string metadata.
-// Returns the entries appended.
+// the match count the smallest live threshold needs, and its count
+// signature, an upper bound on the matches; pairs that cannot reach it are
+// decided here, the rest go to the ring with their first 16 symbols.  Pairs
+// decided without a scan that pass go to the ring for their members' further
+// predicates, or match at once when a passing member has none.  lm: the
+// item's left string metadata.  Returns the entries appended.
 __device__ __forceinline__ uint32_t filter_batch(const EvalParams& P, const WarpCtl* C,
                                                  const StrMeta* lm, const uint32_t* rows,
                                                  const StrMeta* meta, uint32_t n, uint32_t e0,
@@ -891,24 +976,39 @@ __device__ __forceinline__ uint32_t filter_batch(const EvalParams& P, const Warp
   const bool act = e < n;
   const uint32_t rrow = act ? rows[e] : 0u;
   const uint32_t la = lm->loc.y, a_off = lm->loc.x;
-  const bool more = C->i_more != 0;
-  const float thr = C->i_thr;
+  const Rule* R = P.rules + C->i_rule;
+  const uint32_t all = C->i_all;
+  uint32_t live = act ? all : 0u;
+  float thr = C->i_thr;
+  if (act && (C->i_kind & kItemExtras)) {
+    uint32_t eqm = 0;
+    const uint32_t nx = R->n_xslots;
+    for (uint32_t j = 0; j < nx; j++)
+      if (P.R.eq_codes[(size_t)R->xslot[j] * P.R.n_rows + rrow] == C->i_lcode[j]) eqm |= 1u << j;
+    for (uint32_t x = all; x; x &= x - 1) {
+      const uint32_t k = (uint32_t)__ffs(x) - 1u;
+      if (R->mem[k].xmask & ~eqm) live &= ~(1u << k);
+    }
+    if (live != all) thr = live_thr(R, live);
+  }
   uint4 loc = make_uint4(0, 0, 0, 0), head = make_uint4(0, 0, 0, 0);
-  if (act) {
+  if (live) {
     loc = meta[e].loc;
     head = meta[e].head;
   }
-  bool pass = false, scan = false;
+  uint32_t pass1 = 0;  // members that passed the first column without a scan
+  bool scan = false;
   uint32_t p = 0;
   int need = 0;
-  if (act) {
+  if (live) {
     const uint32_t lb = loc.y;
     if (!C->i_fast) {  // the reference's own loops
       if (la && lb) ops->ops += jw_eval_ops(min(la, lb), max(la, lb));
-      pass = sim_pass_slow(P.L.arena + 16ull * a_off, la, P.R.arena + 16ull * loc.x, lb, thr,
-                           P.ctr);
+      uint32_t m = 0, pp = 0;
+      sim_m_slow(P.L.arena + 16ull * a_off, la, P.R.arena + 16ull * loc.x, lb, P.ctr, &m, &pp);
+      pass1 = first_pass(R, live, m, la, lb, pp, &P.ctr->ambiguous);
     } else if (lb == 0) {
-      pass = jw_exact(0, la, 0, 0, thr, &P.ctr->ambiguous);
+      pass1 = first_pass(R, live, 0, la, 0, 0, &P.ctr->ambiguous);
     } else {
       const uint32_t ls = min(la, lb), ll = max(la, lb);
       ops->ops += jw_eval_ops(ls, ll);
@@ -929,17 +1029,20 @@ __device__ __forceinline__ uint32_t filter_batch(const EvalParams& P, const Warp
       }
     }
   }
-  const bool push = scan || (pass && more);
+  const bool done = pass1 && member_done(R, pass1);
+  const bool push = scan || (pass1 && !done);
   const unsigned qm = __ballot_sync(kFull, push);
   const uint32_t lrow = C->i_lrow;
   if (push) {
     const uint32_t slot = (tail + __popc(qm & lt)) & (kRing - 1);
     uint4* en = q + kRingWords / 4 * slot;
-    en[0] = make_uint4(rrow, loc.x, loc.y, scan ? ring_tag((uint32_t)need, p, 0) : kAdvance);
+    const uint32_t tag = scan ? ring_tag((uint32_t)need, p, 0, live, 0)
+                              : (ring_tag(0, 0, 0, pass1, (uint32_t)__ffs(pass1) - 1u) | kAdvance);
+    en[0] = make_uint4(rrow, loc.x, loc.y, tag);
     en[1] = head;
     en[2] = make_uint4(lrow, la, a_off, C->i_rule);
   }
-  emit(P, pass && !more, lrow, rrow, lane);
+  emit(P, done, lrow, rrow, lane);
   return __popc(qm);
 }
 
@@ -1058,15 +1161,16 @@ __device__ __forceinline__ uint32_t claim_chunk(const EvalParams& P, WarpCtl* C,
   const uint32_t rb1 = min(rb0 + P.tile_right, offr + R.cnt_r[key]);
   const uint32_t a0 = rb0 & ~3u;
   ItemDesc d;
-  d.n_sim = R.n_sim;
-  d.meta_src = d.n_sim ? R.sorted_meta_r + rb0 : nullptr;
+  const bool sim = R.n_sim != 0;
+  d.kind = (sim ? kItemSim : 0u) | (R.n_xslots ? kItemExtras : 0u) | (R.n_members << 8);
+  d.meta_src = sim ? R.sorted_meta_r + rb0 : nullptr;
   d.rows_src = R.sorted_r + a0;
-  d.lm_src = d.n_sim ? P.L.str_meta + (size_t)R.sim_l[0] * P.L.n_rows + lrow : nullptr;
+  d.lm_src = sim ? P.L.str_meta + (size_t)R.sim_l[0] * P.L.n_rows + lrow : nullptr;
   d.lrow = lrow;
   d.rule = r;
   d.n = rb1 - rb0;
   d.shift = rb0 - a0;
-  d.thr0 = d.n_sim ? R.thr[0] : 0.0f;
+  d.thr0 = sim ? R.thr_min : 0.0f;
   __syncwarp();  // earlier reads of the descriptors are done
   if ((uint32_t)lane < n) C->desc[lane] = d;
   __syncwarp();
@@ -1101,7 +1205,7 @@ __device__ __forceinline__ void claim_item(const EvalParams& P, WarpCtl* C, uint
       break;
     }
     const ItemDesc d = C->desc[(*d_pos)++];
-    if (d.n_sim == 0) {  // equalities only: every candidate matches
+    if (!(d.kind & kItemSim)) {  // equalities only: every candidate matches
       for (uint32_t e = 0; e < d.n; e += 32) {
         const uint32_t k = e + (uint32_t)lane;
         const uint32_t rrow = k < d.n ? d.rows_src[d.shift + k] : 0u;
@@ -1125,7 +1229,7 @@ __device__ __forceinline__ void claim_item(const EvalParams& P, WarpCtl* C, uint
     C->c_lrow[b] = d.lrow;
     C->c_n[b] = d.n;
     C->c_shift[b] = d.shift;
-    C->c_more[b] = d.n_sim > 1 ? 1u : 0u;
+    C->c_kind[b] = d.kind;
     C->c_thr[b] = d.thr0;
     return;
   }
@@ -1139,8 +1243,9 @@ __device__ __forceinline__ void claim_item(const EvalParams& P, WarpCtl* C, uint
 // take the next queued pair as soon as theirs is decided, whichever item it
 // came from, since every pair reads its left string's Peq table from device
 // memory; the ring is refilled from the current item, then the next ones, as
-// it drains.  A pair that passes a predicate goes on with the rule's next
-// one in the same lane; matches leave by warp-aggregated atomics.
+// it drains.  A pair that passes its group's first column goes on with the
+// further predicates of the members that passed, member by member, in the
+// same lane; matches leave by warp-aggregated atomics.
 template <int W>
 __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
                                           unsigned long long n_work, WorkTally* ops,
@@ -1166,9 +1271,10 @@ __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
   bool active = false;  // current item waited for and being filtered
   uint32_t in_pos = 0, cur_n = C->c_n[0];
   uint32_t head = 0, tail = 0;
-  // lane state
-  bool busy = false;
-  uint32_t rrow = 0, lrow = 0, rule = 0, s = 0;
+  // lane state: the pair, its group's live members, the member and predicate
+  // in hand (first = the group's first column)
+  bool busy = false, first = false;
+  uint32_t rrow = 0, lrow = 0, rule = 0, s = 0, live = 0, mi = 0;
   Scan<W> z;
   z.tab = nullptr;
   z.b = nullptr;
@@ -1217,14 +1323,22 @@ __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
       in_pos = 0;
       (*done)++;
       const StrMeta* lm = reinterpret_cast<const StrMeta*>(buf + P.buf_lmeta_off);
-      const uint32_t ir = C->c_rule[cb], il = C->c_lrow[cb], more = C->c_more[cb];
+      const uint32_t ir = C->c_rule[cb], il = C->c_lrow[cb], kind = C->c_kind[cb];
       const float thr = C->c_thr[cb];
       const uint32_t la = lm->loc.y;
+      __syncwarp();  // the previous item's fields are read
       C->i_rule = ir;
       C->i_lrow = il;
       C->i_thr = thr;
-      C->i_more = more;
+      C->i_kind = kind;
+      C->i_all = (1u << item_members(kind)) - 1u;
       C->i_fast = has_table(P, la) ? 1u : 0u;
+      if (kind & kItemExtras) {  // the left row's codes of the extra equality slots
+        const Rule* R = P.rules + ir;
+        if ((uint32_t)lane < R->n_xslots)
+          C->i_lcode[lane] = P.L.eq_codes[(size_t)R->xslot[lane] * P.L.n_rows + il];
+      }
+      __syncwarp();
     }
     // idle lanes take the next queued pairs
     bool fin = false, pass = false;
@@ -1236,17 +1350,21 @@ __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
       rrow = e0.x;
       lrow = e2.x;
       rule = e2.w;
-      s = (e0.w >> 15) & 7u;
+      live = tag_live(e0.w);
       int st = 0;
       if (e0.w & kAdvance) {
-        st = advance<W>(P, rule, &s, lrow, rrow, z, ops);
+        first = false;
+        mi = tag_member(e0.w);
+        s = tag_s(e0.w);
+        st = advance_group<W>(P, rule, &live, &mi, &s, lrow, rrow, z, ops);
       } else {
+        // the group's first column at the smallest live threshold
+        first = true;
         const Rule* R = P.rules + rule;
-        const uint32_t sl = R->sim_l[s];
         const uint32_t p = (e0.w >> 10) & 31u;
-        st = scan_begin<W>(z, peq_table(P, sl, lrow), P.L.arena + 16ull * e2.z,
+        st = scan_begin<W>(z, peq_table(P, R->sim_l[0], lrow), P.L.arena + 16ull * e2.z,
                            P.R.arena + 16ull * e0.y, en[1], e2.y, e0.z, p, (int)(e0.w & 1023u),
-                           R->thr[s], ops)
+                           live_thr(R, live), ops)
                  ? 2
                  : 0;
       }
@@ -1259,11 +1377,36 @@ __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
     }
     head += min(n_idle, avail);
     if (busy) {
-      bool ok = false;
-      if (scan_step<W>(z, &ok, P.ctr, ops)) {
+      uint32_t m = 0;
+      const int sc = scan_step<W>(z, &m, ops);
+      if (sc) {
         busy = false;
-        int st = ok ? 1 : 0;
-        if (ok) st = advance<W>(P, rule, &s, lrow, rrow, z, ops);
+        int st = 0;
+        if (first) {
+          // decided per live member; the scan stopped early only when even
+          // the smallest threshold is out of reach
+          const Rule* R = P.rules + rule;
+          const uint32_t pass1 =
+              sc == 1 ? first_pass(R, live, m, z.ls, z.ll, z.p, &P.ctr->ambiguous) : 0u;
+          if (pass1 && member_done(R, pass1)) {
+            st = 1;
+          } else if (pass1) {
+            first = false;
+            live = pass1;
+            mi = (uint32_t)__ffs(pass1) - 1u;
+            s = 0;
+            st = advance_group<W>(P, rule, &live, &mi, &s, lrow, rrow, z, ops);
+          }
+        } else {
+          if (sc == 1 && jw_decide(m, z.ls, z.ll, z.p, z.thr, &P.ctr->ambiguous)) {
+            s++;  // member mi passed predicate s
+          } else {
+            live &= ~(1u << mi);
+            mi = live ? (uint32_t)__ffs(live) - 1u : 0u;
+            s = 0;
+          }
+          if (live) st = advance_group<W>(P, rule, &live, &mi, &s, lrow, rrow, z, ops);
+        }
         if (st == 2) {
           busy = true;
         } else {

@@ -98,6 +98,19 @@ struct Side {
   uint32_t n_rows;
 };
 
+// A rule evaluated as a member of a group (see Rule): its threshold on the
+// group's first similarity column, the extra equality slots it needs beyond
+// the group root's (bits of Rule::xslot), and its other similarity
+// predicates in evaluation order.
+constexpr uint32_t kMaxMembers = 8;
+struct Member {
+  float thr_first;
+  uint32_t xmask;
+  uint32_t n_rest;
+  uint32_t rest_l[kMaxSim], rest_r[kMaxSim];
+  float rest_thr[kMaxSim];
+};
+
 struct Rule {
   uint32_t n_eq, n_sim, composite, comp_index;
   uint32_t eq_slot[kMaxEq];
@@ -127,7 +140,41 @@ struct Rule {
   // order, so that a work item's metadata is one contiguous, 16-byte-aligned
   // block for a bulk copy into shared memory (null without similarities)
   StrMeta* sorted_meta_r;
+  // Group evaluation.  The work items of this rule's join are evaluated for
+  // n_members rules at once: member 0 is this rule, the others are rules whose
+  // equality slots contain this rule's (their candidates are this join's
+  // candidates whose extra slots xslot[] also hold) and whose similarity
+  // predicates include this rule's first column (sim_l[0], sim_r[0]).  The
+  // first column is filtered and scanned once per pair, at the smallest
+  // threshold of the members still live, and decided per member from the
+  // match count; members that pass go on with their other predicates, and
+  // the pair matches when one member passes them all (OR across rules).
+  // n_members == 0: the rule is a member of another rule's group and has no
+  // work items of its own (its join still counts its pair-comparisons).
+  uint32_t n_members;
+  uint32_t n_xslots;
+  uint32_t xslot[kMaxEq];
+  float thr_min;  // smallest member threshold on the first column
+  Member mem[kMaxMembers];
 };
+
+// Host: a rule as the only member of its own group (the plain form, serving,
+// and any rule no group takes in).
+inline void make_singleton(Rule* d) {
+  d->n_members = 1;
+  d->n_xslots = 0;
+  Member& m = d->mem[0];
+  m = Member{};
+  m.thr_first = d->n_sim ? d->thr[0] : 0.0f;
+  m.xmask = 0;
+  m.n_rest = d->n_sim > 1 ? d->n_sim - 1 : 0;
+  for (uint32_t k = 1; k < d->n_sim; k++) {
+    m.rest_l[k - 1] = d->sim_l[k];
+    m.rest_r[k - 1] = d->sim_r[k];
+    m.rest_thr[k - 1] = d->thr[k];
+  }
+  d->thr_min = m.thr_first;
+}
 
 constexpr uint32_t kWordClasses = 5;
 constexpr uint32_t kMaxSegments = 8;
@@ -171,7 +218,7 @@ constexpr uint32_t kMaxStageBufs = 4;
 struct WarpLayout {
   uint32_t n_bufs, buf_off, buf_words, buf_rows_off, buf_lmeta_off, mbar_off, ctl_off, warp_words;
 };
-constexpr uint32_t kWarpCtlWords = 224;  // the warp's control block (kernels.cu: WarpCtl)
+constexpr uint32_t kWarpCtlWords = 236;  // the warp's control block (kernels.cu: WarpCtl)
 
 inline WarpLayout warp_layout(uint32_t tile_right, uint32_t n_bufs) {
   WarpLayout w;

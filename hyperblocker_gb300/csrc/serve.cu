@@ -556,6 +556,7 @@ void open_server(hbx_server* S, const hbx_plan* const* plans, int32_t n_plans, c
       d.n_wclass = (d.n_sim && D * dev::kWordClasses <= (1ull << 22)) ? dev::kWordClasses : 1u;
       d.wclass_slot = d.n_sim ? d.sim_l[0] : 0u;
       d.domain_l = d.n_wclass * d.domain;
+      dev::make_singleton(&d);
       // right half of the join: rows grouped by key, metadata in that order
       T->key_r.alloc(std::max<uint32_t>(nR, 1));
       T->cnt_r.alloc(D);

@@ -213,6 +213,7 @@ void place(Carve& c, const hbx::Encoded& E, size_t smem_cap, Layout* Y,
     d.n_wclass = split ? dev::kWordClasses : 1u;
     d.wclass_slot = split ? (uint32_t)re.sim_slot_l[0] : 0u;
     d.domain_l = d.n_wclass * d.domain;
+    dev::make_singleton(&d);
     d.key_l = c.take<uint32_t>(nL);
     d.key_r = c.take<uint32_t>(nR);
     d.cnt_l = c.take<uint32_t>(d.domain_l);

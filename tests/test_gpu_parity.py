@@ -108,6 +108,44 @@ def test_random_tables_against_oracle(ctx, seed):
         assert st.pairs_covered == want.pairs_covered
 
 
+RULE_GROUP_SETS = [
+    # one group over k1 (title first): the root, a member with the same
+    # equalities (title and authors), two members with the extra equality k2,
+    # each at its own title threshold; k2 alone roots a second group
+    [synth.rule_yaml([3], [(1, 0.70)]), synth.rule_yaml([3, 4], [(1, 0.62), (2, 0.5)]),
+     synth.rule_yaml([4, 3], [(2, 0.55), (1, 0.66)]), synth.rule_yaml([3], [(2, 0.7), (1, 0.8)]),
+     synth.rule_yaml([4], [(1, 0.75)])],
+    # the root tests authors before title; title is what its members share,
+    # so it moves to the front of the group
+    [synth.rule_yaml([3], [(2, 0.6), (1, 0.7)]), synth.rule_yaml([3, 4], [(1, 0.65)]),
+     synth.rule_yaml([4, 3], [(1, 0.72), (2, 0.58)])],
+    # no equalities at the root: every pair of a partition is a candidate
+    [synth.rule_yaml([], [(1, 0.8)]), synth.rule_yaml([3], [(1, 0.7), (2, 0.6)]),
+     synth.rule_yaml([4], [(1, 0.68)]), synth.rule_yaml([3, 4], [(2, 0.5), (1, 0.6)])],
+]
+
+
+@pytest.mark.parametrize("seed", range(4))
+@pytest.mark.parametrize("rule_set", range(len(RULE_GROUP_SETS)))
+def test_rule_groups_against_oracle(ctx, rule_set, seed):
+    """The batched form evaluates rules whose equalities contain another
+    rule's, and that test its first similarity column, inside that rule's
+    join (one first-column scan per pair, decided per member); the plain form
+    evaluates every rule on its own.  Both must give the oracle's set and
+    pair-comparison count (every rule's candidates are still counted)."""
+    alpha = [b"abc", b"abcdefgh ", b"xyz, ", b"abcdefghijklmnopqrstuvwxyz"][seed]
+    cl, cr = _util.random_tables(500 + 10 * rule_set + seed, 70, 160, alpha, [30, 90, 140, 70][seed])
+    docs = RULE_GROUP_SETS[rule_set]
+    n_part = 1 + seed % 3
+    want = api.run_block(api.CTable(cl), api.CTable(cr), _oracle_plan(docs), n_part)
+    assert len(want.pairs) > 0
+    for mode in MODES:
+        got, st = _engine_pairs(ctx, docs, cl, cr, n_part, _util.INT_MAX, mode)
+        assert np.array_equal(got, want.pairs), mode
+        assert st.pair_comparisons == want.pair_comparisons, mode
+        assert st.fma_ambiguous == 0
+
+
 @pytest.mark.parametrize("n_values", [500, 1500, 3000, 40000])
 def test_key_domains_across_scan_chunks(ctx, n_values):
     """Left key domains (2 partitions x codes x 5 length classes) of 3, 8
