@@ -254,8 +254,11 @@ class C3:
                                     self.stream.cuda_stream)
 
     def timed(self, mode, k, warm):
+        """warm untimed steps, then k timed ones, inside an NVTX range named
+        c3_<mode> (an ncu capture can pick the form's launches by it)."""
         import torch
 
+        torch.cuda.nvtx.range_push(f"c3_{mode}")
         for _ in range(warm):
             self.step(mode)
         rec = {"ms": [], "ms_eval": [], "ops": [], "scan_ops": [], "cmp": [], "launches": 0,
@@ -277,6 +280,7 @@ class C3:
                 rec["cmp"].append(st.pair_comparisons)
                 rec["launches"] += st.n_launches
                 rec["matches"] = n
+        torch.cuda.nvtx.range_pop()
         return rec
 
     def parity(self, args, n_matches):
@@ -878,7 +882,7 @@ def main():
     ap.add_argument("--ref-per-part", type=int, default=16)
     ap.add_argument("--c2-steps", type=int, default=20)
     ap.add_argument("--c5-rows", type=int, default=500_000)
-    ap.add_argument("--c5-window-mb", type=int, default=512)
+    ap.add_argument("--c5-window-mb", type=int, default=128)
     ap.add_argument("--c5-sample-per-part", type=int, default=16)
     ap.add_argument("--serve-rows", type=int, default=10_000_000)
     ap.add_argument("--serve-requests", type=int, default=800)

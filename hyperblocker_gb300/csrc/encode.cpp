@@ -237,26 +237,31 @@ void encode_rows(const Table& left, const Table& right, Encoded* Ep) {
   pack_side(right, E.R);
 }
 
+bool rule_mixed_domain(const Encoded& E, RuleEnc* rp) {
+  RuleEnc& re = *rp;
+  const uint64_t n_partitions = E.n_partitions;
+  re.radix.clear();
+  re.part_key_begin.clear();
+  re.composite = false;
+  re.comp_index = -1;
+  unsigned __int128 M = 1;
+  for (int s : re.eq_slot) {
+    re.radix.push_back(E.eq_card[(size_t)s]);
+    M *= E.eq_card[(size_t)s];
+  }
+  const unsigned __int128 D = M * n_partitions;
+  if (D > kMaxKeyDomain) return false;
+  re.domain = (uint64_t)D;
+  for (uint64_t p = 0; p <= n_partitions; p++) re.part_key_begin.push_back(p * (uint64_t)M);
+  return true;
+}
+
 bool finish_rules(Encoded* Ep, bool allow_composite) {
   Encoded& E = *Ep;
   const uint64_t n_partitions = E.n_partitions;
   for (RuleEnc& re : E.rules) {
-    re.radix.clear();
-    re.part_key_begin.clear();
-    re.composite = false;
-    re.comp_index = -1;
     // mixed-radix domain
-    unsigned __int128 M = 1;
-    for (int s : re.eq_slot) {
-      re.radix.push_back(E.eq_card[(size_t)s]);
-      M *= E.eq_card[(size_t)s];
-    }
-    unsigned __int128 D = M * n_partitions;
-    if (D <= kMaxKeyDomain) {
-      re.domain = (uint64_t)D;
-      for (uint64_t p = 0; p <= n_partitions; p++) re.part_key_begin.push_back(p * (uint64_t)M);
-      continue;
-    }
+    if (rule_mixed_domain(E, &re)) continue;
     if (!allow_composite) return false;
     // dense ids of the (bucket, codes...) tuples that occur, grouped by bucket
     re.composite = true;

@@ -64,6 +64,10 @@ void encode_rows(const Table& left, const Table& right, Encoded* E);
 // the host codes of encode_rows; with allow_composite false such a rule makes
 // this return false instead.
 bool finish_rules(Encoded* E, bool allow_composite);
+// One rule's mixed-radix join-key domain (bucket x eq codes) from the
+// dictionary sizes, when it is at most kMaxKeyDomain: sets radix, domain and
+// part_key_begin and returns true; else returns false (composite ids needed).
+bool rule_mixed_domain(const Encoded& E, RuleEnc* re);
 // The whole host encoding (schema, rows, domains).
 Encoded encode(const Plan& plan, const Table& left, const Table& right, uint64_t n_partitions,
                int64_t prefix_idx);

@@ -91,6 +91,7 @@ struct hbx_session {
   // caller's buffer, 0 = none) returns its count without growing and rerunning
   uint64_t out_hint = 1 << 16, cap_limit = 0;
   int blocks_per_sm = 1;
+  int max_eval_ctas = 0;  // cap on the evaluation grid (set_eval_ctas), 0 = none
   size_t smem_bytes = 0;
   cudaGraphExec_t graph = nullptr;
   // the caller's device output (hbx_session_run), written by the kernels
@@ -613,7 +614,8 @@ uint32_t enqueue_batched(hbx_session* S, cudaStream_t st) {
   uint32_t launches = enqueue_join(S, st, S->d_groups.p);
   dev::EvalParams P = eval_params(S, S->d_groups.p);
   P.n_seg = 0;  // every work item of every group
-  const int grid = S->ctx->n_sm * S->blocks_per_sm;
+  int grid = S->ctx->n_sm * S->blocks_per_sm;
+  if (S->max_eval_ctas > 0) grid = std::min(grid, S->max_eval_ctas);
   HBX_CUDA(cudaEventRecordWithFlags(S->ev_eval0, st, rec_flags));
   dev::eval_kernel(S->variant)<<<grid, kThreads, S->smem_bytes, st>>>(P);
   launch_check("k_eval");
@@ -714,7 +716,8 @@ dev::Counters run_once(hbx_session* S, hbx_mode mode, cudaStream_t st, uint32_t*
                            cudaMemcpyDeviceToHost, st));
   HBX_CUDA(cudaStreamSynchronize(st));
   dev::EvalParams P = eval_params(S, S->d_rules.p);
-  const int max_grid = S->ctx->n_sm * S->blocks_per_sm;
+  int max_grid = S->ctx->n_sm * S->blocks_per_sm;
+  if (S->max_eval_ctas > 0) max_grid = std::min(max_grid, S->max_eval_ctas);
   HBX_CUDA(cudaEventRecord(S->ev_eval0, st));
   for (uint64_t p = 0; p < S->E.n_partitions; p++) {
     for (uint32_t r = 0; r < n_rules; r++) {
@@ -1030,6 +1033,11 @@ void session_run(hbx_session* S, hbx_mode mode, cudaStream_t st) {
     grow_output(S, need);
   }
   fail(HBX_ERR_CAPACITY, "output kept growing");
+}
+
+void set_eval_ctas(hbx_session* S, int ctas) {
+  S->max_eval_ctas = std::max(0, ctas);
+  drop_graph(S);
 }
 
 void reserve_output(hbx_session* S, uint64_t pairs) {

@@ -24,6 +24,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <string>
@@ -93,11 +94,14 @@ __global__ void k_pairs_covered(const unsigned long long* hl, const unsigned lon
 
 __global__ void k_dict_insert(ColDev c, uint32_t n, uint32_t gid_base, unsigned long long* keys,
                               uint32_t* rep, uint32_t mask, uint32_t* row_slot,
-                              unsigned long long* sum) {
+                              unsigned long long* sum, unsigned long long seed) {
+  // seed bit 63 set: the test build of kDictSeed that keeps 3 bits of the hash
+  const unsigned long long hmask = (seed >> 63) ? 7ull : ~0ull;
+  seed &= ~(1ull << 63);
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     int64_t a;
     const uint32_t len = cell_len(c, i, &a);
-    unsigned long long h = std_hash_bytes(c.bytes + a, len);
+    unsigned long long h = hash_bytes_seeded(c.bytes + a, len, seed) & hmask;
     if (h == kEmpty) h = kEmpty - 1;  // the empty marker; verification keeps this exact
     uint32_t slot = (uint32_t)(h ^ (h >> 32)) & mask;
     bool placed = false;
@@ -141,6 +145,53 @@ __global__ void k_dict_assign(ColDev c, uint32_t n, uint32_t gid_base, const uin
     for (uint32_t k = 0; same && k < la; k++) same = c.bytes[a + k] == pb[b + k];
     if (!same) atomicOr(&sum[kSumFlags], (unsigned long long)kFlagCollision);
   }
+}
+
+// Composite join keys.  Row i's tuple: its bucket, then its dictionary code
+// of each of the rule's equality slots, as 4-byte little-endian words (a
+// fixed-width cell for the dictionary kernels).
+struct TupleSlots {
+  uint32_t k;
+  uint32_t slot[dev::kMaxEq];
+};
+__global__ void k_tuples(const uint32_t* bucket, const int32_t* eq, uint32_t n, TupleSlots ts,
+                         uint32_t* out) {
+  const uint32_t w = ts.k + 1;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    uint32_t* o = out + (size_t)i * w;
+    o[0] = bucket[i];
+    for (uint32_t j = 0; j < ts.k; j++) o[1 + j] = (uint32_t)eq[(size_t)ts.slot[j] * n + i];
+  }
+}
+
+// The bucket of every tuple code (the bucket of its slot's representative
+// row), and the tuples per bucket.
+__global__ void k_code_bucket(const unsigned long long* keys, const uint32_t* code,
+                              const uint32_t* rep, uint32_t cap, const uint32_t* bucket_l,
+                              const uint32_t* bucket_r, uint32_t n_left, uint32_t* code_bucket,
+                              uint32_t* per_bucket) {
+  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < cap; s += gridDim.x * blockDim.x) {
+    if (keys[s] == kEmpty) continue;
+    const uint32_t r = rep[s];
+    const uint32_t b = r < n_left ? bucket_l[r] : bucket_r[r - n_left];
+    code_bucket[code[s]] = b;
+    atomicAdd(per_bucket + b, 1u);
+  }
+}
+
+// Dense ids grouped by bucket: code c gets start[bucket] + its rank there
+// (ranks in any order; only equality and the grouping matter).
+__global__ void k_code_remap(const uint32_t* code_bucket, uint32_t n_codes, const uint32_t* start,
+                             uint32_t* cursor, uint32_t* remap) {
+  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < n_codes; c += gridDim.x * blockDim.x) {
+    const uint32_t b = code_bucket[c];
+    remap[c] = start[b] + atomicAdd(cursor + b, 1u);
+  }
+}
+
+__global__ void k_apply_remap(const int32_t* codes, uint32_t n, const uint32_t* remap, int32_t* out) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    out[i] = (int32_t)remap[(uint32_t)codes[i]];
 }
 
 // dst = scan[n - 1] + in[n - 1] (+ extra): the total of an exclusive scan
@@ -457,45 +508,58 @@ bool device_encode(const hbx_table* left, const hbx_table* right, Encoded* Ep, S
                                                                    sum.p);
   check_launch("ingest buckets");
 
-  // ---- joint dictionaries
+  // ---- joint dictionaries (rebuilt with a fresh seed after a collision,
+  // below)
   LB->eq.alloc(std::max<size_t>(n_eq * nL, 1));
   RB->eq.alloc(std::max<size_t>(n_eq * nR, 1));
-  LB->comp.alloc(1);
-  RB->comp.alloc(1);
-  if (n_eq) {
-    uint32_t cap = 1024;
-    while (cap < 2ull * ((uint64_t)nL + nR)) cap <<= 1;
-    DBuf<unsigned long long> keys;
-    DBuf<uint32_t> rep, occ, code, slot_l, slot_r;
-    keys.alloc(cap);
-    rep.alloc(cap);
-    occ.alloc(cap);
-    code.alloc(cap);
-    slot_l.alloc(std::max<uint32_t>(nL, 1));
-    slot_r.alloc(std::max<uint32_t>(nR, 1));
-    for (size_t k = 0; k < n_eq; k++) {
-      const ing::ColDev cl = view(cols_l, E.eq_slots[k].first);
-      const ing::ColDev cr = view(cols_r, E.eq_slots[k].second);
-      HBX_CUDA(cudaMemsetAsync(keys.p, 0xff, (size_t)cap * sizeof(unsigned long long), st));
-      HBX_CUDA(cudaMemsetAsync(rep.p, 0xff, (size_t)cap * sizeof(uint32_t), st));
-      if (nL)
-        ing::k_dict_insert<<<grid_for(nL, n_sm), 256, 0, st>>>(cl, nL, 0, keys.p, rep.p, cap - 1,
-                                                               slot_l.p, sum.p);
-      if (nR)
-        ing::k_dict_insert<<<grid_for(nR, n_sm), 256, 0, st>>>(cr, nR, nL, keys.p, rep.p, cap - 1,
-                                                               slot_r.p, sum.p);
-      ing::k_occupied<<<grid_for(cap, n_sm), 256, 0, st>>>(keys.p, cap, occ.p);
-      scan_u32(occ.p, cap, code.p, st);
-      if (nL)
-        ing::k_dict_assign<<<grid_for(nL, n_sm), 256, 0, st>>>(
-            cl, nL, 0, slot_l.p, code.p, rep.p, cl, cr, nL, LB->eq.p + k * nL, sum.p);
-      if (nR)
-        ing::k_dict_assign<<<grid_for(nR, n_sm), 256, 0, st>>>(
-            cr, nR, nL, slot_r.p, code.p, rep.p, cl, cr, nL, RB->eq.p + k * nR, sum.p);
-      ing::k_scan_total<<<1, 32, 0, st>>>(code.p, occ.p, cap, 0, sum.p + i_card + k);
-      check_launch("ingest dictionary");
-    }
-  }
+  uint32_t cap = 1024;
+  while (cap < 2ull * ((uint64_t)nL + nR)) cap <<= 1;
+  DBuf<unsigned long long> keys;
+  DBuf<uint32_t> rep, occ, code, slot_l, slot_r;
+  keys.alloc(cap);
+  rep.alloc(cap);
+  occ.alloc(cap);
+  code.alloc(cap);
+  slot_l.alloc(std::max<uint32_t>(nL, 1));
+  slot_r.alloc(std::max<uint32_t>(nR, 1));
+  // One joint dictionary of columns cl (left) and cr (right): codes into
+  // out_l / out_r, the number of distinct cells into *card_sum.
+  auto dictionary = [&](const ing::ColDev& cl, const ing::ColDev& cr, int32_t* out_l,
+                        int32_t* out_r, unsigned long long* card_sum, unsigned long long seed) {
+    HBX_CUDA(cudaMemsetAsync(keys.p, 0xff, (size_t)cap * sizeof(unsigned long long), st));
+    HBX_CUDA(cudaMemsetAsync(rep.p, 0xff, (size_t)cap * sizeof(uint32_t), st));
+    if (nL)
+      ing::k_dict_insert<<<grid_for(nL, n_sm), 256, 0, st>>>(cl, nL, 0, keys.p, rep.p, cap - 1,
+                                                             slot_l.p, sum.p, seed);
+    if (nR)
+      ing::k_dict_insert<<<grid_for(nR, n_sm), 256, 0, st>>>(cr, nR, nL, keys.p, rep.p, cap - 1,
+                                                             slot_r.p, sum.p, seed);
+    ing::k_occupied<<<grid_for(cap, n_sm), 256, 0, st>>>(keys.p, cap, occ.p);
+    scan_u32(occ.p, cap, code.p, st);
+    if (nL)
+      ing::k_dict_assign<<<grid_for(nL, n_sm), 256, 0, st>>>(cl, nL, 0, slot_l.p, code.p, rep.p,
+                                                             cl, cr, nL, out_l, sum.p);
+    if (nR)
+      ing::k_dict_assign<<<grid_for(nR, n_sm), 256, 0, st>>>(cr, nR, nL, slot_r.p, code.p, rep.p,
+                                                             cl, cr, nL, out_r, sum.p);
+    ing::k_scan_total<<<1, 32, 0, st>>>(code.p, occ.p, cap, 0, card_sum);
+    check_launch("ingest dictionary");
+  };
+  const char* collide_env = std::getenv("HBX_TEST_DICT_COLLIDE");
+  const bool collide_test = collide_env && std::strcmp(collide_env, "1") == 0;
+  // attempt k hashes with seed kDictSeed + k; the test build of attempt 0
+  // keeps 3 bits of each hash (bit 63 of the seed word asks for that)
+  auto seed_of = [&](int attempt) {
+    unsigned long long sd = kDictSeed + (unsigned long long)attempt;
+    if (collide_test && attempt == 0) sd |= 1ull << 63;
+    return sd;
+  };
+  auto eq_dictionaries = [&](unsigned long long seed) {
+    for (size_t k = 0; k < n_eq; k++)
+      dictionary(view(cols_l, E.eq_slots[k].first), view(cols_r, E.eq_slots[k].second),
+                 LB->eq.p + k * nL, RB->eq.p + k * nR, sum.p + i_card + k, seed);
+  };
+  eq_dictionaries(seed_of(0));
 
   // ---- symbol alphabet
   DBuf<unsigned long long> bhist;
@@ -546,19 +610,31 @@ bool device_encode(const hbx_table* left, const hbx_table* right, Encoded* Ep, S
   arenas(cols_r, E.R.str_col, nR, TR, RB, i_mxr, i_units + 1);
 
   // ---- summary
+  constexpr int kMaxAttempts = 4;
   std::vector<unsigned long long> h(n_sum);
-  HBX_CUDA(cudaMemcpyAsync(h.data(), sum.p, n_sum * sizeof(unsigned long long),
-                           cudaMemcpyDeviceToHost, st));
+  auto read_summary = [&]() {
+    HBX_CUDA(cudaMemcpyAsync(h.data(), sum.p, n_sum * sizeof(unsigned long long),
+                             cudaMemcpyDeviceToHost, st));
+    HBX_CUDA(cudaStreamSynchronize(st));
+  };
   HBX_CUDA(cudaMemcpyAsync(E.sym_of_byte.data(), sym.p, 256, cudaMemcpyDeviceToHost, st));
-  HBX_CUDA(cudaStreamSynchronize(st));
+  read_summary();
   auto give_up = [&](const std::string& reason) {
     *why = reason;
     *LB = SideBufs{};
     *RB = SideBufs{};
     return false;
   };
+  // two distinct cells shared a hash: every dictionary again with the next seed
+  for (int attempt = 1; (h[ing::kSumFlags] & ing::kFlagCollision) && attempt < kMaxAttempts;
+       attempt++) {
+    const unsigned long long clear = h[ing::kSumFlags] & ~(unsigned long long)ing::kFlagCollision;
+    HBX_CUDA(cudaMemcpyAsync(sum.p + ing::kSumFlags, &clear, sizeof clear, cudaMemcpyHostToDevice, st));
+    eq_dictionaries(seed_of(attempt));
+    read_summary();
+  }
   if (h[ing::kSumFlags] & ing::kFlagCollision)
-    return give_up("two distinct dictionary cells share a 64-bit hash");
+    return give_up("dictionary cells collide under four hash seeds");
   if (h[ing::kSumFlags] & ing::kFlagTableFull) return give_up("dictionary table full");
   E.pairs_covered = h[ing::kSumPairs];
   E.n_partitions_used = (uint32_t)h[ing::kSumUsed];
@@ -569,7 +645,79 @@ bool device_encode(const hbx_table* left, const hbx_table* right, Encoded* Ep, S
   E.R.str_maxlen.assign(n_sr, 0);
   for (size_t s = 0; s < n_sl; s++) E.L.str_maxlen[s] = (uint32_t)h[i_mxl + s];
   for (size_t s = 0; s < n_sr; s++) E.R.str_maxlen[s] = (uint32_t)h[i_mxr + s];
-  if (!finish_rules(&E, false)) return give_up("a rule's join keys need composite ids");
+
+  // ---- join-key domains; composite ids for rules whose mixed-radix domain
+  // is too large: each row's (bucket, codes) tuple through a dictionary of
+  // its own, then the tuple ids regrouped by bucket
+  std::vector<size_t> comp_rules;
+  for (size_t r = 0; r < E.rules.size(); r++)
+    if (!rule_mixed_domain(E, &E.rules[r])) comp_rules.push_back(r);
+  const size_t n_comp = comp_rules.size();
+  LB->comp.alloc(std::max<size_t>(n_comp * nL, 1));
+  RB->comp.alloc(std::max<size_t>(n_comp * nR, 1));
+  if (n_comp) {
+    DBuf<int32_t> tcode_l, tcode_r;
+    DBuf<uint32_t> tup_l, tup_r, code_bucket, per_bucket, start, cursor, remap;
+    tcode_l.alloc(std::max<uint32_t>(nL, 1));
+    tcode_r.alloc(std::max<uint32_t>(nR, 1));
+    code_bucket.alloc(cap);
+    remap.alloc(cap);
+    per_bucket.alloc(n_part + 1);
+    start.alloc(n_part + 1);
+    cursor.alloc(n_part + 1);
+    DBuf<unsigned long long> dsum;
+    dsum.alloc(1);
+    for (size_t ci = 0; ci < n_comp; ci++) {
+      RuleEnc& re = E.rules[comp_rules[ci]];
+      ing::TupleSlots ts{};
+      ts.k = (uint32_t)re.eq_slot.size();
+      for (uint32_t j = 0; j < ts.k; j++) ts.slot[j] = (uint32_t)re.eq_slot[j];
+      const uint32_t w = ts.k + 1;
+      tup_l.alloc(std::max<size_t>((size_t)nL * w, 1));
+      tup_r.alloc(std::max<size_t>((size_t)nR * w, 1));
+      if (nL) ing::k_tuples<<<grid_for(nL, n_sm), 256, 0, st>>>(LB->bucket.p, LB->eq.p, nL, ts, tup_l.p);
+      if (nR) ing::k_tuples<<<grid_for(nR, n_sm), 256, 0, st>>>(RB->bucket.p, RB->eq.p, nR, ts, tup_r.p);
+      const ing::ColDev tl{reinterpret_cast<const uint8_t*>(tup_l.p), nullptr, 0, 4 * w};
+      const ing::ColDev tr{reinterpret_cast<const uint8_t*>(tup_r.p), nullptr, 0, 4 * w};
+      unsigned long long n_codes = 0;
+      for (int attempt = 0;; attempt++) {
+        HBX_CUDA(cudaMemsetAsync(sum.p + ing::kSumFlags, 0, sizeof(unsigned long long), st));
+        dictionary(tl, tr, tcode_l.p, tcode_r.p, dsum.p, seed_of(attempt));
+        unsigned long long got[2] = {0, 0};
+        HBX_CUDA(cudaMemcpyAsync(&got[0], sum.p + ing::kSumFlags, 8, cudaMemcpyDeviceToHost, st));
+        HBX_CUDA(cudaMemcpyAsync(&got[1], dsum.p, 8, cudaMemcpyDeviceToHost, st));
+        HBX_CUDA(cudaStreamSynchronize(st));
+        if (got[0] & ing::kFlagTableFull) return give_up("dictionary table full");
+        n_codes = got[1];
+        if (!(got[0] & ing::kFlagCollision)) break;
+        if (attempt + 1 == kMaxAttempts) return give_up("join-key tuples collide under four hash seeds");
+      }
+      HBX_CUDA(cudaMemsetAsync(per_bucket.p, 0, (n_part + 1) * 4, st));
+      HBX_CUDA(cudaMemsetAsync(cursor.p, 0, (n_part + 1) * 4, st));
+      ing::k_code_bucket<<<grid_for(cap, n_sm), 256, 0, st>>>(keys.p, code.p, rep.p, cap,
+                                                              LB->bucket.p, RB->bucket.p, nL,
+                                                              code_bucket.p, per_bucket.p);
+      scan_u32(per_bucket.p, (uint32_t)(n_part + 1), start.p, st);  // start[n_part] = n_codes
+      if (n_codes)
+        ing::k_code_remap<<<grid_for(n_codes, n_sm), 256, 0, st>>>(code_bucket.p, (uint32_t)n_codes,
+                                                                  start.p, cursor.p, remap.p);
+      if (nL)
+        ing::k_apply_remap<<<grid_for(nL, n_sm), 256, 0, st>>>(tcode_l.p, nL, remap.p,
+                                                               LB->comp.p + ci * nL);
+      if (nR)
+        ing::k_apply_remap<<<grid_for(nR, n_sm), 256, 0, st>>>(tcode_r.p, nR, remap.p,
+                                                               RB->comp.p + ci * nR);
+      check_launch("ingest composite keys");
+      std::vector<uint32_t> hs(n_part + 1);
+      HBX_CUDA(cudaMemcpyAsync(hs.data(), start.p, (n_part + 1) * 4, cudaMemcpyDeviceToHost, st));
+      HBX_CUDA(cudaStreamSynchronize(st));
+      re.composite = true;
+      re.comp_index = (int)ci;
+      re.domain = std::max<uint64_t>(n_codes, 1);
+      re.part_key_begin.assign(hs.begin(), hs.end());
+      if (re.domain > (1ull << 31)) fail(HBX_ERR_UNSUPPORTED, "join key domain too large");
+    }
+  }
   return true;
 }
 

@@ -20,16 +20,22 @@ constexpr uint32_t kFlagCollision = 1, kFlagTableFull = 2;
 // alphabet size, then call-specific words
 enum : uint32_t { kSumPairs = 0, kSumUsed = 1, kSumFlags = 2, kSumSymbols = 3, kSumFixed = 4 };
 
-// One device column: cell bytes and int64 offsets (n + 1), as a host Column.
+// One device column: cell bytes and int64 offsets (n + 1), as a host Column;
+// or, with width > 0, cells of `width` bytes back to back (no offsets).
 struct ColDev {
   const uint8_t* bytes;
   const int64_t* off;
   uint32_t has_nul;
+  uint32_t width;
 };
 
 // Length of cell i, cut at its first NUL when the column has NUL bytes
 // (the reference compares cells as C strings); *start = its first byte.
 __device__ __forceinline__ uint32_t cell_len(const ColDev& c, uint32_t i, int64_t* start) {
+  if (c.width) {
+    *start = (int64_t)i * c.width;
+    return c.width;
+  }
   const int64_t a = c.off[i];
   const uint32_t n = (uint32_t)(c.off[i + 1] - a);
   *start = a;
@@ -41,7 +47,7 @@ __device__ __forceinline__ uint32_t cell_len(const ColDev& c, uint32_t i, int64_
 
 __global__ void k_dict_insert(ColDev c, uint32_t n, uint32_t gid_base, unsigned long long* keys,
                               uint32_t* rep, uint32_t mask, uint32_t* row_slot,
-                              unsigned long long* sum);
+                              unsigned long long* sum, unsigned long long seed);
 __global__ void k_occupied(const unsigned long long* keys, uint32_t cap, uint32_t* occ);
 __global__ void k_dict_assign(ColDev c, uint32_t n, uint32_t gid_base, const uint32_t* row_slot,
                               const uint32_t* code, const uint32_t* rep, ColDev cl, ColDev cr,
@@ -64,6 +70,12 @@ void check_launch(const char* what);
 // its scratch comes from the current pool.
 void scan_u32(const uint32_t* in, uint32_t n, uint32_t* out, cudaStream_t st);
 
+// Seed of the dictionaries' first hash; a rebuild after a collision uses
+// kDictSeed + attempt.  With the environment variable
+// HBX_TEST_DICT_COLLIDE=1 the first build keeps only 3 bits of each hash, so
+// that tests can check that collisions are resolved on the device.
+constexpr unsigned long long kDictSeed = 0xc70f6907ull;
+
 // Encodes both tables for one plan on the device, writing the side buffers
 // directly: partition buckets with the reference's std::hash
 // (data_mngr.h:150-202), one joint dictionary per equality slot, the
@@ -75,11 +87,15 @@ void scan_u32(const uint32_t* in, uint32_t n, uint32_t* out, cudaStream_t st);
 //
 // E must come from encode_schema.  On success E gets the dictionary sizes,
 // the alphabet size, the longest string per slot, pairs_covered and the rule
-// domains, and *h2d the bytes copied.  Returns false, with the reason in
-// *why, when only the host encoder is exact for the input: a rule whose join
-// keys need composite ids, or two distinct cells of a dictionary column with
-// the same 64-bit hash (detected by comparing every cell with its slot's
-// representative).  The side buffers are then left empty.
+// domains (a rule whose mixed-radix key domain exceeds kMaxKeyDomain gets
+// dense composite ids built on the device: its (bucket, codes) tuples go
+// through the same dictionary, and the ids are regrouped by bucket), and
+// *h2d the bytes copied.  Two distinct cells with the same 64-bit hash are
+// detected by comparing every cell with its slot's representative; the
+// dictionaries are then rebuilt with another seed.  Returns false, with the
+// reason in *why, only when the input is beyond the device path (2^30 rows
+// or more, or collisions under four seeds); the side buffers are then left
+// empty.
 bool device_encode(const hbx_table* left, const hbx_table* right, Encoded* E, SideBufs* L,
                    SideBufs* R, int n_sm, cudaStream_t st, uint64_t* h2d, std::string* why);
 

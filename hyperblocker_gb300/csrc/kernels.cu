@@ -33,6 +33,19 @@ __global__ void k_keys_hist(Side S, const Rule* rules, uint32_t rule, int side) 
   }
 }
 
+// A right row's metadata as the join stores it in sorted_meta_r: the string
+// metadata of the rule's first similarity column, with the row's dictionary
+// codes of the group's first two extra equality slots in loc.z and loc.w
+// (unused words of the string record), so that the filter compares them
+// from the staged copy.
+__device__ __forceinline__ StrMeta sorted_meta(const Side& S, const Rule& Q, const StrMeta* meta_in,
+                                               uint32_t row) {
+  StrMeta m = meta_in[row];
+  if (Q.n_xslots > 0) m.loc.z = (uint32_t)S.eq_codes[(size_t)Q.xslot[0] * S.n_rows + row];
+  if (Q.n_xslots > 1) m.loc.w = (uint32_t)S.eq_codes[(size_t)Q.xslot[1] * S.n_rows + row];
+  return m;
+}
+
 __global__ void k_scatter(Side S, const Rule* rules, uint32_t rule, int side) {
   const Rule& R = rules[rule];
   if (!R.n_members) return;  // evaluated in another rule's group: no items of its own
@@ -47,7 +60,7 @@ __global__ void k_scatter(Side S, const Rule* rules, uint32_t rule, int side) {
     const uint32_t k = keys[row];
     const uint32_t pos = off[k] + atomicAdd(cur + k, 1u);
     sorted[pos] = row;
-    if (meta_out) meta_out[pos] = meta_in[row];
+    if (meta_out) meta_out[pos] = sorted_meta(S, R, meta_in, row);
   }
 }
 
@@ -364,7 +377,7 @@ __global__ void k_join_scatter(Side L, Side R, const Rule* rules, uint32_t n_rul
       const uint32_t k = Q.key_r[row];
       const uint32_t pos = Q.off_r[k] + atomicAdd(Q.cur_r + k, 1u);
       Q.sorted_r[pos] = row;
-      if (Q.sorted_meta_r) Q.sorted_meta_r[pos] = meta_in[row];
+      if (Q.sorted_meta_r) Q.sorted_meta_r[pos] = sorted_meta(R, Q, meta_in, row);
     }
   }
 }
@@ -864,10 +877,18 @@ __device__ __forceinline__ int scan_step(Scan<W>& z, uint32_t* m_out, WorkTally*
 // member is left (0).  A member drops out at its first failing predicate.
 // Each predicate first goes through the filters of the first column: length
 // bound, common prefix, count signatures.
+//
+// *memo names the column (left slot << 16 | right slot) whose scan the lane
+// finished last, with match count memo_m, while the scan state z still holds
+// its lengths and prefix: a later member testing the same column at its own
+// threshold is decided from it without another scan.  Starting a scan ends
+// the memo.
+constexpr uint32_t kNoMemo = 0xffffffffu;
 template <int W>
 __device__ __forceinline__ int advance_group(const EvalParams& P, uint32_t rule, uint32_t* live,
                                              uint32_t* mi, uint32_t* s, uint32_t lrow,
-                                             uint32_t rrow, Scan<W>& z, WorkTally* ops) {
+                                             uint32_t rrow, Scan<W>& z, uint32_t* memo,
+                                             uint32_t memo_m, WorkTally* ops) {
   const Rule* R = P.rules + rule;
   while (*live) {
     const Member* M = R->mem + *mi;
@@ -876,6 +897,10 @@ __device__ __forceinline__ int advance_group(const EvalParams& P, uint32_t rule,
     for (; k < n_rest; k++) {
       const uint32_t sl = M->rest_l[k], sr = M->rest_r[k];
       const float thr = M->rest_thr[k];
+      if (*memo == (sl << 16 | sr)) {
+        if (!jw_decide(memo_m, z.ls, z.ll, z.p, thr, &P.ctr->ambiguous)) break;
+        continue;
+      }
       const StrMeta* am = P.L.str_meta + (size_t)sl * P.L.n_rows + lrow;
       const StrMeta* bm = P.R.str_meta + (size_t)sr * P.R.n_rows + rrow;
       const uint4 al = am->loc, bl = bm->loc;
@@ -905,6 +930,7 @@ __device__ __forceinline__ int advance_group(const EvalParams& P, uint32_t rule,
         if (need > 0 && (int)sig_bound(am->sig[0], am->sig[1], bm->sig[0], bm->sig[1]) < need)
           break;
       }
+      *memo = kNoMemo;  // z is about to hold another pair's scan
       if (scan_begin<W>(z, peq_table(P, sl, lrow), a, b, bh, la, lb, p, need, thr, ops)) {
         *s = k;
         return 2;
@@ -980,10 +1006,16 @@ __device__ __forceinline__ uint32_t filter_batch(const EvalParams& P, const Warp
   const uint32_t all = C->i_all;
   uint32_t live = act ? all : 0u;
   float thr = C->i_thr;
+  uint4 loc = make_uint4(0, 0, 0, 0), head = make_uint4(0, 0, 0, 0);
+  if (act) loc = meta[e].loc;
   if (act && (C->i_kind & kItemExtras)) {
+    // the right row's codes of the extra slots: the first two staged with
+    // its metadata (sorted_meta), the others from device memory
     uint32_t eqm = 0;
     const uint32_t nx = R->n_xslots;
-    for (uint32_t j = 0; j < nx; j++)
+    if ((int32_t)loc.z == C->i_lcode[0]) eqm |= 1u;
+    if (nx > 1 && (int32_t)loc.w == C->i_lcode[1]) eqm |= 2u;
+    for (uint32_t j = 2; j < nx; j++)
       if (P.R.eq_codes[(size_t)R->xslot[j] * P.R.n_rows + rrow] == C->i_lcode[j]) eqm |= 1u << j;
     for (uint32_t x = all; x; x &= x - 1) {
       const uint32_t k = (uint32_t)__ffs(x) - 1u;
@@ -991,11 +1023,7 @@ __device__ __forceinline__ uint32_t filter_batch(const EvalParams& P, const Warp
     }
     if (live != all) thr = live_thr(R, live);
   }
-  uint4 loc = make_uint4(0, 0, 0, 0), head = make_uint4(0, 0, 0, 0);
-  if (live) {
-    loc = meta[e].loc;
-    head = meta[e].head;
-  }
+  if (live) head = meta[e].head;
   uint32_t pass1 = 0;  // members that passed the first column without a scan
   bool scan = false;
   uint32_t p = 0;
@@ -1275,6 +1303,7 @@ __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
   // in hand (first = the group's first column)
   bool busy = false, first = false;
   uint32_t rrow = 0, lrow = 0, rule = 0, s = 0, live = 0, mi = 0;
+  uint32_t memo = kNoMemo, memo_m = 0;  // the last finished column scan (advance_group)
   Scan<W> z;
   z.tab = nullptr;
   z.b = nullptr;
@@ -1351,12 +1380,13 @@ __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
       lrow = e2.x;
       rule = e2.w;
       live = tag_live(e0.w);
+      memo = kNoMemo;
       int st = 0;
       if (e0.w & kAdvance) {
         first = false;
         mi = tag_member(e0.w);
         s = tag_s(e0.w);
-        st = advance_group<W>(P, rule, &live, &mi, &s, lrow, rrow, z, ops);
+        st = advance_group<W>(P, rule, &live, &mi, &s, lrow, rrow, z, &memo, memo_m, ops);
       } else {
         // the group's first column at the smallest live threshold
         first = true;
@@ -1395,9 +1425,15 @@ __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
             live = pass1;
             mi = (uint32_t)__ffs(pass1) - 1u;
             s = 0;
-            st = advance_group<W>(P, rule, &live, &mi, &s, lrow, rrow, z, ops);
+            memo = kNoMemo;
+            st = advance_group<W>(P, rule, &live, &mi, &s, lrow, rrow, z, &memo, memo_m, ops);
           }
         } else {
+          // a complete scan is remembered for the other members' tests of
+          // the same column; a scan stopped early is not (its count is partial)
+          const Member* M = P.rules[rule].mem + mi;
+          memo = sc == 1 ? (M->rest_l[s] << 16 | M->rest_r[s]) : kNoMemo;
+          memo_m = m;
           if (sc == 1 && jw_decide(m, z.ls, z.ll, z.p, z.thr, &P.ctr->ambiguous)) {
             s++;  // member mi passed predicate s
           } else {
@@ -1405,7 +1441,8 @@ __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
             mi = live ? (uint32_t)__ffs(live) - 1u : 0u;
             s = 0;
           }
-          if (live) st = advance_group<W>(P, rule, &live, &mi, &s, lrow, rrow, z, ops);
+          if (live)
+            st = advance_group<W>(P, rule, &live, &mi, &s, lrow, rrow, z, &memo, memo_m, ops);
         }
         if (st == 2) {
           busy = true;

@@ -465,7 +465,8 @@ void open_server(hbx_server* S, const hbx_plan* const* plans, int32_t n_plans, c
     const ing::ColDev rc = S->rcols[pr.second].view();
     if (nR)
       ing::k_dict_insert<<<grid_for(nR, C->n_sm), 256, 0, st>>>(rc, nR, 0, D.keys.p, D.rep.p,
-                                                                 D.cap - 1, row_slot.p, sum.p);
+                                                                 D.cap - 1, row_slot.p, sum.p,
+                                                                 kDictSeed);
     ing::k_occupied<<<grid_for(D.cap, C->n_sm), 256, 0, st>>>(D.keys.p, D.cap, occ.p);
     scan_u32(occ.p, D.cap, D.code.p, st);
     if (nR)

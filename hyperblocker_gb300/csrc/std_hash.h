@@ -38,8 +38,10 @@ HBX_HD uint64_t load_le(const uint8_t* p, uint32_t n) {
   return v;
 }
 
-HBX_HD uint64_t std_hash_bytes(const uint8_t* p, uint64_t len) {
-  uint64_t h = kStdHashSeed ^ (len * kStdHashMul);
+// The same hash with another seed (the dictionaries rehash with a fresh seed
+// when two distinct cells share a hash).
+HBX_HD uint64_t hash_bytes_seeded(const uint8_t* p, uint64_t len, uint64_t seed) {
+  uint64_t h = seed ^ (len * kStdHashMul);
   const uint64_t whole = len & ~7ull;
   for (uint64_t i = 0; i < whole; i += 8) {
     const uint64_t w = std_hash_mix(load_le(p + i, 8) * kStdHashMul) * kStdHashMul;
@@ -47,6 +49,10 @@ HBX_HD uint64_t std_hash_bytes(const uint8_t* p, uint64_t len) {
   }
   if (len & 7) h = (h ^ load_le(p + whole, (uint32_t)(len & 7))) * kStdHashMul;
   return std_hash_mix(std_hash_mix(h) * kStdHashMul);
+}
+
+HBX_HD uint64_t std_hash_bytes(const uint8_t* p, uint64_t len) {
+  return hash_bytes_seeded(p, len, kStdHashSeed);
 }
 
 }  // namespace hbx

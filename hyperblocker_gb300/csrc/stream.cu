@@ -193,6 +193,11 @@ extern "C" hbx_status hbx_block_streamed(hbx_ctx* ctx, const hbx_plan* plan, con
     }
 
     // ---- two workers, each with its own context and stream
+    int eval_ctas = 0;
+    {
+      // 2 CTAs per SM is what the evaluation kernels fit (kernels.cuh)
+      eval_ctas = std::max(1, ctx->n_sm * 2 - std::max(2, ctx->n_sm / 4));
+    }
     std::atomic<size_t> next{0};
     std::mutex mu;
     // matches per pair covered in the windows done so far: sizes the next
@@ -259,6 +264,10 @@ extern "C" hbx_status hbx_block_streamed(hbx_ctx* ctx, const hbx_plan* plan, con
               const uint64_t cap = std::max<uint64_t>(window_bytes / 8, 1 << 16);
               reserve_output(s, (uint64_t)std::min<double>(want, (double)cap));
             }
+            // leave an eighth of the CTA slots to the other worker, so that
+            // its window's copies, encoding and join run beside this
+            // window's persistent evaluation instead of after it
+            if (windows.size() > 1) set_eval_ctas(s, eval_ctas);
             run_to_host(s, mode, &l, &r);
             hbx_session_stats(s, &ws);
           } catch (const Error& e) {

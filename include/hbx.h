@@ -75,8 +75,10 @@ typedef struct hbx_opts {
                                 registers, 0 = autotuned */
   int32_t pred_order;        /* similarity predicates of a rule run in: 0 = order of measured
                                 selectivity and cost (default), 1 = the order the rule gives */
-  int32_t ingest;            /* tables are encoded: 0 = on the device (default; the host
-                                encoder still takes the inputs only it encodes exactly),
+  int32_t ingest;            /* tables are encoded: 0 = on the device (default: buckets,
+                                dictionaries, composite join keys, arenas; the host
+                                encoder takes over only beyond 2^30 rows, or when
+                                dictionary cells collide under four hash seeds),
                                 1 = on the host */
   uint64_t watchdog_cycles;  /* per-CTA SM-cycle budget of the persistent loop, 0 = none */
 } hbx_opts;

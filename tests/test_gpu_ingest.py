@@ -5,9 +5,11 @@ restatement of libstdc++'s std::hash (data_mngr.h:150-202), joint
 dictionaries, the symbol alphabet, arenas and string metadata.  Every case
 here runs the same inputs through the device encoder and the host encoder
 (hbx_opts.ingest = 1) and requires both to give the oracle's pair set and
-the same pairs_covered / pair_comparisons, including the inputs the device
-path hands back to the host encoder (composite join keys).
+the same pairs_covered / pair_comparisons, including composite join keys
+(built on the device) and dictionary hash collisions (rebuilt on the device
+with another seed).
 """
+
 import numpy as np
 import pytest
 
@@ -103,10 +105,11 @@ def test_no_equalities(built):
     _check(docs, cl, cr, 1)
 
 
-def test_composite_keys_go_to_the_host_encoder(built):
+def test_composite_keys_on_the_device(built):
     """Two equalities with ~4000 distinct values each: the mixed-radix key
-    domain is above 2^24, so the join needs composite ids, which only the
-    host encoder builds; the device session must hand over and stay exact."""
+    domain is above 2^24, so the join needs composite ids; the device encoder
+    builds them (tuple dictionary, ids regrouped by partition) and gives the
+    host encoder's pairs and counts."""
     rng = np.random.Generator(np.random.PCG64(35))
 
     def table(n, prefix):
@@ -120,8 +123,19 @@ def test_composite_keys_go_to_the_host_encoder(built):
     # make some rows agree on both keys
     for i in range(1, 400):
         cr[3][i], cr[4][i] = cl[3][i], cl[4][i]
-    docs = [synth.rule_yaml([3, 4], [(1, 0.5)])]
-    _check(docs, cl, cr, 2, expect_device=False)
+    docs = [synth.rule_yaml([3, 4], [(1, 0.5)]), synth.rule_yaml([3], [(1, 0.9)])]
+    _check(docs, cl, cr, 2)
+
+
+def test_dictionary_collisions_are_rebuilt_on_the_device(built, monkeypatch):
+    """HBX_TEST_DICT_COLLIDE=1 makes the first dictionary build keep 3 bits of
+    each hash, so distinct cells collide; the exact check against each slot's
+    representative finds it and the dictionaries are rebuilt with the next
+    seed, on the device, with the same result (composite keys included)."""
+    monkeypatch.setenv("HBX_TEST_DICT_COLLIDE", "1")
+    cl, cr = _util.random_tables(36, 150, 400, b"abcdef", 30, n_eq_values=40)
+    docs = [synth.rule_yaml([3], [(1, 0.6)]), synth.rule_yaml([3, 4], [(2, 0.5)])]
+    _check(docs, cl, cr, 3)
 
 
 def test_c2_shape_device_and_host_agree(built, tmp_path):
