@@ -261,8 +261,8 @@ class C3:
         torch.cuda.nvtx.range_push(f"c3_{mode}")
         for _ in range(warm):
             self.step(mode)
-        rec = {"ms": [], "ms_eval": [], "ops": [], "scan_ops": [], "cmp": [], "launches": 0,
-               "matches": 0}
+        rec = {"ms": [], "ms_eval": [], "ops": [], "scan_ops": [], "scanned": [], "cmp": [],
+               "launches": 0, "matches": 0, "stats": None}
         with torch.cuda.stream(self.stream):
             for _ in range(k):
                 self.flush.zero_()
@@ -277,9 +277,11 @@ class C3:
                 rec["ms_eval"].append(st.ms_eval)
                 rec["ops"].append(st.jw_word_ops)
                 rec["scan_ops"].append(st.scan_word_ops)
+                rec["scanned"].append(st.pairs_scanned)
                 rec["cmp"].append(st.pair_comparisons)
                 rec["launches"] += st.n_launches
                 rec["matches"] = n
+                rec["stats"] = st  # of the form's last step
         torch.cuda.nvtx.range_pop()
         return rec
 
@@ -768,7 +770,7 @@ def run_engine(args, rank, world, local_rank):
 
     line = None
     if rank == 0:
-        st = c3.sess.stats()
+        st = bat["stats"]  # the batched form's last timed step
         e2e = c3.e2e(ctx, args.e2e_steps)
         e2e["value"] *= world
         peaks = _peaks()
@@ -796,7 +798,9 @@ def run_engine(args, rank, world, local_rank):
                             "this run"),
             "scan_word_ops_per_launch": scan_ops, "jw_word_ops_per_launch": ops,
             "ms_per_launch": ms_eval, "scan_words": int(st.scan_words),
-            "pairs_scanned_per_launch": int(st.pairs_scanned),
+            "pairs_scanned_per_launch": int(statistics.mean(bat["scanned"])),
+            "pairs_scanned_per_launch_plain": int(statistics.mean(pla["scanned"])),
+            "scan_word_ops_per_step_plain": statistics.mean(pla["scan_ops"]),
             "tile_right": int(st.tile_right), "eval_variant": int(st.eval_variant),
             "join_ms_per_step": statistics.mean([m - e for m, e in zip(bat["ms"], bat["ms_eval"])]),
             "hbm_gbs_measured": peaks.get("hbm_gbs"),

@@ -85,6 +85,7 @@ struct hbx_session {
   hbx::dev::PeqShape peq_shape{};
   hbx::DBuf<uint32_t> peq;  // Peq tables of the left strings [slot][row]
   int variant = 0;  // evaluation kernel: 0 = k_eval, 1 = k_eval_wide
+  bool groups = false;  // some rule evaluates others in the batched form (h_groups)
   bool tuned = false;
   bool one_shot = false;  // runs once (hbx_block): no graph is captured
   // output slots to start with; a run needing more than cap_limit (the
@@ -149,6 +150,7 @@ void configure(hbx_session* S, uint32_t tile_right, int variant) {
   S->tile_right = std::min<uint32_t>(512, std::max<uint32_t>(32, (tile_right + 31) / 32 * 32));
   S->variant = variant ? 1 : 0;
   const dev::EvalKernel kern = dev::eval_kernel(S->variant);
+  const dev::EvalKernel kern_g = dev::eval_kernel(S->variant, true);
   const size_t smem_cap = std::min<size_t>(C->smem_optin, 200 * 1024);
   const uint32_t cap_warp_words = (uint32_t)(smem_cap / 4 / dev::kWarpsPerCta) / 4 * 4;
   S->wl = dev::warp_layout_fit(S->tile_right, smem_cap);
@@ -162,6 +164,7 @@ void configure(hbx_session* S, uint32_t tile_right, int variant) {
                            cudaMemcpyHostToDevice, C->stream));
   HBX_CUDA(cudaStreamSynchronize(C->stream));
   raise_smem_limit(kern, S->smem_bytes);
+  raise_smem_limit(kern_g, S->smem_bytes);
   int bps = 0;
   HBX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, kThreads, S->smem_bytes));
   S->blocks_per_sm = std::max(1, bps);
@@ -299,6 +302,9 @@ void setup_session(hbx_session* S, uint64_t h2d_tables) {
     if (S->fused_join) S->scan_totals.alloc((size_t)S->h_rules.size() * 3 * nb);
   }
   S->h_groups = group_rules(S->h_rules);
+  S->groups = false;
+  for (const dev::Rule& g : S->h_groups)
+    if (g.n_members > 1) S->groups = true;
   S->d_rules.alloc(E.rules.size());
   S->d_groups.alloc(E.rules.size());
   S->d_rule_base.alloc(E.rules.size() + 1);
@@ -617,7 +623,7 @@ uint32_t enqueue_batched(hbx_session* S, cudaStream_t st) {
   int grid = S->ctx->n_sm * S->blocks_per_sm;
   if (S->max_eval_ctas > 0) grid = std::min(grid, S->max_eval_ctas);
   HBX_CUDA(cudaEventRecordWithFlags(S->ev_eval0, st, rec_flags));
-  dev::eval_kernel(S->variant)<<<grid, kThreads, S->smem_bytes, st>>>(P);
+  dev::eval_kernel(S->variant, S->groups)<<<grid, kThreads, S->smem_bytes, st>>>(P);
   launch_check("k_eval");
   HBX_CUDA(cudaEventRecordWithFlags(S->ev_eval1, st, rec_flags));
   // the counters travel back inside the run (graph nodes when captured)

@@ -870,6 +870,56 @@ __device__ __forceinline__ int scan_step(Scan<W>& z, uint32_t* m_out, WorkTally*
   return 0;
 }
 
+// The similarity predicates after predicate s of a pair that passed it, in
+// order, until one needs a scan (returns 2, the scan state set up and s its
+// index), one fails (0) or all pass (1).  Each predicate first goes through
+// the filters of the first one: length bound, common prefix, count
+// signatures.  (A launch without rule groups: every rule evaluated alone.)
+template <int W>
+__device__ __forceinline__ int advance_rule(const EvalParams& P, uint32_t rule, uint32_t* s,
+                                            uint32_t lrow, uint32_t rrow, Scan<W>& z,
+                                            WorkTally* ops) {
+  const Rule* R = P.rules + rule;
+  const uint32_t n_sim = R->n_sim;
+  for (uint32_t k = *s + 1; k < n_sim; k++) {
+    *s = k;
+    const uint32_t sl = R->sim_l[k], sr = R->sim_r[k];
+    const float thr = R->thr[k];
+    const StrMeta* am = P.L.str_meta + (size_t)sl * P.L.n_rows + lrow;
+    const StrMeta* bm = P.R.str_meta + (size_t)sr * P.R.n_rows + rrow;
+    const uint4 al = am->loc, bl = bm->loc;
+    const uint32_t la = al.y, lb = bl.y;
+    const uint8_t* a = P.L.arena + 16ull * al.x;
+    const uint8_t* b = P.R.arena + 16ull * bl.x;
+    if (!has_table(P, la)) {  // the reference's own loops
+      if (la && lb) ops->ops += jw_eval_ops(min(la, lb), max(la, lb));
+      if (!sim_pass_slow(a, la, b, lb, thr, P.ctr)) return 0;
+      continue;
+    }
+    if (lb == 0) {
+      if (!jw_exact(0, la, 0, 0, thr, &P.ctr->ambiguous)) return 0;
+      continue;
+    }
+    const uint32_t ls = min(la, lb), ll = max(la, lb);
+    ops->ops += jw_eval_ops(ls, ll);
+    const uint4 bh = bm->head;
+    const uint32_t p16 = prefix16(am->head, bh);
+    uint32_t p = kPrefixUnknown;
+    int need = 0;
+    if (!(p16 == 16u && ls > 16u)) {
+      p = min(p16, ls);
+      need = m_need_lo(ls, ll, p, thr);
+      const uint32_t n_iter = min(lb, la + ((ls + 1u) >> 1));
+      if (need > (int)min(n_iter, ls)) return 0;
+      if (need > 0 &&
+          (int)sig_bound(am->sig[0], am->sig[1], bm->sig[0], bm->sig[1]) < need)
+        return 0;
+    }
+    return scan_begin<W>(z, peq_table(P, sl, lrow), a, b, bh, la, lb, p, need, thr, ops) ? 2 : 0;
+  }
+  return 1;
+}
+
 // The similarity predicates after the group's first column, for the live
 // members of a pair's group in member order, from predicate *s of member
 // *mi: until one needs a scan (returns 2, the scan state set up for (*mi,
@@ -954,7 +1004,7 @@ constexpr uint32_t kMaxClaimChunk = 16;
 // Kind of a claimed item: its rule has similarity predicates, and some
 // member of its group has extra equality slots; bits 8-11 hold the group's
 // member count.
-constexpr uint32_t kItemSim = 1u, kItemExtras = 2u;
+constexpr uint32_t kItemSim = 1u, kItemExtras = 2u, kItemMore = 4u;  // more: n_sim > 1
 __device__ __forceinline__ uint32_t item_members(uint32_t kind) { return (kind >> 8) & 15u; }
 // A claimed work item: the sources of its bulk copies (right-row metadata
 // from the block's first row, right rows from the 16-byte boundary at or
@@ -992,6 +1042,9 @@ static_assert(sizeof(WarpCtl) <= kWarpCtlWords * 4, "warp control block outgrows
 // decided without a scan that pass go to the ring for their members' further
 // predicates, or match at once when a passing member has none.  lm: the
 // item's left string metadata.  Returns the entries appended.
+// G: the launch has rule groups; without, every rule is its own group of one
+// and its predicates take the plain path (one threshold per predicate).
+template <bool G>
 __device__ __forceinline__ uint32_t filter_batch(const EvalParams& P, const WarpCtl* C,
                                                  const StrMeta* lm, const uint32_t* rows,
                                                  const StrMeta* meta, uint32_t n, uint32_t e0,
@@ -1008,7 +1061,7 @@ __device__ __forceinline__ uint32_t filter_batch(const EvalParams& P, const Warp
   float thr = C->i_thr;
   uint4 loc = make_uint4(0, 0, 0, 0), head = make_uint4(0, 0, 0, 0);
   if (act) loc = meta[e].loc;
-  if (act && (C->i_kind & kItemExtras)) {
+  if (G && act && (C->i_kind & kItemExtras)) {
     // the right row's codes of the extra slots: the first two staged with
     // its metadata (sorted_meta), the others from device memory
     uint32_t eqm = 0;
@@ -1032,11 +1085,19 @@ __device__ __forceinline__ uint32_t filter_batch(const EvalParams& P, const Warp
     const uint32_t lb = loc.y;
     if (!C->i_fast) {  // the reference's own loops
       if (la && lb) ops->ops += jw_eval_ops(min(la, lb), max(la, lb));
-      uint32_t m = 0, pp = 0;
-      sim_m_slow(P.L.arena + 16ull * a_off, la, P.R.arena + 16ull * loc.x, lb, P.ctr, &m, &pp);
-      pass1 = first_pass(R, live, m, la, lb, pp, &P.ctr->ambiguous);
+      if constexpr (G) {
+        uint32_t m = 0, pp = 0;
+        sim_m_slow(P.L.arena + 16ull * a_off, la, P.R.arena + 16ull * loc.x, lb, P.ctr, &m, &pp);
+        pass1 = first_pass(R, live, m, la, lb, pp, &P.ctr->ambiguous);
+      } else {
+        pass1 = sim_pass_slow(P.L.arena + 16ull * a_off, la, P.R.arena + 16ull * loc.x, lb, thr,
+                              P.ctr) ? 1u : 0u;
+      }
     } else if (lb == 0) {
-      pass1 = first_pass(R, live, 0, la, 0, 0, &P.ctr->ambiguous);
+      if constexpr (G)
+        pass1 = first_pass(R, live, 0, la, 0, 0, &P.ctr->ambiguous);
+      else
+        pass1 = jw_exact(0, la, 0, 0, thr, &P.ctr->ambiguous) ? 1u : 0u;
     } else {
       const uint32_t ls = min(la, lb), ll = max(la, lb);
       ops->ops += jw_eval_ops(ls, ll);
@@ -1057,7 +1118,11 @@ __device__ __forceinline__ uint32_t filter_batch(const EvalParams& P, const Warp
       }
     }
   }
-  const bool done = pass1 && member_done(R, pass1);
+  bool done;
+  if constexpr (G)
+    done = pass1 && member_done(R, pass1);
+  else
+    done = pass1 && !(C->i_kind & kItemMore);
   const bool push = scan || (pass1 && !done);
   const unsigned qm = __ballot_sync(kFull, push);
   const uint32_t lrow = C->i_lrow;
@@ -1190,7 +1255,8 @@ __device__ __forceinline__ uint32_t claim_chunk(const EvalParams& P, WarpCtl* C,
   const uint32_t a0 = rb0 & ~3u;
   ItemDesc d;
   const bool sim = R.n_sim != 0;
-  d.kind = (sim ? kItemSim : 0u) | (R.n_xslots ? kItemExtras : 0u) | (R.n_members << 8);
+  d.kind = (sim ? kItemSim : 0u) | (R.n_xslots ? kItemExtras : 0u) |
+           (R.n_sim > 1 ? kItemMore : 0u) | (R.n_members << 8);
   d.meta_src = sim ? R.sorted_meta_r + rb0 : nullptr;
   d.rows_src = R.sorted_r + a0;
   d.lm_src = sim ? P.L.str_meta + (size_t)R.sim_l[0] * P.L.n_rows + lrow : nullptr;
@@ -1274,7 +1340,7 @@ __device__ __forceinline__ void claim_item(const EvalParams& P, WarpCtl* C, uint
 // it drains.  A pair that passes its group's first column goes on with the
 // further predicates of the members that passed, member by member, in the
 // same lane; matches leave by warp-aggregated atomics.
-template <int W>
+template <int W, bool G>
 __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
                                           unsigned long long n_work, WorkTally* ops,
                                           unsigned long long* done) {
@@ -1322,7 +1388,7 @@ __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
       uint32_t* buf = region + P.buf_off + cb * P.buf_words;
       if (active) {
         if (in_pos < cur_n) {
-          tail += filter_batch(P, C, reinterpret_cast<const StrMeta*>(buf + P.buf_lmeta_off),
+          tail += filter_batch<G>(P, C, reinterpret_cast<const StrMeta*>(buf + P.buf_lmeta_off),
                                buf + P.buf_rows_off + C->c_shift[cb],
                                reinterpret_cast<const StrMeta*>(buf), cur_n, in_pos, q, tail, ops);
           in_pos += 32;
@@ -1362,7 +1428,7 @@ __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
       C->i_kind = kind;
       C->i_all = (1u << item_members(kind)) - 1u;
       C->i_fast = has_table(P, la) ? 1u : 0u;
-      if (kind & kItemExtras) {  // the left row's codes of the extra equality slots
+      if (G && (kind & kItemExtras)) {  // the left row's codes of the extra equality slots
         const Rule* R = P.rules + ir;
         if ((uint32_t)lane < R->n_xslots)
           C->i_lcode[lane] = P.L.eq_codes[(size_t)R->xslot[lane] * P.L.n_rows + il];
@@ -1386,15 +1452,20 @@ __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
         first = false;
         mi = tag_member(e0.w);
         s = tag_s(e0.w);
-        st = advance_group<W>(P, rule, &live, &mi, &s, lrow, rrow, z, &memo, memo_m, ops);
+        if constexpr (G)
+          st = advance_group<W>(P, rule, &live, &mi, &s, lrow, rrow, z, &memo, memo_m, ops);
+        else
+          st = advance_rule<W>(P, rule, &s, lrow, rrow, z, ops);
       } else {
-        // the group's first column at the smallest live threshold
+        // the group's first column at the smallest live threshold (without
+        // groups: the rule's first predicate)
         first = true;
+        s = 0;
         const Rule* R = P.rules + rule;
         const uint32_t p = (e0.w >> 10) & 31u;
         st = scan_begin<W>(z, peq_table(P, R->sim_l[0], lrow), P.L.arena + 16ull * e2.z,
                            P.R.arena + 16ull * e0.y, en[1], e2.y, e0.z, p, (int)(e0.w & 1023u),
-                           live_thr(R, live), ops)
+                           G ? live_thr(R, live) : R->thr[0], ops)
                  ? 2
                  : 0;
       }
@@ -1412,7 +1483,11 @@ __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
       if (sc) {
         busy = false;
         int st = 0;
-        if (first) {
+        if constexpr (!G) {
+          // one rule: the scanned predicate s decides, then its next ones
+          if (sc == 1 && jw_decide(m, z.ls, z.ll, z.p, z.thr, &P.ctr->ambiguous))
+            st = advance_rule<W>(P, rule, &s, lrow, rrow, z, ops);
+        } else if (first) {
           // decided per live member; the scan stopped early only when even
           // the smallest threshold is out of reach
           const Rule* R = P.rules + rule;
@@ -1459,6 +1534,7 @@ __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
 
 // The evaluation kernel body, instantiated twice below with different
 // register budgets (see k_eval / k_eval_wide).
+template <bool G>
 __device__ __forceinline__ void eval_body(const EvalParams& P) {
   extern __shared__ __align__(16) uint32_t smem[];
   const int lane = threadIdx.x & 31;
@@ -1478,11 +1554,11 @@ __device__ __forceinline__ void eval_body(const EvalParams& P) {
   unsigned long long done = 0;
   WorkTally tally{0ull, 0u, 0u};
   switch (P.peq_w) {
-    case 1: eval_loop<1>(P, region, n_work, &tally, &done); break;
-    case 2: eval_loop<2>(P, region, n_work, &tally, &done); break;
-    case 3: eval_loop<3>(P, region, n_work, &tally, &done); break;
-    case 4: eval_loop<4>(P, region, n_work, &tally, &done); break;
-    default: eval_loop<8>(P, region, n_work, &tally, &done); break;
+    case 1: eval_loop<1, G>(P, region, n_work, &tally, &done); break;
+    case 2: eval_loop<2, G>(P, region, n_work, &tally, &done); break;
+    case 3: eval_loop<3, G>(P, region, n_work, &tally, &done); break;
+    case 4: eval_loop<4, G>(P, region, n_work, &tally, &done); break;
+    default: eval_loop<8, G>(P, region, n_work, &tally, &done); break;
   }
   if (lane == 0 && done) atomicAdd(&P.ctr->items_done, done);
   unsigned long long ops = tally.ops, scans = tally.scans, steps = tally.steps;
@@ -1529,11 +1605,21 @@ __global__ void k_peq_build(Side L, uint32_t n_slots, PeqShape shape, uint32_t* 
 }
 
 // Dense variant: 3 CTAs (24 warps) per SM, at most 85 registers per thread.
-__global__ void __launch_bounds__(kWarpsPerCta * 32, 3) k_eval(EvalParams P) { eval_body(P); }
+__global__ void __launch_bounds__(kWarpsPerCta * 32, 3) k_eval(EvalParams P) { eval_body<false>(P); }
 
 // Wide variant: 2 CTAs (16 warps) per SM, up to 128 registers per thread, so
 // the longer-string scan variants keep their state in registers.
-__global__ void __launch_bounds__(kWarpsPerCta * 32, 2) k_eval_wide(EvalParams P) { eval_body(P); }
+__global__ void __launch_bounds__(kWarpsPerCta * 32, 2) k_eval_wide(EvalParams P) {
+  eval_body<false>(P);
+}
+
+// The same two over rule groups (Rule: "Group evaluation").
+__global__ void __launch_bounds__(kWarpsPerCta * 32, 3) k_eval_groups(EvalParams P) {
+  eval_body<true>(P);
+}
+__global__ void __launch_bounds__(kWarpsPerCta * 32, 2) k_eval_groups_wide(EvalParams P) {
+  eval_body<true>(P);
+}
 
 }  // namespace dev
 }  // namespace hbx

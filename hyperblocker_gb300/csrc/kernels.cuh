@@ -352,9 +352,14 @@ __global__ void k_join_scatter(Side L, Side R, const Rule* rules, uint32_t n_rul
 __global__ void k_peq_build(Side L, uint32_t n_slots, PeqShape shape, uint32_t* peq);
 __global__ void k_eval(EvalParams P);       // 3 CTAs per SM (register-limited)
 __global__ void k_eval_wide(EvalParams P);  // 2 CTAs per SM (more registers)
+// the same over rule groups (launches where some rule evaluates others)
+__global__ void k_eval_groups(EvalParams P);
+__global__ void k_eval_groups_wide(EvalParams P);
 
 using EvalKernel = void (*)(EvalParams);
-inline EvalKernel eval_kernel(int wide) { return wide ? k_eval_wide : k_eval; }
+inline EvalKernel eval_kernel(int wide, bool groups = false) {
+  return groups ? (wide ? k_eval_groups_wide : k_eval_groups) : (wide ? k_eval_wide : k_eval);
+}
 
 constexpr uint32_t kScanChunk = 4096;  // elements per CTA in the scans (1024 threads x 4)
 
