@@ -278,6 +278,9 @@ class C3:
                 rec["ops"].append(st.jw_word_ops)
                 rec["scan_ops"].append(st.scan_word_ops)
                 rec["scanned"].append(st.pairs_scanned)
+                rec.setdefault("rest", []).append(st.rest_scans)
+                rec.setdefault("lane_util", []).append(
+                    st.scan_steps / (128.0 * st.scan_warp_steps) if st.scan_warp_steps else None)
                 rec["cmp"].append(st.pair_comparisons)
                 rec["launches"] += st.n_launches
                 rec["matches"] = n
@@ -800,6 +803,10 @@ def run_engine(args, rank, world, local_rank):
             "ms_per_launch": ms_eval, "scan_words": int(st.scan_words),
             "pairs_scanned_per_launch": int(statistics.mean(bat["scanned"])),
             "pairs_scanned_per_launch_plain": int(statistics.mean(pla["scanned"])),
+            "rest_scans_per_launch": int(statistics.mean(bat["rest"])),
+            "rest_scans_per_launch_plain": int(statistics.mean(pla["rest"])),
+            "scan_lane_utilisation": bat["lane_util"][-1],
+            "scan_lane_utilisation_plain": pla["lane_util"][-1],
             "scan_word_ops_per_step_plain": statistics.mean(pla["scan_ops"]),
             "tile_right": int(st.tile_right), "eval_variant": int(st.eval_variant),
             "join_ms_per_step": statistics.mean([m - e for m, e in zip(bat["ms"], bat["ms_eval"])]),

@@ -1006,6 +1006,8 @@ void session_run(hbx_session* S, hbx_mode mode, cudaStream_t st) {
     // operations per 32-bit word per character (6 per 64-bit word)
     S->stats.scan_word_ops = c.scan_steps * 4ull * 3ull * S->peq_shape.w;
     S->stats.scan_words = S->peq_shape.w;
+    S->stats.scan_warp_steps = c.scan_warp_steps;
+    S->stats.rest_scans = c.rest_scans;
     S->stats.tile_right = S->tile_right;
     S->stats.n_windows = 1;
     S->stats.eval_variant = (uint32_t)S->variant + 1;

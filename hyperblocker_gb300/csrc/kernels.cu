@@ -754,6 +754,8 @@ __device__ __forceinline__ uint32_t prefix16(const uint4& a, const uint4& b) {
 struct WorkTally {
   unsigned long long ops;
   uint32_t scans, steps;
+  uint32_t wsteps;  // warp-level scan steps (counted by lane 0)
+  uint32_t rest;    // scans of predicates after the first (advance_rule / advance_group)
 };
 
 // Does the left string of length la have a Peq table (PeqShape)?
@@ -915,6 +917,7 @@ __device__ __forceinline__ int advance_rule(const EvalParams& P, uint32_t rule, 
           (int)sig_bound(am->sig[0], am->sig[1], bm->sig[0], bm->sig[1]) < need)
         return 0;
     }
+    ops->rest++;
     return scan_begin<W>(z, peq_table(P, sl, lrow), a, b, bh, la, lb, p, need, thr, ops) ? 2 : 0;
   }
   return 1;
@@ -928,12 +931,34 @@ __device__ __forceinline__ int advance_rule(const EvalParams& P, uint32_t rule, 
 // Each predicate first goes through the filters of the first column: length
 // bound, common prefix, count signatures.
 //
-// *memo names the column (left slot << 16 | right slot) whose scan the lane
-// finished last, with match count memo_m, while the scan state z still holds
-// its lengths and prefix: a later member testing the same column at its own
-// threshold is decided from it without another scan.  Starting a scan ends
-// the memo.
+// A member that needs a scan of a column scans it at the smallest threshold
+// among itself and the live members after it that test the same column, so
+// that one scan serves them all: *memo then names the column (left slot <<
+// 16 | right slot) and memo_m holds its match count (the scan state z still
+// holds the pair's lengths and prefix) or kMemoBelow (the scan stopped below
+// that smallest threshold, so every one of those members fails the column).
+// Each member decides at its own threshold.  Starting a scan ends the memo.
 constexpr uint32_t kNoMemo = 0xffffffffu;
+constexpr uint32_t kMemoBelow = 0xffffffffu;
+
+// Smallest threshold on column (sl, sr) of member mi (threshold thr) and of
+// the live members after it that test that column; NaN (no bound) when one
+// of them has a NaN threshold.
+__device__ __forceinline__ float shared_thr(const Rule* R, uint32_t live, uint32_t mi, uint32_t sl,
+                                            uint32_t sr, float thr) {
+  float t = thr;
+  for (uint32_t x = live & ~((2u << mi) - 1u); x; x &= x - 1) {
+    const Member* M = R->mem + (__ffs(x) - 1);
+    for (uint32_t j = 0; j < M->n_rest; j++)
+      if (M->rest_l[j] == sl && M->rest_r[j] == sr) {
+        const float u = M->rest_thr[j];
+        t = (u != u || t != t) ? __int_as_float(0x7fc00000) : fminf(t, u);
+        break;
+      }
+  }
+  return t;
+}
+
 template <int W>
 __device__ __forceinline__ int advance_group(const EvalParams& P, uint32_t rule, uint32_t* live,
                                              uint32_t* mi, uint32_t* s, uint32_t lrow,
@@ -948,7 +973,8 @@ __device__ __forceinline__ int advance_group(const EvalParams& P, uint32_t rule,
       const uint32_t sl = M->rest_l[k], sr = M->rest_r[k];
       const float thr = M->rest_thr[k];
       if (*memo == (sl << 16 | sr)) {
-        if (!jw_decide(memo_m, z.ls, z.ll, z.p, thr, &P.ctr->ambiguous)) break;
+        if (memo_m == kMemoBelow || !jw_decide(memo_m, z.ls, z.ll, z.p, thr, &P.ctr->ambiguous))
+          break;
         continue;
       }
       const StrMeta* am = P.L.str_meta + (size_t)sl * P.L.n_rows + lrow;
@@ -980,8 +1006,13 @@ __device__ __forceinline__ int advance_group(const EvalParams& P, uint32_t rule,
         if (need > 0 && (int)sig_bound(am->sig[0], am->sig[1], bm->sig[0], bm->sig[1]) < need)
           break;
       }
+      // member *mi may pass: one scan for it and the later members testing
+      // this column, at the smallest of their thresholds
+      const float ts = shared_thr(R, *live, *mi, sl, sr, thr);
+      if (p != kPrefixUnknown && ts != thr) need = m_need_lo(ls, ll, p, ts);
       *memo = kNoMemo;  // z is about to hold another pair's scan
-      if (scan_begin<W>(z, peq_table(P, sl, lrow), a, b, bh, la, lb, p, need, thr, ops)) {
+      ops->rest++;
+      if (scan_begin<W>(z, peq_table(P, sl, lrow), a, b, bh, la, lb, p, need, ts, ops)) {
         *s = k;
         return 2;
       }
@@ -1477,6 +1508,7 @@ __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
       }
     }
     head += min(n_idle, avail);
+    if (lane == 0 && __any_sync(kFull, busy)) ops->wsteps++;
     if (busy) {
       uint32_t m = 0;
       const int sc = scan_step<W>(z, &m, ops);
@@ -1504,12 +1536,13 @@ __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
             st = advance_group<W>(P, rule, &live, &mi, &s, lrow, rrow, z, &memo, memo_m, ops);
           }
         } else {
-          // a complete scan is remembered for the other members' tests of
-          // the same column; a scan stopped early is not (its count is partial)
+          // the scan ran at the smallest threshold of the members testing
+          // this column (advance_group): remembered for them, and member mi
+          // decides at its own threshold
           const Member* M = P.rules[rule].mem + mi;
-          memo = sc == 1 ? (M->rest_l[s] << 16 | M->rest_r[s]) : kNoMemo;
-          memo_m = m;
-          if (sc == 1 && jw_decide(m, z.ls, z.ll, z.p, z.thr, &P.ctr->ambiguous)) {
+          memo = M->rest_l[s] << 16 | M->rest_r[s];
+          memo_m = sc == 1 ? m : kMemoBelow;
+          if (sc == 1 && jw_decide(m, z.ls, z.ll, z.p, M->rest_thr[s], &P.ctr->ambiguous)) {
             s++;  // member mi passed predicate s
           } else {
             live &= ~(1u << mi);
@@ -1552,7 +1585,7 @@ __device__ __forceinline__ void eval_body(const EvalParams& P) {
     for (uint32_t k = 0; k < P.n_seg; k++) n_work += P.seg_end[k] - P.seg_begin[k];
   }
   unsigned long long done = 0;
-  WorkTally tally{0ull, 0u, 0u};
+  WorkTally tally{0ull, 0u, 0u, 0u, 0u};
   switch (P.peq_w) {
     case 1: eval_loop<1, G>(P, region, n_work, &tally, &done); break;
     case 2: eval_loop<2, G>(P, region, n_work, &tally, &done); break;
@@ -1561,17 +1594,20 @@ __device__ __forceinline__ void eval_body(const EvalParams& P) {
     default: eval_loop<8, G>(P, region, n_work, &tally, &done); break;
   }
   if (lane == 0 && done) atomicAdd(&P.ctr->items_done, done);
-  unsigned long long ops = tally.ops, scans = tally.scans, steps = tally.steps;
+  unsigned long long ops = tally.ops, scans = tally.scans, steps = tally.steps, rest = tally.rest;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     ops += __shfl_down_sync(kFull, ops, o);
     scans += __shfl_down_sync(kFull, scans, o);
     steps += __shfl_down_sync(kFull, steps, o);
+    rest += __shfl_down_sync(kFull, rest, o);
   }
   if (lane == 0) {
     if (ops) atomicAdd(&P.ctr->jw_word_ops, ops);
     if (scans) atomicAdd(&P.ctr->scans, scans);
     if (steps) atomicAdd(&P.ctr->scan_steps, steps);
+    if (rest) atomicAdd(&P.ctr->rest_scans, rest);
+    if (tally.wsteps) atomicAdd(&P.ctr->scan_warp_steps, (unsigned long long)tally.wsteps);
   }
 }
 

@@ -265,6 +265,8 @@ struct Counters {
   unsigned long long scans;       // pairs that reached a bit-parallel scan
   unsigned long long scan_steps;  // scan steps of 4 symbols
   unsigned long long items_total; // work items of the run (written by the join)
+  unsigned long long scan_warp_steps;  // warp-level scan steps (any lane scanning)
+  unsigned long long rest_scans;       // scans of predicates after a rule's or group's first
 };
 
 struct EvalParams {

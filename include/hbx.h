@@ -127,6 +127,10 @@ typedef struct hbx_stats {
                                  64-bit mask word per character scanned) */
   uint32_t scan_words;        /* 32-bit words per scan mask in the last run (1, 2, 3, 4 or 8) */
   uint32_t reserved0;
+  uint64_t scan_warp_steps;   /* warp-level scan steps: scan_steps / (4 x 32 x this) is the
+                                 share of lanes busy in the scan loop */
+  uint64_t rest_scans;        /* of pairs_scanned, scans of predicates after a rule's (or rule
+                                 group's) first similarity predicate */
 } hbx_stats;
 
 /* ---- context ------------------------------------------------------------ */
