@@ -482,9 +482,11 @@ def bench_c5(args, ctx, dev):
             "matches": int(s1.n_matches), "same_pairs": bool(same),
             "long_string_pairs": int(s1.long_string_pairs),
             "one_shot": {"value": s1.pair_comparisons / t_one, "wall_ms": 1000 * t_one,
-                         "ms_eval": s1.ms_eval, "ms_create": s1.ms_create},
+                         "ms_eval": s1.ms_eval, "ms_create": s1.ms_create,
+                         "tile_right": int(s1.tile_right), "eval_variant": int(s1.eval_variant)},
             "streamed": {"value": s2.pair_comparisons / t_st, "wall_ms": 1000 * t_st,
                          "windows": int(s2.n_windows), "window_mib": args.c5_window_mb,
+                         "tile_right": int(s2.tile_right), "eval_variant": int(s2.eval_variant),
                          "ms_eval_summed": s2.ms_eval, "ms_create_summed": s2.ms_create},
             "streamed_vs_one_shot": t_st / t_one,
             "parity": {"sampled_left_rows": n_rows, "per_partition": args.c5_sample_per_part,

@@ -1508,7 +1508,9 @@ __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
       }
     }
     head += min(n_idle, avail);
-    if (lane == 0 && __any_sync(kFull, busy)) ops->wsteps++;
+    // every lane votes (a warp vote must be reached by all lanes of its mask)
+    const bool any_busy = __any_sync(kFull, busy);
+    if (lane == 0 && any_busy) ops->wsteps++;
     if (busy) {
       uint32_t m = 0;
       const int sc = scan_step<W>(z, &m, ops);

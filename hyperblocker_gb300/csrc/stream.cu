@@ -78,7 +78,6 @@ extern "C" hbx_status hbx_block_streamed(hbx_ctx* ctx, const hbx_plan* plan, con
   if (!ctx || !plan || !left || !right || !out || window_bytes == 0) return HBX_ERR_INVALID_ARG;
   if (mode != HBX_MODE_PLAIN && mode != HBX_MODE_BATCHED) return HBX_ERR_INVALID_ARG;
   const auto t0 = std::chrono::steady_clock::now();
-  std::vector<uint32_t> res_l, res_r;
   hbx_stats agg{};
   try {
     if (prefix_idx != INT_MAX && (prefix_idx < 0 || prefix_idx > INT_MAX))
@@ -199,6 +198,7 @@ extern "C" hbx_status hbx_block_streamed(hbx_ctx* ctx, const hbx_plan* plan, con
       eval_ctas = std::max(1, ctx->n_sm * 2 - std::max(2, ctx->n_sm / 4));
     }
     std::atomic<size_t> next{0};
+    std::vector<std::vector<uint32_t>> win_l(windows.size()), win_r(windows.size());
     std::mutex mu;
     // matches per pair covered in the windows done so far: sizes the next
     // windows' output so that their runs do not overflow and repeat
@@ -276,6 +276,18 @@ extern "C" hbx_status hbx_block_streamed(hbx_ctx* ctx, const hbx_plan* plan, con
           }
         }
         if (s) hbx_session_destroy(s);
+        if (st == HBX_OK) {
+          // the window's rows back to table rows, outside the lock: each
+          // window has its own result vectors, joined once at the end
+          std::vector<uint32_t>& wl = win_l[k];
+          std::vector<uint32_t>& wr = win_r[k];
+          wl.resize(l.size());
+          wr.resize(r.size());
+          for (size_t i = 0; i < l.size(); i++) {
+            wl[i] = il[l[i]];
+            wr[i] = ir[r[i]];
+          }
+        }
         std::lock_guard<std::mutex> lock(mu);
         if (st != HBX_OK) {
           if (err == HBX_OK) {
@@ -283,10 +295,6 @@ extern "C" hbx_status hbx_block_streamed(hbx_ctx* ctx, const hbx_plan* plan, con
             err_text = hbx_last_error(wc);
           }
           break;
-        }
-        for (size_t i = 0; i < l.size(); i++) {
-          res_l.push_back(il[l[i]]);
-          res_r.push_back(ir[r[i]]);
         }
         if (ws.pairs_covered)
           density = std::max(density, (double)l.size() / (double)ws.pairs_covered);
@@ -323,6 +331,21 @@ extern "C" hbx_status hbx_block_streamed(hbx_ctx* ctx, const hbx_plan* plan, con
       if (a && b) agg.n_partitions_used++;
     }
     agg.n_windows = (uint32_t)windows.size();
+    size_t total = 0;
+    for (auto& v : win_l) total += v.size();
+    agg.n_matches = total;
+    out->n_required = total;
+    out->n_written = 0;
+    if (total > out->capacity) fail(HBX_ERR_CAPACITY, "output capacity below the match count");
+    if (total && (!out->l_row || !out->r_row)) fail(HBX_ERR_INVALID_ARG, "null output pointer");
+    size_t pos = 0;
+    for (size_t k = 0; k < windows.size(); k++) {
+      if (win_l[k].empty()) continue;
+      std::memcpy(out->l_row + pos, win_l[k].data(), win_l[k].size() * 4);
+      std::memcpy(out->r_row + pos, win_r[k].data(), win_r[k].size() * 4);
+      pos += win_l[k].size();
+    }
+    out->n_written = total;
   } catch (const Error& e) {
     ctx->err = e.what();
     return e.status;
@@ -330,22 +353,9 @@ extern "C" hbx_status hbx_block_streamed(hbx_ctx* ctx, const hbx_plan* plan, con
     ctx->err = "host out of memory";
     return HBX_ERR_OOM;
   }
-  agg.n_matches = res_l.size();
   agg.ms_last_run =
       std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   if (stats) *stats = agg;
-  out->n_required = res_l.size();
-  out->n_written = 0;
-  if (res_l.size() > out->capacity) {
-    ctx->err = "output capacity below the match count";
-    return HBX_ERR_CAPACITY;
-  }
-  if (!res_l.empty()) {
-    if (!out->l_row || !out->r_row) return HBX_ERR_INVALID_ARG;
-    std::memcpy(out->l_row, res_l.data(), res_l.size() * 4);
-    std::memcpy(out->r_row, res_r.data(), res_r.size() * 4);
-  }
-  out->n_written = res_l.size();
   ctx->err.clear();
   return HBX_OK;
 }
