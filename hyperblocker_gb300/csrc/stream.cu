@@ -257,13 +257,16 @@ extern "C" hbx_status hbx_block_streamed(hbx_ctx* ctx, const hbx_plan* plan, con
               std::lock_guard<std::mutex> lock(mu);
               d = density;
             }
-            if (d >= 0) {
-              hbx_stats pre{};
-              hbx_session_stats(s, &pre);
-              const double want = 1.5 * d * (double)pre.pairs_covered + 4096.0;
-              const uint64_t cap = std::max<uint64_t>(window_bytes / 8, 1 << 16);
-              reserve_output(s, (uint64_t)std::min<double>(want, (double)cap));
-            }
+            // output slots before the run, so that it does not overflow and
+            // evaluate the window again: from the match density of the
+            // windows done so far, or, for the first windows, as many as the
+            // window's pairs can give, up to window_bytes / 8 slots
+            hbx_stats pre{};
+            hbx_session_stats(s, &pre);
+            const uint64_t cap = std::max<uint64_t>(window_bytes / 8, 1 << 16);
+            const double want =
+                d >= 0 ? 1.5 * d * (double)pre.pairs_covered + 4096.0 : (double)pre.pairs_covered + 1.0;
+            reserve_output(s, (uint64_t)std::min<double>(want, (double)cap));
             // leave an eighth of the CTA slots to the other worker, so that
             // its window's copies, encoding and join run beside this
             // window's persistent evaluation instead of after it

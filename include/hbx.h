@@ -212,7 +212,9 @@ hbx_status hbx_write_pairs_device(hbx_ctx* ctx, const hbx_table* left, const hbx
  * bound): partitions are grouped into windows of at most window_bytes of
  * device memory (a partition larger than that is split by its left rows), and
  * two workers with their own streams process windows in turn, so one
- * window's copies and encoding overlap another's evaluation.  Same pairs as
+ * window's copies and encoding overlap another's evaluation.  A window's
+ * pair output (up to window_bytes / 8 pairs, more if it needs them) comes on
+ * top of the budget.  Same pairs as
  * hbx_block (in another order); stats->n_windows counts the windows and
  * ms_last_run is the wall time of the call.  out holds HOST pointers. */
 hbx_status hbx_block_streamed(hbx_ctx* ctx, const hbx_plan* plan, const hbx_table* left,
