@@ -11,6 +11,7 @@ struct hbx_ctx {
   int device = 0;
   int n_sm = 0;
   size_t smem_optin = 0;
+  size_t smem_per_sm = 0;  // shared memory of one SM (all resident blocks)
   cudaStream_t stream = nullptr;
   cudaMemPool_t pool = nullptr;  // device memory of this context's sessions and servers
   hbx_opts opts{};

@@ -151,9 +151,11 @@ void configure(hbx_session* S, uint32_t tile_right, int variant) {
   S->variant = variant ? 1 : 0;
   const dev::EvalKernel kern = dev::eval_kernel(S->variant);
   const dev::EvalKernel kern_g = dev::eval_kernel(S->variant, true);
-  const size_t smem_cap = std::min<size_t>(C->smem_optin, 200 * 1024);
-  const uint32_t cap_warp_words = (uint32_t)(smem_cap / 4 / dev::kWarpsPerCta) / 4 * 4;
-  S->wl = dev::warp_layout_fit(S->tile_right, smem_cap);
+  // two blocks per SM: the SM's shared memory less 1 KB the hardware keeps
+  // per block
+  const size_t smem_cap = std::min<size_t>(C->smem_optin * 2, C->smem_per_sm - 2048);
+  const uint32_t cap_warp_words = (uint32_t)(C->smem_optin / 4 / dev::kWarpsPerCta) / 4 * 4;
+  S->wl = dev::warp_layout_fit(S->tile_right, smem_cap, S->peq_shape.tab_words);
   S->warp_words = S->wl.warp_words;
   if (S->warp_words > cap_warp_words) fail(HBX_ERR_INVALID_ARG, "tile_right too large");
   // every warp region lies inside the dynamic allocation
@@ -312,17 +314,19 @@ void setup_session(hbx_session* S, uint64_t h2d_tables) {
   // one page-locked counter block per context: its sessions run one at a time
   if (!C->h_ctr) HBX_CUDA(cudaHostAlloc(&C->h_ctr, sizeof(dev::Counters), cudaHostAllocPortable));
   S->h_ctr = static_cast<dev::Counters*>(C->h_ctr);
-  const uint32_t tile = C->opts.tile_right > 0 ? (uint32_t)C->opts.tile_right : 128u;
-  const int variant = C->opts.eval_variant > 0 ? C->opts.eval_variant - 1 : 1;
-  configure(S, tile, variant);
-
   // Peq tables of every left string slot, shaped for the longest left
-  // string any similarity predicate reads
+  // string any similarity predicate reads (the shape sizes the warps' table
+  // slots, so it comes before the layout)
   {
     uint32_t mx = 1;
     for (const RuleEnc& re : E.rules)
       for (int sl : re.sim_slot_l) mx = std::max(mx, E.L.str_maxlen[(size_t)sl]);
     S->peq_shape = dev::peq_shape(mx, E.n_symbols);
+  }
+  const uint32_t tile = C->opts.tile_right > 0 ? (uint32_t)C->opts.tile_right : 128u;
+  const int variant = C->opts.eval_variant > 0 ? C->opts.eval_variant - 1 : 1;
+  configure(S, tile, variant);
+  {
     const uint32_t n_slots = (uint32_t)E.L.str_maxlen.size();
     const size_t words = (size_t)n_slots * nL * S->peq_shape.tab_words;
     S->peq.alloc(std::max<size_t>(words, 4));
@@ -774,7 +778,7 @@ std::string autotune_path() {
 
 std::string workload_signature(const hbx_session* S) {
   std::string sig = S->ctx->device_name;
-  sig += "|k3";  // evaluation kernel generation: entries of earlier kernels do not apply
+  sig += "|k4";  // evaluation kernel generation: entries of earlier kernels do not apply
   auto bucket = [](uint64_t n) {  // power-of-two bucket
     uint32_t b = 0;
     while ((1ull << b) < n) b++;
@@ -877,7 +881,7 @@ void autotune(hbx_session* S, cudaStream_t st) {
       return;
     }
   }
-  std::vector<uint32_t> tiles = {32, 64, 128};
+  std::vector<uint32_t> tiles = {32, 64, 96, 128};
   std::vector<int> variants = {0, 1};
   if (o.tile_right > 0) tiles = {(uint32_t)o.tile_right};
   if (o.eval_variant > 0) variants = {o.eval_variant - 1};
@@ -1008,6 +1012,7 @@ void session_run(hbx_session* S, hbx_mode mode, cudaStream_t st) {
     S->stats.scan_words = S->peq_shape.w;
     S->stats.scan_warp_steps = c.scan_warp_steps;
     S->stats.rest_scans = c.rest_scans;
+    S->stats.smem_table_scans = c.smem_table_scans;
     S->stats.tile_right = S->tile_right;
     S->stats.n_windows = 1;
     S->stats.eval_variant = (uint32_t)S->variant + 1;
@@ -1118,6 +1123,7 @@ hbx_status hbx_ctx_create(int device, const hbx_opts* opts, hbx_ctx** out) {
     HBX_CUDA(cudaGetDeviceProperties(&prop, device));
     ctx->n_sm = prop.multiProcessorCount;
     ctx->smem_optin = prop.sharedMemPerBlockOptin;
+    ctx->smem_per_sm = prop.sharedMemPerMultiprocessor;
     ctx->device_name = prop.name;
     HBX_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
     cudaMemPoolProps props{};

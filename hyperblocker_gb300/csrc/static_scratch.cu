@@ -432,6 +432,7 @@ void run_static(int device, const hbx_plan* plan, const hbx_table* left, const h
     stats->scan_words = Y.shape.w;
     stats->scan_warp_steps = c.scan_warp_steps;
     stats->rest_scans = c.rest_scans;
+    stats->smem_table_scans = c.smem_table_scans;
     stats->h2d_bytes = h2d;  // bytes copied to the device by this call
     stats->n_windows = 1;
   }
