@@ -279,7 +279,6 @@ class C3:
                 rec["scan_ops"].append(st.scan_word_ops)
                 rec["scanned"].append(st.pairs_scanned)
                 rec.setdefault("rest", []).append(st.rest_scans)
-                rec.setdefault("smem", []).append(st.smem_table_scans)
                 rec.setdefault("lane_util", []).append(
                     st.scan_steps / (128.0 * st.scan_warp_steps) if st.scan_warp_steps else None)
                 rec["cmp"].append(st.pair_comparisons)
@@ -807,7 +806,6 @@ def run_engine(args, rank, world, local_rank):
             "pairs_scanned_per_launch": int(statistics.mean(bat["scanned"])),
             "pairs_scanned_per_launch_plain": int(statistics.mean(pla["scanned"])),
             "rest_scans_per_launch": int(statistics.mean(bat["rest"])),
-            "smem_table_scans_per_launch": int(statistics.mean(bat["smem"])),
             "rest_scans_per_launch_plain": int(statistics.mean(pla["rest"])),
             "scan_lane_utilisation": bat["lane_util"][-1],
             "scan_lane_utilisation_plain": pla["lane_util"][-1],

@@ -79,7 +79,7 @@ class Stats(ctypes.Structure):
                 ("pairs_scanned", ctypes.c_uint64), ("scan_steps", ctypes.c_uint64),
                 ("scan_word_ops", ctypes.c_uint64), ("scan_words", ctypes.c_uint32),
                 ("reserved0", ctypes.c_uint32), ("scan_warp_steps", ctypes.c_uint64),
-                ("rest_scans", ctypes.c_uint64), ("smem_table_scans", ctypes.c_uint64)]
+                ("rest_scans", ctypes.c_uint64)]
 
     def as_dict(self) -> Dict[str, float]:
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -149,13 +149,11 @@ void configure(hbx_session* S, uint32_t tile_right, int variant) {
   hbx_ctx* C = S->ctx;
   S->tile_right = std::min<uint32_t>(512, std::max<uint32_t>(32, (tile_right + 31) / 32 * 32));
   S->variant = variant ? 1 : 0;
-  const dev::EvalKernel kern = dev::eval_kernel(S->variant);
-  const dev::EvalKernel kern_g = dev::eval_kernel(S->variant, true);
   // two blocks per SM: the SM's shared memory less 1 KB the hardware keeps
   // per block
   const size_t smem_cap = std::min<size_t>(C->smem_optin * 2, C->smem_per_sm - 2048);
   const uint32_t cap_warp_words = (uint32_t)(C->smem_optin / 4 / dev::kWarpsPerCta) / 4 * 4;
-  S->wl = dev::warp_layout_fit(S->tile_right, smem_cap, S->peq_shape.tab_words);
+  S->wl = dev::warp_layout_fit(S->tile_right, smem_cap);
   S->warp_words = S->wl.warp_words;
   if (S->warp_words > cap_warp_words) fail(HBX_ERR_INVALID_ARG, "tile_right too large");
   // every warp region lies inside the dynamic allocation
@@ -165,10 +163,10 @@ void configure(hbx_session* S, uint32_t tile_right, int variant) {
   HBX_CUDA(cudaMemcpyAsync(S->d_groups.p, S->h_groups.data(), S->h_groups.size() * sizeof(dev::Rule),
                            cudaMemcpyHostToDevice, C->stream));
   HBX_CUDA(cudaStreamSynchronize(C->stream));
-  raise_smem_limit(kern, S->smem_bytes);
-  raise_smem_limit(kern_g, S->smem_bytes);
+  for (bool g : {false, true}) raise_smem_limit(dev::eval_kernel(S->variant, g, S->peq_shape.w), S->smem_bytes);
   int bps = 0;
-  HBX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, kThreads, S->smem_bytes));
+  HBX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &bps, dev::eval_kernel(S->variant, S->groups, S->peq_shape.w), kThreads, S->smem_bytes));
   S->blocks_per_sm = std::max(1, bps);
   if (S->graph) {
     cudaGraphExecDestroy(S->graph);
@@ -315,8 +313,8 @@ void setup_session(hbx_session* S, uint64_t h2d_tables) {
   if (!C->h_ctr) HBX_CUDA(cudaHostAlloc(&C->h_ctr, sizeof(dev::Counters), cudaHostAllocPortable));
   S->h_ctr = static_cast<dev::Counters*>(C->h_ctr);
   // Peq tables of every left string slot, shaped for the longest left
-  // string any similarity predicate reads (the shape sizes the warps' table
-  // slots, so it comes before the layout)
+  // string any similarity predicate reads (the shape picks the evaluation
+  // kernel, so it comes before the configuration)
   {
     uint32_t mx = 1;
     for (const RuleEnc& re : E.rules)
@@ -627,7 +625,7 @@ uint32_t enqueue_batched(hbx_session* S, cudaStream_t st) {
   int grid = S->ctx->n_sm * S->blocks_per_sm;
   if (S->max_eval_ctas > 0) grid = std::min(grid, S->max_eval_ctas);
   HBX_CUDA(cudaEventRecordWithFlags(S->ev_eval0, st, rec_flags));
-  dev::eval_kernel(S->variant, S->groups)<<<grid, kThreads, S->smem_bytes, st>>>(P);
+  dev::eval_kernel(S->variant, S->groups, S->peq_shape.w)<<<grid, kThreads, S->smem_bytes, st>>>(P);
   launch_check("k_eval");
   HBX_CUDA(cudaEventRecordWithFlags(S->ev_eval1, st, rec_flags));
   // the counters travel back inside the run (graph nodes when captured)
@@ -747,7 +745,7 @@ dev::Counters run_once(hbx_session* S, hbx_mode mode, cudaStream_t st, uint32_t*
       HBX_CUDA(cudaMemsetAsync(&S->d_ctr.p->work_next, 0, sizeof(unsigned long long), st));
       const unsigned long long ctas = (n_items + dev::kWarpsPerCta - 1) / dev::kWarpsPerCta;
       const int grid = (int)std::min<unsigned long long>(ctas, (unsigned long long)max_grid);
-      dev::eval_kernel(S->variant)<<<grid, kThreads, S->smem_bytes, st>>>(P);
+      dev::eval_kernel(S->variant, false, S->peq_shape.w)<<<grid, kThreads, S->smem_bytes, st>>>(P);
       n++;
       launch_check("k_eval (plain)");
     }
@@ -1012,7 +1010,6 @@ void session_run(hbx_session* S, hbx_mode mode, cudaStream_t st) {
     S->stats.scan_words = S->peq_shape.w;
     S->stats.scan_warp_steps = c.scan_warp_steps;
     S->stats.rest_scans = c.rest_scans;
-    S->stats.smem_table_scans = c.smem_table_scans;
     S->stats.tile_right = S->tile_right;
     S->stats.n_windows = 1;
     S->stats.eval_variant = (uint32_t)S->variant + 1;

@@ -409,8 +409,8 @@ __global__ void k_reset(Counters* ctr, uint32_t* counts, uint64_t n_counts,
 // Jaro-Winkler
 // =====================================================================
 
-// One symbol row of a Peq table, in a warp's shared-memory slot or in device
-// memory (generic loads: the table pointer may point to either).
+// One symbol row of a Peq table in device memory (plain loads: they need
+// fewer registers around the scan than the read-only path's).
 template <int S>
 __device__ __forceinline__ void load_row(const uint32_t* row, uint32_t (&pe)[S]) {
   if constexpr (S == 1) {
@@ -757,7 +757,6 @@ struct WorkTally {
   uint32_t scans, steps;
   uint32_t wsteps;  // warp-level scan steps (counted by lane 0)
   uint32_t rest;    // scans of predicates after the first (advance_rule / advance_group)
-  uint32_t smem;    // scans whose Peq table was in a shared-memory slot
 };
 
 // Does the left string of length la have a Peq table (PeqShape)?
@@ -1062,10 +1061,6 @@ struct WarpCtl {
   uint32_t i_rule, i_lrow, i_kind, i_fast, i_all;
   float i_thr;
   int32_t i_lcode[kMaxEq];
-  // Peq table slots (EvalParams::tab_off): the (left string slot, left row)
-  // whose table each holds (tab_lrow ~0: none), and the slot the next item
-  // takes
-  uint32_t tab_lrow[kTabSlots], tab_sl[kTabSlots], tab_next;
 };
 static_assert(sizeof(WarpCtl) <= kWarpCtlWords * 4, "warp control block outgrows its words");
 
@@ -1394,10 +1389,6 @@ __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
       (uint32_t)max(1ull, min((unsigned long long)kMaxClaimChunk, n_work / (n_warps * 8ull)));
   bool stop = false;
   uint32_t d_pos = 0, d_n = 0;  // the warp's claimed descriptors not yet taken
-  uint32_t* const tab_slots = region + P.tab_off;  // kTabSlots x P.tab_slot_words
-  if (lane < (int)kTabSlots) C->tab_lrow[lane] = ~0u;
-  if (lane == 0) C->tab_next = 0;
-  __syncwarp();
   for (uint32_t b = 0; b < P.n_bufs; b++)
     claim_item(P, C, b, region + P.buf_off + b * P.buf_words, bar0 + b, n_work, chunk, t_start,
                &stop, &d_pos, &d_n, done);
@@ -1475,29 +1466,6 @@ __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
           C->i_lcode[lane] = P.L.eq_codes[(size_t)R->xslot[lane] * P.L.n_rows + il];
       }
       __syncwarp();
-      if (P.tab_slot_words && has_table(P, la)) {
-        // the item's first-column Peq table into the next slot, unless a
-        // lane is still scanning with that slot's table (then this item's
-        // scans read device memory); scans of the slot's former item that
-        // start later find it gone and read device memory too
-        const uint32_t ts = C->tab_next;
-        uint32_t* slot = tab_slots + ts * P.tab_slot_words;
-        const bool in_use = __any_sync(kFull, busy && z.tab == slot);
-        if (!in_use) {
-          const uint32_t sl0 = P.rules[ir].sim_l[0];
-          if (lane == 0) C->tab_lrow[ts] = ~0u;
-          const uint4* src = reinterpret_cast<const uint4*>(peq_table(P, sl0, il));
-          uint4* dst = reinterpret_cast<uint4*>(slot);
-          for (uint32_t w = (uint32_t)lane; w < P.tab_words / 4; w += 32) dst[w] = __ldg(src + w);
-          __syncwarp();
-          if (lane == 0) {
-            C->tab_lrow[ts] = il;
-            C->tab_sl[ts] = sl0;
-            C->tab_next = ts + 1 == kTabSlots ? 0 : ts + 1;
-          }
-          __syncwarp();
-        }
-      }
     }
     // idle lanes take the next queued pairs
     bool fin = false, pass = false;
@@ -1527,23 +1495,11 @@ __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
         s = 0;
         const Rule* R = P.rules + rule;
         const uint32_t p = (e0.w >> 10) & 31u;
-        const uint32_t sl0 = R->sim_l[0];
-        const uint32_t* tab = peq_table(P, sl0, lrow);
-        bool in_slot = false;
-        if (P.tab_slot_words) {
-#pragma unroll
-          for (uint32_t t = 0; t < kTabSlots; t++)
-            if (C->tab_lrow[t] == lrow && C->tab_sl[t] == sl0) {
-              tab = tab_slots + t * P.tab_slot_words;
-              in_slot = true;
-            }
-        }
-        st = scan_begin<W>(z, tab, P.L.arena + 16ull * e2.z,
+        st = scan_begin<W>(z, peq_table(P, R->sim_l[0], lrow), P.L.arena + 16ull * e2.z,
                            P.R.arena + 16ull * e0.y, en[1], e2.y, e0.z, p, (int)(e0.w & 1023u),
                            G ? live_thr(R, live) : R->thr[0], ops)
                  ? 2
                  : 0;
-        if (st == 2 && in_slot) ops->smem++;
       }
       if (st == 2) {
         busy = true;
@@ -1612,9 +1568,11 @@ __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
   }
 }
 
-// The evaluation kernel body, instantiated twice below with different
-// register budgets (see k_eval / k_eval_wide).
-template <bool G>
+// The evaluation kernel body for masks of W words, instantiated below with
+// two register budgets (k_eval / k_eval_wide) and for rule groups.  One
+// kernel per mask width: a kernel holding every width's scan loop is
+// register-allocated for the widest and spills in the narrow ones too.
+template <int W, bool G>
 __device__ __forceinline__ void eval_body(const EvalParams& P) {
   extern __shared__ __align__(16) uint32_t smem[];
   const int lane = threadIdx.x & 31;
@@ -1632,31 +1590,22 @@ __device__ __forceinline__ void eval_body(const EvalParams& P) {
     for (uint32_t k = 0; k < P.n_seg; k++) n_work += P.seg_end[k] - P.seg_begin[k];
   }
   unsigned long long done = 0;
-  WorkTally tally{0ull, 0u, 0u, 0u, 0u, 0u};
-  switch (P.peq_w) {
-    case 1: eval_loop<1, G>(P, region, n_work, &tally, &done); break;
-    case 2: eval_loop<2, G>(P, region, n_work, &tally, &done); break;
-    case 3: eval_loop<3, G>(P, region, n_work, &tally, &done); break;
-    case 4: eval_loop<4, G>(P, region, n_work, &tally, &done); break;
-    default: eval_loop<8, G>(P, region, n_work, &tally, &done); break;
-  }
+  WorkTally tally{0ull, 0u, 0u, 0u, 0u};
+  eval_loop<W, G>(P, region, n_work, &tally, &done);
   if (lane == 0 && done) atomicAdd(&P.ctr->items_done, done);
-  unsigned long long ops = tally.ops, scans = tally.scans, steps = tally.steps, rest = tally.rest,
-                     in_slot = tally.smem;
+  unsigned long long ops = tally.ops, scans = tally.scans, steps = tally.steps, rest = tally.rest;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     ops += __shfl_down_sync(kFull, ops, o);
     scans += __shfl_down_sync(kFull, scans, o);
     steps += __shfl_down_sync(kFull, steps, o);
     rest += __shfl_down_sync(kFull, rest, o);
-    in_slot += __shfl_down_sync(kFull, in_slot, o);
   }
   if (lane == 0) {
     if (ops) atomicAdd(&P.ctr->jw_word_ops, ops);
     if (scans) atomicAdd(&P.ctr->scans, scans);
     if (steps) atomicAdd(&P.ctr->scan_steps, steps);
     if (rest) atomicAdd(&P.ctr->rest_scans, rest);
-    if (in_slot) atomicAdd(&P.ctr->smem_table_scans, in_slot);
     if (tally.wsteps) atomicAdd(&P.ctr->scan_warp_steps, (unsigned long long)tally.wsteps);
   }
 }
@@ -1691,20 +1640,44 @@ __global__ void k_peq_build(Side L, uint32_t n_slots, PeqShape shape, uint32_t* 
 }
 
 // Dense variant: 3 CTAs (24 warps) per SM, at most 85 registers per thread.
-__global__ void __launch_bounds__(kWarpsPerCta * 32, 3) k_eval(EvalParams P) { eval_body<false>(P); }
+template <int W>
+__global__ void __launch_bounds__(kWarpsPerCta * 32, 3) k_eval(EvalParams P) {
+  eval_body<W, false>(P);
+}
 
 // Wide variant: 2 CTAs (16 warps) per SM, up to 128 registers per thread, so
 // the longer-string scan variants keep their state in registers.
+template <int W>
 __global__ void __launch_bounds__(kWarpsPerCta * 32, 2) k_eval_wide(EvalParams P) {
-  eval_body<false>(P);
+  eval_body<W, false>(P);
 }
 
 // The same two over rule groups (Rule: "Group evaluation").
+template <int W>
 __global__ void __launch_bounds__(kWarpsPerCta * 32, 3) k_eval_groups(EvalParams P) {
-  eval_body<true>(P);
+  eval_body<W, true>(P);
 }
+template <int W>
 __global__ void __launch_bounds__(kWarpsPerCta * 32, 2) k_eval_groups_wide(EvalParams P) {
-  eval_body<true>(P);
+  eval_body<W, true>(P);
+}
+
+namespace {
+template <int W>
+EvalKernel pick(int wide, bool groups) {
+  return groups ? (wide ? k_eval_groups_wide<W> : k_eval_groups<W>)
+                : (wide ? k_eval_wide<W> : k_eval<W>);
+}
+}  // namespace
+
+EvalKernel eval_kernel(int wide, bool groups, uint32_t peq_w) {
+  switch (peq_w) {
+    case 1: return pick<1>(wide, groups);
+    case 2: return pick<2>(wide, groups);
+    case 3: return pick<3>(wide, groups);
+    case 4: return pick<4>(wide, groups);
+    default: return pick<8>(wide, groups);
+  }
 }
 
 }  // namespace dev

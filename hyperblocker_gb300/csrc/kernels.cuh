@@ -215,19 +215,12 @@ inline PeqShape peq_shape(uint32_t max_len, uint32_t n_symbols) {
 // bytes) when tile_right is a multiple of 32.  A control block of
 // kWarpCtlWords words follows.
 constexpr uint32_t kMaxStageBufs = 4;
-// Peq table slots of a warp: the tables of the first similarity column's
-// left strings of the items it filtered last, in shared memory, so that the
-// scans of their pairs read their rows there (kernels.cu, eval_loop).
-constexpr uint32_t kTabSlots = 2;
-constexpr uint32_t kMaxSlotTabWords = 1024;  // larger tables stay in device memory only
 struct WarpLayout {
   uint32_t n_bufs, buf_off, buf_words, buf_rows_off, buf_lmeta_off, mbar_off, ctl_off, warp_words;
-  uint32_t tab_off, tab_words;  // kTabSlots table slots of tab_words words (0: none)
 };
-constexpr uint32_t kWarpCtlWords = 244;  // the warp's control block (kernels.cu: WarpCtl)
+constexpr uint32_t kWarpCtlWords = 236;  // the warp's control block (kernels.cu: WarpCtl)
 
-// tab_words: words of one Peq table for the shared-memory slots, 0 for none.
-inline WarpLayout warp_layout(uint32_t tile_right, uint32_t n_bufs, uint32_t tab_words = 0) {
+inline WarpLayout warp_layout(uint32_t tile_right, uint32_t n_bufs) {
   WarpLayout w;
   w.n_bufs = n_bufs < 1 ? 1 : (n_bufs > kMaxStageBufs ? kMaxStageBufs : n_bufs);
   const uint32_t meta_words = (uint32_t)(sizeof(StrMeta) / 4) * tile_right;
@@ -236,9 +229,7 @@ inline WarpLayout warp_layout(uint32_t tile_right, uint32_t n_bufs, uint32_t tab
   w.buf_words = w.buf_lmeta_off + (uint32_t)(sizeof(StrMeta) / 4);
   w.buf_off = kRingWords * kRingEntries;
   w.mbar_off = w.buf_off + w.n_bufs * w.buf_words;
-  w.tab_words = tab_words <= kMaxSlotTabWords ? (tab_words + 3) / 4 * 4 : 0;
-  w.tab_off = w.mbar_off + (2 * w.n_bufs + 3) / 4 * 4;
-  w.ctl_off = w.tab_off + kTabSlots * w.tab_words;
+  w.ctl_off = w.mbar_off + (2 * w.n_bufs + 3) / 4 * 4;
   w.warp_words = w.ctl_off + kWarpCtlWords;
   return w;
 }
@@ -246,19 +237,13 @@ inline WarpLayout warp_layout(uint32_t tile_right, uint32_t n_bufs, uint32_t tab
 // The deepest staging (up to kMaxStageBufs buffers) that keeps two blocks of
 // kWarpsPerCta warps on an SM within smem_cap bytes of shared memory; one
 // buffer when none does (with one buffer the next item's copies start once
-// the current item is filtered, and other warps cover their latency).  The
-// Peq table slots are kept when two blocks still fit with one buffer, else
-// left out.
-inline WarpLayout warp_layout_fit(uint32_t tile_right, size_t smem_cap, uint32_t tab_words = 0) {
-  auto fits = [&](const WarpLayout& c) {
-    return (size_t)c.warp_words * 4 * kWarpsPerCta * 2 <= smem_cap;
-  };
+// the current item is filtered, and other warps cover their latency).
+inline WarpLayout warp_layout_fit(uint32_t tile_right, size_t smem_cap) {
   for (uint32_t n = kMaxStageBufs; n > 1; n--) {
-    const WarpLayout c = warp_layout(tile_right, n, tab_words);
-    if (fits(c)) return c;
+    const WarpLayout c = warp_layout(tile_right, n);
+    if ((size_t)c.warp_words * 4 * kWarpsPerCta * 2 <= smem_cap) return c;
   }
-  const WarpLayout one = warp_layout(tile_right, 1, tab_words);
-  return fits(one) ? one : warp_layout(tile_right, 1, 0);
+  return warp_layout(tile_right, 1);
 }
 
 __host__ __device__ inline uint32_t word_class(uint32_t len) {
@@ -281,7 +266,6 @@ struct Counters {
   unsigned long long scan_steps;  // scan steps of 4 symbols
   unsigned long long items_total; // work items of the run (written by the join)
   unsigned long long scan_warp_steps;  // warp-level scan steps (any lane scanning)
-  unsigned long long smem_table_scans; // scans that read their Peq rows from shared memory
   unsigned long long rest_scans;       // scans of predicates after a rule's or group's first
 };
 
@@ -300,7 +284,6 @@ struct EvalParams {
   uint32_t tile_right;  // TR
   // shared-memory words per warp and offsets inside a warp's region (warp_layout)
   uint32_t warp_words, n_bufs, buf_off, buf_words, buf_rows_off, buf_lmeta_off, mbar_off, ctl_off;
-  uint32_t tab_off, tab_slot_words;  // Peq table slots (tab_slot_words == 0: none)
   // Peq tables of the left strings (PeqShape): [left string slot][left row]
   const uint32_t* peq;
   uint32_t peq_w, tab_words, fast_max;
@@ -324,9 +307,6 @@ inline void set_layout(EvalParams* P, const WarpLayout& w, const PeqShape& s, co
   P->buf_lmeta_off = w.buf_lmeta_off;
   P->mbar_off = w.mbar_off;
   P->ctl_off = w.ctl_off;
-  P->tab_off = w.tab_off;
-  // a slot holds one whole table of this launch's shape
-  P->tab_slot_words = (w.tab_words && w.tab_words >= s.tab_words) ? w.tab_words : 0;
   P->peq = peq;
   P->peq_w = s.w;
   P->tab_words = s.tab_words;
@@ -372,16 +352,13 @@ __global__ void k_join_scatter(Side L, Side R, const Rule* rules, uint32_t n_rul
 // ------------------------------------------------------------------ evaluation
 // Peq tables of every left string of n_slots string slots (PeqShape).
 __global__ void k_peq_build(Side L, uint32_t n_slots, PeqShape shape, uint32_t* peq);
-__global__ void k_eval(EvalParams P);       // 3 CTAs per SM (register-limited)
-__global__ void k_eval_wide(EvalParams P);  // 2 CTAs per SM (more registers)
-// the same over rule groups (launches where some rule evaluates others)
-__global__ void k_eval_groups(EvalParams P);
-__global__ void k_eval_groups_wide(EvalParams P);
-
+// The evaluation kernel for masks of peq_w words (PeqShape::w): k_eval<W>
+// (3 CTAs per SM, register-limited) or k_eval_wide<W> (2 CTAs per SM, more
+// registers), or the same two over rule groups (k_eval_groups<W>,
+// k_eval_groups_wide<W>: launches where some rule evaluates others).
 using EvalKernel = void (*)(EvalParams);
-inline EvalKernel eval_kernel(int wide, bool groups = false) {
-  return groups ? (wide ? k_eval_groups_wide : k_eval_groups) : (wide ? k_eval_wide : k_eval);
-}
+EvalKernel eval_kernel(int wide, bool groups, uint32_t peq_w);
+constexpr uint32_t kPeqWidths[] = {1, 2, 3, 4, 8};  // every PeqShape::w
 
 constexpr uint32_t kScanChunk = 4096;  // elements per CTA in the scans (1024 threads x 4)
 

@@ -525,7 +525,6 @@ void open_server(hbx_server* S, const hbx_plan* const* plans, int32_t n_plans, c
   S->tile_right = S->opts.tile_right > 0 ? (uint32_t)S->opts.tile_right : 128u;
   S->tile_right = std::min<uint32_t>(512, std::max<uint32_t>(32, (S->tile_right + 31) / 32 * 32));
   S->variant = S->opts.eval_variant == 1 ? 0 : 1;
-  const dev::EvalKernel kern = dev::eval_kernel(S->variant);
   const size_t smem_cap = std::min<size_t>(C->smem_optin, 200 * 1024);
   const uint32_t cap_warp_words = (uint32_t)(smem_cap / 4 / dev::kWarpsPerCta) / 4 * 4;
   S->wl = dev::warp_layout_fit(S->tile_right, smem_cap);
@@ -586,11 +585,15 @@ void open_server(hbx_server* S, const hbx_plan* const* plans, int32_t n_plans, c
       S->rules.push_back(std::move(T));
     }
   }
-  raise_smem_limit(kern, S->smem_bytes);
-  {
+  // a request batch's longest left string picks the mask width: the grid is
+  // sized by the width with the fewest resident blocks
+  S->blocks_per_sm = 1 << 20;
+  for (uint32_t w : dev::kPeqWidths) {
+    const dev::EvalKernel kern = dev::eval_kernel(S->variant, false, w);
+    raise_smem_limit(kern, S->smem_bytes);
     int bps = 0;
     HBX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, kThreads, S->smem_bytes));
-    S->blocks_per_sm = std::max(1, bps);
+    S->blocks_per_sm = std::max(1, std::min(S->blocks_per_sm, bps));
   }
   HBX_CUDA(cudaStreamSynchronize(st));
 
@@ -836,7 +839,7 @@ void launch_eval(hbx_server* S, Slot& B) {
   P.seen = B.seen.p;
   P.seen_mask = B.seen.p ? B.seen.n - 1 : 0;
   const int grid = S->ctx->n_sm * S->blocks_per_sm;
-  dev::eval_kernel(S->variant)<<<grid, kThreads, S->smem_bytes, st>>>(P);
+  dev::eval_kernel(S->variant, false, B.shape.w)<<<grid, kThreads, S->smem_bytes, st>>>(P);
   check_launch("serving k_eval");
   uint8_t* h = (uint8_t*)B.h_ctr.p;
   HBX_CUDA(cudaMemcpyAsync(h, B.d_ctr.p, sizeof(dev::Counters), cudaMemcpyDeviceToHost, st));

@@ -389,19 +389,18 @@ void run_static(int device, const hbx_plan* plan, const hbx_table* left, const h
   P.seen = Y.seen;
   P.seen_mask = Y.seen ? Y.seen_slots - 1 : 0;
   const size_t smem = (size_t)Y.wl.warp_words * 4 * dev::kWarpsPerCta;
+  const dev::EvalKernel kern = dev::eval_kernel(1, false, Y.shape.w);
   {
     static std::mutex mu;
     std::lock_guard<std::mutex> lock(mu);
     cudaFuncAttributes fa;
-    HBX_STATIC_CUDA(cudaFuncGetAttributes(&fa, dev::k_eval_wide));
+    HBX_STATIC_CUDA(cudaFuncGetAttributes(&fa, kern));
     if ((size_t)fa.maxDynamicSharedSizeBytes < smem)
-      HBX_STATIC_CUDA(cudaFuncSetAttribute(dev::k_eval_wide, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)smem));
+      HBX_STATIC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   }
   int bps = 0;
-  HBX_STATIC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, dev::k_eval_wide,
-                                                                dev::kWarpsPerCta * 32, smem));
-  dev::k_eval_wide<<<n_sm * std::max(1, bps), dev::kWarpsPerCta * 32, smem, st>>>(P);
+  HBX_STATIC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, dev::kWarpsPerCta * 32, smem));
+  kern<<<n_sm * std::max(1, bps), dev::kWarpsPerCta * 32, smem, st>>>(P);
   HBX_STATIC_CUDA(cudaGetLastError());
 
   dev::Counters c{};
@@ -432,7 +431,6 @@ void run_static(int device, const hbx_plan* plan, const hbx_table* left, const h
     stats->scan_words = Y.shape.w;
     stats->scan_warp_steps = c.scan_warp_steps;
     stats->rest_scans = c.rest_scans;
-    stats->smem_table_scans = c.smem_table_scans;
     stats->h2d_bytes = h2d;  // bytes copied to the device by this call
     stats->n_windows = 1;
   }

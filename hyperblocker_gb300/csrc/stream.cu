@@ -319,7 +319,6 @@ extern "C" hbx_status hbx_block_streamed(hbx_ctx* ctx, const hbx_plan* plan, con
         agg.scan_word_ops += ws.scan_word_ops;
         agg.scan_warp_steps += ws.scan_warp_steps;
         agg.rest_scans += ws.rest_scans;
-        agg.smem_table_scans += ws.smem_table_scans;
         agg.scan_words = std::max(agg.scan_words, ws.scan_words);
       }
       hbx_ctx_destroy(wc);

@@ -131,7 +131,6 @@ typedef struct hbx_stats {
                                  share of lanes busy in the scan loop */
   uint64_t rest_scans;        /* of pairs_scanned, scans of predicates after a rule's (or rule
                                  group's) first similarity predicate */
-  uint64_t smem_table_scans;  /* of pairs_scanned, scans whose Peq table was in shared memory */
 } hbx_stats;
 
 /* ---- context ------------------------------------------------------------ */
