@@ -75,7 +75,6 @@ struct hbx_session {
   // key histograms and scatter cursors of every rule, one block: one memset
   hbx::DBuf<uint32_t> counts;
   bool fused_join = false;  // every key domain small: join kernels covering all rules
-  hbx::DBuf<unsigned long long> scan_totals;  // fused join: chunk totals [rule][scan][chunk]
   hbx::DBuf<uint32_t> bound_idx;              // per rule, n_partitions + 1 key indices
   hbx::DBuf<unsigned long long> bound_val;    // item_off at those keys
   hbx::dev::Side side_l{}, side_r{};
@@ -92,7 +91,6 @@ struct hbx_session {
   // caller's buffer, 0 = none) returns its count without growing and rerunning
   uint64_t out_hint = 1 << 16, cap_limit = 0;
   int blocks_per_sm = 1;
-  int max_eval_ctas = 0;  // cap on the evaluation grid (set_eval_ctas), 0 = none
   size_t smem_bytes = 0;
   cudaGraphExec_t graph = nullptr;
   // the caller's device output (hbx_session_run), written by the kernels
@@ -296,10 +294,6 @@ void setup_session(hbx_session* S, uint64_t h2d_tables) {
       pos += 2ull * d.domain_l + 2ull * d.domain;
       if (d.domain_l > dev::kFusedJoinMaxDomain) S->fused_join = false;
     }
-    uint32_t max_d = 1;
-    for (const dev::Rule& d : S->h_rules) max_d = std::max(max_d, d.domain_l);
-    const uint32_t nb = (max_d + dev::kScanChunk - 1) / dev::kScanChunk;
-    if (S->fused_join) S->scan_totals.alloc((size_t)S->h_rules.size() * 3 * nb);
   }
   S->h_groups = group_rules(S->h_rules);
   S->groups = false;
@@ -522,20 +516,11 @@ uint32_t enqueue_join(hbx_session* S, cudaStream_t st, const dev::Rule* rules) {
     const uint32_t nb = (max_d + dev::kScanChunk - 1) / dev::kScanChunk;
     unsigned long long* comparisons = &S->d_ctr.p->comparisons;
     dev::k_join_count<<<grid, 256, smem, st>>>(S->side_l, S->side_r, rules);
-    const bool two_pass = nb > dev::kJoinScanLoopChunks;
-    if (two_pass) {
-      dev::k_join_scan_totals<<<dim3(nb, 3, n_rules), 1024, 0, st>>>(
-          rules, S->tile_right, nb, S->scan_totals.p, comparisons);
-      dev::k_join_scan_final<<<dim3(nb, 3, n_rules), 1024, 0, st>>>(
-          rules, S->tile_right, nb, S->scan_totals.p, nullptr);
-    } else {  // one block per (y, rule) walks the chunks
-      dev::k_join_scan_final<<<dim3(1, 3, n_rules), 1024, 0, st>>>(rules, S->tile_right, nb,
-                                                                   nullptr, comparisons);
-    }
+    dev::k_join_scan<<<dim3(nb, 3, n_rules), 1024, 0, st>>>(rules, S->tile_right, comparisons);
     dev::k_join_scatter<<<grid, 256, 0, st>>>(S->side_l, S->side_r, rules, n_rules,
                                                S->d_rule_base.p, &S->d_ctr.p->items_total);
     launch_check("join kernels");
-    return launches + (two_pass ? 4 : 3);
+    return launches + 3;
   }
   for (size_t r = 0; r < S->rb.size(); r++) {
     RuleBufs& b = S->rb[r];
@@ -622,8 +607,7 @@ uint32_t enqueue_batched(hbx_session* S, cudaStream_t st) {
   uint32_t launches = enqueue_join(S, st, S->d_groups.p);
   dev::EvalParams P = eval_params(S, S->d_groups.p);
   P.n_seg = 0;  // every work item of every group
-  int grid = S->ctx->n_sm * S->blocks_per_sm;
-  if (S->max_eval_ctas > 0) grid = std::min(grid, S->max_eval_ctas);
+  const int grid = S->ctx->n_sm * S->blocks_per_sm;
   HBX_CUDA(cudaEventRecordWithFlags(S->ev_eval0, st, rec_flags));
   dev::eval_kernel(S->variant, S->groups, S->peq_shape.w)<<<grid, kThreads, S->smem_bytes, st>>>(P);
   launch_check("k_eval");
@@ -724,8 +708,7 @@ dev::Counters run_once(hbx_session* S, hbx_mode mode, cudaStream_t st, uint32_t*
                            cudaMemcpyDeviceToHost, st));
   HBX_CUDA(cudaStreamSynchronize(st));
   dev::EvalParams P = eval_params(S, S->d_rules.p);
-  int max_grid = S->ctx->n_sm * S->blocks_per_sm;
-  if (S->max_eval_ctas > 0) max_grid = std::min(max_grid, S->max_eval_ctas);
+  const int max_grid = S->ctx->n_sm * S->blocks_per_sm;
   HBX_CUDA(cudaEventRecord(S->ev_eval0, st));
   for (uint64_t p = 0; p < S->E.n_partitions; p++) {
     for (uint32_t r = 0; r < n_rules; r++) {
@@ -1043,11 +1026,6 @@ void session_run(hbx_session* S, hbx_mode mode, cudaStream_t st) {
     grow_output(S, need);
   }
   fail(HBX_ERR_CAPACITY, "output kept growing");
-}
-
-void set_eval_ctas(hbx_session* S, int ctas) {
-  S->max_eval_ctas = std::max(0, ctas);
-  drop_graph(S);
 }
 
 void reserve_output(hbx_session* S, uint64_t pairs) {

@@ -15,11 +15,6 @@ void run_to_host(hbx_session* s, hbx_mode mode, std::vector<uint32_t>* l, std::v
 // slots before a run, so that a run expected to produce that many pairs
 // does not overflow and repeat.
 void reserve_output(hbx_session* s, uint64_t pairs);
-// Caps the evaluation launch of a session at `ctas` CTAs (0 = every slot the
-// device holds), so that other streams' kernels (another window's copies,
-// encoding and join) find room on the SMs while it runs.
-void set_eval_ctas(hbx_session* s, int ctas);
-
 struct Table;
 // sort.cu: sorts n device pairs by (left row, right row) in place.
 void sort_pairs_device(hbx_ctx* ctx, uint32_t* l, uint32_t* r, uint64_t n, uint32_t n_left,

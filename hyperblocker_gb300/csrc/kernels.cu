@@ -193,10 +193,9 @@ __global__ void k_items_final(const Rule* rules, uint32_t rule, uint32_t tile_ri
 }
 
 // ---- fused join for small key domains (every rule's left key domain at most
-// kFusedJoinMaxDomain): one launch for keys + histograms, one or two for
-// offsets + work items (chunk totals when a domain spans several chunks,
-// then each chunk's scan), one for the scatter, each covering every rule
-// and both tables.  The row kernels run one block row per (rule, table)
+// kFusedJoinMaxDomain): one launch for keys + histograms, one for offsets +
+// work items, one for the scatter, each covering every rule and both
+// tables.  The row kernels run one block row per (rule, table)
 // (blockIdx.y = rule, blockIdx.z = table), so the rules' and tables'
 // dependent load -> atomic -> store chains run side by side.
 
@@ -235,116 +234,68 @@ __global__ void k_join_count(Side L, Side R, const Rule* rules) {
 // The three independent scans of every rule -- row offsets per left key
 // (y = 0), row offsets per right key (y = 1), work items per left key with
 // the rule's pair-comparison count (y = 2) -- in chunks of kScanChunk keys,
-// one block of 1024 threads per (chunk, y, rule): k_join_scan_totals writes
-// every chunk's total, k_join_scan_final adds the totals of the earlier
-// chunks to the chunk's own exclusive scan.  When every domain spans at most
-// kJoinScanLoopChunks chunks the totals pass is left out: one block per
-// (y, rule) scans the chunks in turn, carrying the running total, and also
-// sums the pair-comparison count.
+// one block of 1024 threads per (chunk, y, rule), in one launch: a block
+// first sums the values of the keys before its chunk itself (at most
+// kFusedJoinMaxDomain / kScanChunk - 1 = 15 chunks, read from L2), then
+// scans its own chunk.
 __device__ __forceinline__ uint32_t join_scan_domain(const Rule& Q, uint32_t y) {
   return y == 1 ? Q.domain : Q.domain_l;
 }
 
-// The values of one chunk: 4 keys per thread (counts, or work items).
-__device__ __forceinline__ void join_scan_values(const Rule& Q, uint32_t y, uint32_t tile_right,
-                                                 uint32_t b, uint32_t D,
-                                                 unsigned long long (&v)[4],
-                                                 unsigned long long* pairs) {
-  const uint32_t* cnt = y == 1 ? Q.cnt_r : Q.cnt_l;
-  unsigned long long pr = 0;
-#pragma unroll
-  for (int k = 0; k < 4; k++) {
-    v[k] = 0;
-    if (b + k < D) {
-      if (y == 2) {
-        unsigned long long p = 0;
-        v[k] = key_items(Q, b + k, tile_right, &p);
-        pr += p;
-      } else {
-        v[k] = cnt[b + k];
-      }
-    }
+// The value of key k (< D): its row count, or its work items (y = 2, with
+// the key's pair comparisons added to *pairs).
+__device__ __forceinline__ unsigned long long join_scan_value(const Rule& Q, uint32_t y,
+                                                              uint32_t tile_right, uint32_t k,
+                                                              unsigned long long* pairs) {
+  if (y == 2) {
+    unsigned long long p = 0;
+    const unsigned long long v = key_items(Q, k, tile_right, &p);
+    *pairs += p;
+    return v;
   }
-  *pairs = pr;
+  return (y == 1 ? Q.cnt_r : Q.cnt_l)[k];
 }
 
-__global__ void k_join_scan_totals(const Rule* rules, uint32_t tile_right, uint32_t nb_max,
-                                   unsigned long long* totals, unsigned long long* comparisons) {
+__global__ void k_join_scan(const Rule* rules, uint32_t tile_right,
+                            unsigned long long* comparisons) {
   __shared__ unsigned long long s_w64[32];
   __shared__ unsigned long long s_t64;
   const uint32_t c = blockIdx.x, y = blockIdx.y, r = blockIdx.z;
   const Rule& Q = rules[r];
   const uint32_t D = join_scan_domain(Q, y);
   if ((unsigned long long)c * kScanChunk >= D) return;
+  // the keys before this chunk
+  unsigned long long before = 0, unused = 0;
+  for (uint32_t k = threadIdx.x; k < c * kScanChunk; k += blockDim.x)
+    before += join_scan_value(Q, y, tile_right, k, &unused);
+  block_excl_scan<unsigned long long>(before, s_w64, &s_t64);  // block sum in s_t64
+  const unsigned long long base_all = s_t64;
+  // this chunk: 4 keys per thread
+  const uint32_t b = c * kScanChunk + threadIdx.x * 4u;
   unsigned long long v[4], pairs = 0;
-  join_scan_values(Q, y, tile_right, c * kScanChunk + threadIdx.x * 4u, D, v, &pairs);
-  const unsigned long long sum = v[0] + v[1] + v[2] + v[3];
-  block_excl_scan<unsigned long long>(sum, s_w64, &s_t64);
-  if (threadIdx.x == 0) totals[((size_t)r * 3 + y) * nb_max + c] = s_t64;
+#pragma unroll
+  for (int k = 0; k < 4; k++) v[k] = b + k < D ? join_scan_value(Q, y, tile_right, b + k, &pairs) : 0ull;
+  unsigned long long ex =
+      block_excl_scan<unsigned long long>(v[0] + v[1] + v[2] + v[3], s_w64, &s_t64) + base_all;
+  const unsigned long long chunk_total = s_t64;
   if (y == 2) {
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      if (b + k < D) Q.item_off[b + k] = ex;
+      ex += v[k];
+    }
+    if ((unsigned long long)(c + 1) * kScanChunk >= D && threadIdx.x == 0)
+      Q.item_off[D] = base_all + chunk_total;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) pairs += __shfl_xor_sync(kFull, pairs, o);
     if ((threadIdx.x & 31) == 0 && pairs) atomicAdd(comparisons, pairs);
-  }
-}
-
-__global__ void k_join_scan_final(const Rule* rules, uint32_t tile_right, uint32_t nb_max,
-                                  const unsigned long long* totals,
-                                  unsigned long long* comparisons) {
-  __shared__ unsigned long long s_w64[32];
-  __shared__ unsigned long long s_t64;
-  __shared__ unsigned long long s_base;
-  const uint32_t y = blockIdx.y, r = blockIdx.z;
-  const Rule& Q = rules[r];
-  const uint32_t D = join_scan_domain(Q, y);
-  const bool loop = totals == nullptr;  // one block per (y, rule) takes every chunk in turn
-  uint32_t c = loop ? 0u : blockIdx.x;
-  if ((unsigned long long)c * kScanChunk >= D) return;
-  unsigned long long base = 0;
-  if (!loop) {
-    const unsigned long long* tot = totals + ((size_t)r * 3 + y) * nb_max;
-    if (threadIdx.x < 32) {  // totals of the earlier chunks (at most 16 for the fused join)
-      unsigned long long t = 0;
-      for (uint32_t k = threadIdx.x; k < c; k += 32) t += tot[k];
+  } else {
+    uint32_t* off = y == 1 ? Q.off_r : Q.off_l;
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(kFull, t, o);
-      if (threadIdx.x == 0) s_base = t;
+    for (int k = 0; k < 4; k++) {
+      if (b + k < D) off[b + k] = (uint32_t)ex;
+      ex += v[k];
     }
-    __syncthreads();
-    base = s_base;
-  }
-  unsigned long long pairs_sum = 0;
-  for (;; c++) {
-    const uint32_t b = c * kScanChunk + threadIdx.x * 4u;
-    unsigned long long v[4], pairs = 0;
-    join_scan_values(Q, y, tile_right, b, D, v, &pairs);
-    pairs_sum += pairs;
-    unsigned long long ex =
-        block_excl_scan<unsigned long long>(v[0] + v[1] + v[2] + v[3], s_w64, &s_t64) + base;
-    const unsigned long long chunk_total = s_t64;
-    const bool last = (unsigned long long)(c + 1) * kScanChunk >= D;
-    if (y == 2) {
-#pragma unroll
-      for (int k = 0; k < 4; k++) {
-        if (b + k < D) Q.item_off[b + k] = ex;
-        ex += v[k];
-      }
-      if (last && threadIdx.x == 0) Q.item_off[D] = base + chunk_total;
-    } else {
-      uint32_t* off = y == 1 ? Q.off_r : Q.off_l;
-#pragma unroll
-      for (int k = 0; k < 4; k++) {
-        if (b + k < D) off[b + k] = (uint32_t)ex;
-        ex += v[k];
-      }
-    }
-    base += chunk_total;
-    if (!loop || last) break;
-  }
-  if (y == 2 && comparisons) {  // no totals pass ran: the comparison count is summed here
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) pairs_sum += __shfl_xor_sync(kFull, pairs_sum, o);
-    if ((threadIdx.x & 31) == 0 && pairs_sum) atomicAdd(comparisons, pairs_sum);
   }
 }
 
@@ -847,6 +798,7 @@ __device__ __forceinline__ bool scan_begin(Scan<W>& z, const uint32_t* tab, cons
 // remaining symbol stays below its bound.  Returns 0 (not decided yet), 1
 // (the scan is complete: *m = the match count) or 2 (the pair cannot reach
 // the scan's threshold).
+constexpr int kScanQuadUnroll = 1;
 template <int W>
 __device__ __forceinline__ int scan_step(Scan<W>& z, uint32_t* m_out, WorkTally* ops) {
   constexpr int S = row_words(W);
@@ -855,13 +807,20 @@ __device__ __forceinline__ int scan_step(Scan<W>& z, uint32_t* m_out, WorkTally*
     z.cur = z.nxt;
     if (z.i + 16u < z.n_iter) z.nxt = __ldg(reinterpret_cast<const uint4*>(z.b + z.i + 16u));
   }
-  const uint32_t wds[4] = {z.cur.x, z.cur.y, z.cur.z, z.cur.w};
-#pragma unroll
-  for (int q = 0; q < 4; q++)
+  // four symbols per 32-bit word of the chunk, one word per loop turn: the
+  // smaller loop body runs faster than the fully unrolled chunk (C3, 300k
+  // rows: 98.5 ms of evaluation against 102.4 ms with two words per turn and
+  // 113 ms with four), which stalled on instruction fetch
+  uint4 c4 = z.cur;
+#pragma unroll(kScanQuadUnroll)
+  for (uint32_t q = 0; q < 4; q++) {
+    const uint32_t wd = c4.x;
 #pragma unroll
     for (int c = 0; c < 4; c++)
-      bp_step<W, S>(z.tab, (wds[q] >> (8 * c)) & 0xffu, z.win, z.mt,
+      bp_step<W, S>(z.tab, (wd >> (8 * c)) & 0xffu, z.win, z.mt,
                     (z.i + 4u * q + (uint32_t)c) < z.h ? 1u : 0u);
+    c4 = make_uint4(c4.y, c4.z, c4.w, 0u);
+  }
   z.i += 16;
   ops->steps += 4;
   uint32_t m = 0;

@@ -334,19 +334,12 @@ __global__ void k_reset(Counters* ctr, uint32_t* counts, uint64_t n_counts,
 // fused join (every rule's left key domain <= kFusedJoinMaxDomain); k_join_count
 // and k_join_scatter run on grid (blocks, rules, 2 tables); k_join_count
 // takes min(max domain, kSharedHistKeys) * 4 bytes of dynamic shared memory;
-// k_join_scan_final with totals == nullptr runs one block per (y, rule) over
-// every chunk and sums the comparisons itself (no totals pass; for domains
-// of at most kJoinScanLoopChunks chunks: one block walking 5 chunks took
-// longer than the two passes, so only single-chunk domains go that way)
+// k_join_scan runs 1024 threads per (chunk of kScanChunk keys, scan, rule):
+// grid (max domain / kScanChunk rounded up, 3, rules)
 constexpr uint32_t kFusedJoinMaxDomain = 1u << 16;
 constexpr uint32_t kSharedHistKeys = 8192;
-constexpr uint32_t kJoinScanLoopChunks = 1;
 __global__ void k_join_count(Side L, Side R, const Rule* rules);
-__global__ void k_join_scan_totals(const Rule* rules, uint32_t tile_right, uint32_t nb_max,
-                                   unsigned long long* totals, unsigned long long* comparisons);
-__global__ void k_join_scan_final(const Rule* rules, uint32_t tile_right, uint32_t nb_max,
-                                  const unsigned long long* totals,
-                                  unsigned long long* comparisons);
+__global__ void k_join_scan(const Rule* rules, uint32_t tile_right, unsigned long long* comparisons);
 __global__ void k_join_scatter(Side L, Side R, const Rule* rules, uint32_t n_rules,
                                unsigned long long* rule_base, unsigned long long* items_total);
 // ------------------------------------------------------------------ evaluation

@@ -191,15 +191,15 @@ extern "C" hbx_status hbx_block_streamed(hbx_ctx* ctx, const hbx_plan* plan, con
       if (w.p1 > w.p0) windows.push_back(w);
     }
 
-    // ---- two workers, each with its own context and stream
-    int eval_ctas = 0;
-    {
-      // 2 CTAs per SM is what the evaluation kernels fit (kernels.cuh)
-      eval_ctas = std::max(1, ctx->n_sm * 2 - std::max(2, ctx->n_sm / 4));
-    }
+    // ---- two workers, each with its own context and stream.  A window's
+    // copies and encoding run while the other worker's window is joined and
+    // evaluated; the runs themselves take turns (run_mu): two persistent
+    // evaluations side by side split the SMs unevenly (the one launched
+    // second starts on the slots the first leaves), and the whole call then
+    // waits for the starved one.
     std::atomic<size_t> next{0};
     std::vector<std::vector<uint32_t>> win_l(windows.size()), win_r(windows.size());
-    std::mutex mu;
+    std::mutex mu, run_mu;
     // matches per pair covered in the windows done so far: sizes the next
     // windows' output so that their runs do not overflow and repeat
     double density = -1.0;
@@ -210,10 +210,14 @@ extern "C" hbx_status hbx_block_streamed(hbx_ctx* ctx, const hbx_plan* plan, con
       hbx_opts o = ctx->opts;
       o.pred_order = 1;  // the plan is already in measured order
       // windows differ in size: one fixed tile shape and kernel instead of an
-      // autotuning search per window; 64 right rows per item with two staging
-      // buffers is the robust choice (C5's long strings: 2.2x faster than
-      // 128 rows with one buffer, C2: 7 % slower)
-      if (o.tile_right <= 0) o.tile_right = 64;
+      // autotuning search per window.  96 right rows per item (one staging
+      // buffer, 85 KB of shared memory per block) measured best: on the C5
+      // shape (500k x 500k, 64-256 character strings) 1.36 s of evaluation
+      // against 2.37 s with 64 rows (two buffers) and 2.44 s with 128 rows
+      // (one buffer), both of which take 103 KB per block and so leave less
+      // of each SM's L1 to the Peq rows the scans read; on C3 96 and 128
+      // rows are within 1 %
+      if (o.tile_right <= 0) o.tile_right = 96;
       if (o.eval_variant <= 0) o.eval_variant = 2;
       if (hbx_ctx_create(ctx->device, &o, &wc) != HBX_OK) {
         std::lock_guard<std::mutex> lock(mu);
@@ -267,11 +271,10 @@ extern "C" hbx_status hbx_block_streamed(hbx_ctx* ctx, const hbx_plan* plan, con
             const double want =
                 d >= 0 ? 1.5 * d * (double)pre.pairs_covered + 4096.0 : (double)pre.pairs_covered + 1.0;
             reserve_output(s, (uint64_t)std::min<double>(want, (double)cap));
-            // leave an eighth of the CTA slots to the other worker, so that
-            // its window's copies, encoding and join run beside this
-            // window's persistent evaluation instead of after it
-            if (windows.size() > 1) set_eval_ctas(s, eval_ctas);
-            run_to_host(s, mode, &l, &r);
+            {
+              std::lock_guard<std::mutex> turn(run_mu);
+              run_to_host(s, mode, &l, &r);
+            }
             hbx_session_stats(s, &ws);
           } catch (const Error& e) {
             st = e.status;
