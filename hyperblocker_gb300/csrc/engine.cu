@@ -74,6 +74,7 @@ struct hbx_session {
   hbx::DBuf<unsigned long long> seen;  // reported-pair set (plans with several rules)
   // key histograms and scatter cursors of every rule, one block: one memset
   hbx::DBuf<uint32_t> counts;
+  hbx::DBuf<unsigned long long> scan_sync;  // fused join: chunk totals and tickets (k_join_scan)
   bool fused_join = false;  // every key domain small: join kernels covering all rules
   hbx::DBuf<uint32_t> bound_idx;              // per rule, n_partitions + 1 key indices
   hbx::DBuf<unsigned long long> bound_val;    // item_off at those keys
@@ -211,6 +212,14 @@ uint64_t upload_host_encoding(hbx_session* S) {
 
 std::vector<dev::Rule> group_rules(const std::vector<dev::Rule>& singles);
 
+// Chunks of kScanChunk keys in the largest left key domain of the session's
+// rules (the fused join's scan grid).
+uint32_t fused_chunks(const hbx_session* S) {
+  uint32_t max_d = 1;
+  for (const dev::Rule& d : S->h_rules) max_d = std::max(max_d, d.domain_l);
+  return (max_d + dev::kScanChunk - 1) / dev::kScanChunk;
+}
+
 // Device state of a session whose side buffers hold the encoded tables.
 void setup_session(hbx_session* S, uint64_t h2d_tables) {
   hbx_ctx* C = S->ctx;
@@ -294,6 +303,7 @@ void setup_session(hbx_session* S, uint64_t h2d_tables) {
       pos += 2ull * d.domain_l + 2ull * d.domain;
       if (d.domain_l > dev::kFusedJoinMaxDomain) S->fused_join = false;
     }
+    if (S->fused_join) S->scan_sync.alloc(E.rules.size() * 3 * (fused_chunks(S) + 1));
   }
   S->h_groups = group_rules(S->h_rules);
   S->groups = false;
@@ -498,11 +508,13 @@ __global__ void k_gather_bounds(const dev::Rule* rules, uint32_t n_rules, uint32
 // Returns launches.
 uint32_t enqueue_join(hbx_session* S, cudaStream_t st, const dev::Rule* rules) {
   uint32_t launches = 1;  // k_reset
-  {  // counters, histograms and the duplicate set, one launch
+  const uint64_t n_sync = S->fused_join ? S->scan_sync.n : 0;
+  {  // counters, histograms, the duplicate set and the join scan's tickets, one launch
     const uint64_t n_seen = S->seen.p ? S->seen.n : 0;
-    const uint64_t n = std::max<uint64_t>(std::max<uint64_t>(S->counts.n, n_seen), 32);
+    const uint64_t n = std::max<uint64_t>(std::max<uint64_t>(S->counts.n, n_seen), std::max<uint64_t>(n_sync, 32));
     dev::k_reset<<<row_grid(n, S->ctx->n_sm), 256, 0, st>>>(S->d_ctr.p, S->counts.p, S->counts.n,
-                                                            S->seen.p, n_seen);
+                                                            S->seen.p, n_seen, S->scan_sync.p,
+                                                            n_sync);
   }
   const uint32_t nL = S->side_l.n_rows, nR = S->side_r.n_rows;
   const int n_sm = S->ctx->n_sm;
@@ -513,10 +525,11 @@ uint32_t enqueue_join(hbx_session* S, cudaStream_t st, const dev::Rule* rules) {
     const size_t smem = std::min<uint32_t>(max_d, dev::kSharedHistKeys) * sizeof(uint32_t);
     // rows per block row: each (rule, table) pair gets its own blocks
     const dim3 grid(row_grid(std::max(nL, nR), n_sm), n_rules, 2);
-    const uint32_t nb = (max_d + dev::kScanChunk - 1) / dev::kScanChunk;
+    const uint32_t nb = fused_chunks(S);
     unsigned long long* comparisons = &S->d_ctr.p->comparisons;
     dev::k_join_count<<<grid, 256, smem, st>>>(S->side_l, S->side_r, rules);
-    dev::k_join_scan<<<dim3(nb, 3, n_rules), 1024, 0, st>>>(rules, S->tile_right, comparisons);
+    dev::k_join_scan<<<dim3(nb, 3, n_rules), 1024, 0, st>>>(rules, S->tile_right, nb,
+                                                            S->scan_sync.p, comparisons, S->d_ctr.p);
     dev::k_join_scatter<<<grid, 256, 0, st>>>(S->side_l, S->side_r, rules, n_rules,
                                                S->d_rule_base.p, &S->d_ctr.p->items_total);
     launch_check("join kernels");

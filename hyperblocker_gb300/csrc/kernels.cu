@@ -234,10 +234,13 @@ __global__ void k_join_count(Side L, Side R, const Rule* rules) {
 // The three independent scans of every rule -- row offsets per left key
 // (y = 0), row offsets per right key (y = 1), work items per left key with
 // the rule's pair-comparison count (y = 2) -- in chunks of kScanChunk keys,
-// one block of 1024 threads per (chunk, y, rule), in one launch: a block
-// first sums the values of the keys before its chunk itself (at most
-// kFusedJoinMaxDomain / kScanChunk - 1 = 15 chunks, read from L2), then
-// scans its own chunk.
+// one block of 1024 threads per (chunk, y, rule), in one launch.  A block
+// takes its chunk from a ticket counter of its (y, rule) when it starts,
+// publishes the chunk's total (flag bit kScanFlag set) before it reads
+// anything of the other chunks, then adds the totals of the chunks before
+// its own: those blocks took their tickets earlier, so they are running or
+// done, and every wait ends (bounded all the same: a wait that gives up
+// counts a watchdog trip, which fails the run).
 __device__ __forceinline__ uint32_t join_scan_domain(const Rule& Q, uint32_t y) {
   return y == 1 ? Q.domain : Q.domain_l;
 }
@@ -256,28 +259,52 @@ __device__ __forceinline__ unsigned long long join_scan_value(const Rule& Q, uin
   return (y == 1 ? Q.cnt_r : Q.cnt_l)[k];
 }
 
-__global__ void k_join_scan(const Rule* rules, uint32_t tile_right,
-                            unsigned long long* comparisons) {
+constexpr unsigned long long kScanFlag = 1ull << 63;
+constexpr uint32_t kScanWaitPolls = 1u << 20;
+
+__global__ void k_join_scan(const Rule* rules, uint32_t tile_right, uint32_t nb,
+                            unsigned long long* sync, unsigned long long* comparisons,
+                            Counters* ctr) {
   __shared__ unsigned long long s_w64[32];
-  __shared__ unsigned long long s_t64;
-  const uint32_t c = blockIdx.x, y = blockIdx.y, r = blockIdx.z;
+  __shared__ unsigned long long s_t64, s_base;
+  __shared__ uint32_t s_chunk;
+  const uint32_t y = blockIdx.y, r = blockIdx.z;
+  // sync: per (rule, y) nb chunk totals, then one ticket counter each
+  unsigned long long* totals = sync + ((size_t)r * 3 + y) * nb;
+  unsigned long long* ticket = sync + (size_t)gridDim.z * 3 * nb + (size_t)r * 3 + y;
+  if (threadIdx.x == 0) s_chunk = (uint32_t)atomicAdd(ticket, 1ull);
+  __syncthreads();
+  const uint32_t c = s_chunk;
   const Rule& Q = rules[r];
   const uint32_t D = join_scan_domain(Q, y);
   if ((unsigned long long)c * kScanChunk >= D) return;
-  // the keys before this chunk
-  unsigned long long before = 0, unused = 0;
-  for (uint32_t k = threadIdx.x; k < c * kScanChunk; k += blockDim.x)
-    before += join_scan_value(Q, y, tile_right, k, &unused);
-  block_excl_scan<unsigned long long>(before, s_w64, &s_t64);  // block sum in s_t64
-  const unsigned long long base_all = s_t64;
-  // this chunk: 4 keys per thread
   const uint32_t b = c * kScanChunk + threadIdx.x * 4u;
   unsigned long long v[4], pairs = 0;
 #pragma unroll
   for (int k = 0; k < 4; k++) v[k] = b + k < D ? join_scan_value(Q, y, tile_right, b + k, &pairs) : 0ull;
-  unsigned long long ex =
-      block_excl_scan<unsigned long long>(v[0] + v[1] + v[2] + v[3], s_w64, &s_t64) + base_all;
+  unsigned long long ex = block_excl_scan<unsigned long long>(v[0] + v[1] + v[2] + v[3], s_w64, &s_t64);
   const unsigned long long chunk_total = s_t64;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicExch(totals + c, chunk_total | kScanFlag);
+  }
+  if (threadIdx.x < 32) {  // the chunks before this one: at most 15
+    unsigned long long t = 0;
+    for (uint32_t j = threadIdx.x; j < c; j += 32) {
+      unsigned long long f = 0;
+      uint32_t polls = 0;
+      while (!((f = atomicAdd(totals + j, 0ull)) & kScanFlag) && ++polls < kScanWaitPolls)
+        __nanosleep(64);
+      if (!(f & kScanFlag)) atomicAdd(&ctr->watchdog_trips, 1ull);
+      t += f & ~kScanFlag;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(kFull, t, o);
+    if (threadIdx.x == 0) s_base = t;
+  }
+  __syncthreads();
+  const unsigned long long base = s_base;
+  ex += base;
   if (y == 2) {
 #pragma unroll
     for (int k = 0; k < 4; k++) {
@@ -285,7 +312,7 @@ __global__ void k_join_scan(const Rule* rules, uint32_t tile_right,
       ex += v[k];
     }
     if ((unsigned long long)(c + 1) * kScanChunk >= D && threadIdx.x == 0)
-      Q.item_off[D] = base_all + chunk_total;
+      Q.item_off[D] = base + chunk_total;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) pairs += __shfl_xor_sync(kFull, pairs, o);
     if ((threadIdx.x & 31) == 0 && pairs) atomicAdd(comparisons, pairs);
@@ -317,16 +344,31 @@ __global__ void k_join_scatter(Side L, Side R, const Rule* rules, uint32_t n_rul
   const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x;
   const Rule& Q = rules[blockIdx.y];
   if (!Q.n_members) return;  // evaluated in another rule's group: counted, never enumerated
-  if (blockIdx.z == 0) {
-    for (uint32_t row = t0; row < L.n_rows; row += stride) {
-      const uint32_t k = Q.key_l[row];
-      Q.sorted_l[Q.off_l[k] + atomicAdd(Q.cur_l + k, 1u)] = row;
-    }
-  } else {
-    const StrMeta* meta_in = R.str_meta + (size_t)Q.sim_r[0] * R.n_rows;
-    for (uint32_t row = t0; row < R.n_rows; row += stride) {
-      const uint32_t k = Q.key_r[row];
-      const uint32_t pos = Q.off_r[k] + atomicAdd(Q.cur_r + k, 1u);
+  // a warp's rows with the same key take their slots with one atomic (few
+  // keys, e.g. a year, would otherwise serialise every row on a handful of
+  // counters); the loop runs while any lane of the warp has a row
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const bool left = blockIdx.z == 0;
+  const uint32_t n = left ? L.n_rows : R.n_rows;
+  const uint32_t* keys = left ? Q.key_l : Q.key_r;
+  uint32_t* cur = left ? Q.cur_l : Q.cur_r;
+  const uint32_t* off = left ? Q.off_l : Q.off_r;
+  const StrMeta* meta_in = R.str_meta + (size_t)Q.sim_r[0] * R.n_rows;
+  for (uint32_t w0 = t0 - (uint32_t)lane; w0 < n; w0 += stride) {
+    const uint32_t row = w0 + (uint32_t)lane;
+    const bool valid = row < n;
+    const uint32_t k = valid ? keys[row] : 0xffffffffu;
+    const unsigned peers = __match_any_sync(kFull, k);
+    const int leader = __ffs(peers) - 1;
+    uint32_t base = 0;
+    if (valid && lane == leader) base = atomicAdd(cur + k, (uint32_t)__popc(peers));
+    base = __shfl_sync(kFull, base, leader);
+    if (!valid) continue;
+    const uint32_t pos = off[k] + base + (uint32_t)__popc(peers & lt);
+    if (left) {
+      Q.sorted_l[pos] = row;
+    } else {
       Q.sorted_r[pos] = row;
       if (Q.sorted_meta_r) Q.sorted_meta_r[pos] = sorted_meta(R, Q, meta_in, row);
     }
@@ -347,13 +389,15 @@ __global__ void k_rule_base(const Rule* rules, uint32_t n_rules, unsigned long l
 }
 
 __global__ void k_reset(Counters* ctr, uint32_t* counts, uint64_t n_counts,
-                        unsigned long long* seen, uint64_t n_seen) {
+                        unsigned long long* seen, uint64_t n_seen, unsigned long long* zero64,
+                        uint64_t n_zero64) {
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   const uint64_t t0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   constexpr uint64_t kCtrWords = sizeof(Counters) / 8;
   for (uint64_t i = t0; i < kCtrWords; i += stride) reinterpret_cast<unsigned long long*>(ctr)[i] = 0;
   for (uint64_t i = t0; i < n_counts; i += stride) counts[i] = 0;
   for (uint64_t i = t0; i < n_seen; i += stride) seen[i] = ~0ull;
+  for (uint64_t i = t0; i < n_zero64; i += stride) zero64[i] = 0ull;
 }
 
 // =====================================================================
@@ -651,9 +695,10 @@ __device__ __forceinline__ bool first_report(const EvalParams& P, uint32_t lrow,
   return false;
 }
 
-// Emits final matches of one warp step with one atomic per warp.
-__device__ __forceinline__ void emit(const EvalParams& P, bool pass, uint32_t lrow, uint32_t rrow,
-                                     int lane) {
+// Writes up to one match per lane to the output with one atomic per warp
+// (after the duplicate set, when the launch has one).
+__device__ __forceinline__ void flush_pairs(const EvalParams& P, bool pass, uint32_t lrow,
+                                            uint32_t rrow, int lane) {
   if (P.seen) {
     const unsigned cm = __ballot_sync(kFull, pass);
     if (!cm) return;
@@ -1009,6 +1054,7 @@ struct ItemDesc {
   uint32_t lrow, rule, n, shift, kind;
   float thr0;
 };
+constexpr uint32_t kOutBuf = 64;  // matches a warp holds before writing them out
 struct WarpCtl {
   ItemDesc desc[kMaxClaimChunk];  // claimed items not yet staged
   uint32_t c_rule[kMaxStageBufs], c_lrow[kMaxStageBufs];  // claim per staging buffer
@@ -1020,8 +1066,49 @@ struct WarpCtl {
   uint32_t i_rule, i_lrow, i_kind, i_fast, i_all;
   float i_thr;
   int32_t i_lcode[kMaxEq];
+  // matches not yet written out (emit): fewer than 32 between calls
+  uint2 out_buf[kOutBuf];
+  uint32_t out_n;
 };
 static_assert(sizeof(WarpCtl) <= kWarpCtlWords * 4, "warp control block outgrows its words");
+
+// Collects the warp's final matches of one step; every 32 of them go out
+// together (flush_pairs), so the duplicate-set probes and the output
+// reservation pay their round trips once per 32 matches instead of once per
+// step with a match.
+__device__ __forceinline__ void emit(const EvalParams& P, WarpCtl* C, bool pass, uint32_t lrow,
+                                     uint32_t rrow, int lane) {
+  const unsigned pm = __ballot_sync(kFull, pass);
+  if (!pm) return;
+  const uint32_t n0 = C->out_n;
+  if (pass) C->out_buf[n0 + __popc(pm & ((1u << lane) - 1u))] = make_uint2(lrow, rrow);
+  const uint32_t n = n0 + __popc(pm);
+  __syncwarp();
+  if (n < 32) {
+    if (lane == 0) C->out_n = n;
+    __syncwarp();
+    return;
+  }
+  const uint2 e = C->out_buf[lane];
+  const bool more = (uint32_t)lane + 32u < n;
+  const uint2 t = more ? C->out_buf[32 + lane] : make_uint2(0u, 0u);
+  __syncwarp();
+  if (more) C->out_buf[lane] = t;
+  if (lane == 0) C->out_n = n - 32u;
+  __syncwarp();
+  flush_pairs(P, true, e.x, e.y, lane);
+}
+
+// Writes out the matches emit still holds (at the end of the warp's loop).
+__device__ __forceinline__ void emit_drain(const EvalParams& P, WarpCtl* C, int lane) {
+  const uint32_t n = C->out_n;
+  const bool have = (uint32_t)lane < n;
+  const uint2 e = have ? C->out_buf[lane] : make_uint2(0u, 0u);
+  __syncwarp();
+  if (lane == 0) C->out_n = 0;
+  __syncwarp();
+  flush_pairs(P, have, e.x, e.y, lane);
+}
 
 // Filter one batch of 32 right rows of the item against its group's first
 // similarity column: first the members whose extra equalities hold for the
@@ -1036,7 +1123,7 @@ static_assert(sizeof(WarpCtl) <= kWarpCtlWords * 4, "warp control block outgrows
 // G: the launch has rule groups; without, every rule is its own group of one
 // and its predicates take the plain path (one threshold per predicate).
 template <bool G>
-__device__ __forceinline__ uint32_t filter_batch(const EvalParams& P, const WarpCtl* C,
+__device__ __forceinline__ uint32_t filter_batch(const EvalParams& P, WarpCtl* C,
                                                  const StrMeta* lm, const uint32_t* rows,
                                                  const StrMeta* meta, uint32_t n, uint32_t e0,
                                                  uint4* q, uint32_t tail, WorkTally* ops) {
@@ -1126,7 +1213,7 @@ __device__ __forceinline__ uint32_t filter_batch(const EvalParams& P, const Warp
     en[1] = head;
     en[2] = make_uint4(lrow, la, a_off, C->i_rule);
   }
-  emit(P, done, lrow, rrow, lane);
+  emit(P, C, done, lrow, rrow, lane);
   return __popc(qm);
 }
 
@@ -1294,7 +1381,7 @@ __device__ __forceinline__ void claim_item(const EvalParams& P, WarpCtl* C, uint
       for (uint32_t e = 0; e < d.n; e += 32) {
         const uint32_t k = e + (uint32_t)lane;
         const uint32_t rrow = k < d.n ? d.rows_src[d.shift + k] : 0u;
-        emit(P, k < d.n, d.lrow, rrow, lane);
+        emit(P, C, k < d.n, d.lrow, rrow, lane);
       }
       (*done)++;
       continue;
@@ -1341,6 +1428,8 @@ __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
   WarpCtl* C = reinterpret_cast<WarpCtl*>(region + P.ctl_off);
   uint64_t* bar0 = reinterpret_cast<uint64_t*>(region + P.mbar_off);
   const long long t_start = clock64();
+  if (lane == 0) C->out_n = 0;
+  __syncwarp();
   // work positions per claim: every warp gets about eight claims, at most
   // kMaxClaimChunk items each
   const unsigned long long n_warps = (unsigned long long)gridDim.x * kWarpsPerCta;
@@ -1403,6 +1492,7 @@ __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
         mbar_wait(bar0 + cb, ((phs >> cb) & 1u) ^ 1u);
         for (uint32_t b = 0; b < P.n_bufs; b++)
           if (b != cb && C->c_n[b]) mbar_wait(bar0 + b, (phs >> b) & 1u);
+        emit_drain(P, C, lane);
         return;
       }
       active = true;
@@ -1522,9 +1612,10 @@ __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
         }
       }
     }
-    emit(P, fin && pass, lrow, rrow, lane);
+    emit(P, C, fin && pass, lrow, rrow, lane);
     if (!__any_sync(kFull, busy) && head == tail && !active && cur_n == 0) break;
   }
+  emit_drain(P, C, lane);
 }
 
 // The evaluation kernel body for masks of W words, instantiated below with

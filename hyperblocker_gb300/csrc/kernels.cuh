@@ -218,7 +218,7 @@ constexpr uint32_t kMaxStageBufs = 4;
 struct WarpLayout {
   uint32_t n_bufs, buf_off, buf_words, buf_rows_off, buf_lmeta_off, mbar_off, ctl_off, warp_words;
 };
-constexpr uint32_t kWarpCtlWords = 236;  // the warp's control block (kernels.cu: WarpCtl)
+constexpr uint32_t kWarpCtlWords = 360;  // the warp's control block (kernels.cu: WarpCtl)
 
 inline WarpLayout warp_layout(uint32_t tile_right, uint32_t n_bufs) {
   WarpLayout w;
@@ -330,16 +330,20 @@ __global__ void k_rule_base(const Rule* rules, uint32_t n_rules, unsigned long l
 // One launch for a run's resets: the counters and histograms to 0, the
 // duplicate set (n_seen slots, may be 0) to empty.
 __global__ void k_reset(Counters* ctr, uint32_t* counts, uint64_t n_counts,
-                        unsigned long long* seen, uint64_t n_seen);
+                        unsigned long long* seen, uint64_t n_seen, unsigned long long* zero64,
+                        uint64_t n_zero64);
 // fused join (every rule's left key domain <= kFusedJoinMaxDomain); k_join_count
 // and k_join_scatter run on grid (blocks, rules, 2 tables); k_join_count
 // takes min(max domain, kSharedHistKeys) * 4 bytes of dynamic shared memory;
 // k_join_scan runs 1024 threads per (chunk of kScanChunk keys, scan, rule):
-// grid (max domain / kScanChunk rounded up, 3, rules)
+// grid (nb = max domain / kScanChunk rounded up, 3, rules); sync holds
+// rules * 3 * (nb + 1) words, zero before the launch (k_reset)
 constexpr uint32_t kFusedJoinMaxDomain = 1u << 16;
 constexpr uint32_t kSharedHistKeys = 8192;
 __global__ void k_join_count(Side L, Side R, const Rule* rules);
-__global__ void k_join_scan(const Rule* rules, uint32_t tile_right, unsigned long long* comparisons);
+__global__ void k_join_scan(const Rule* rules, uint32_t tile_right, uint32_t nb,
+                            unsigned long long* sync, unsigned long long* comparisons,
+                            Counters* ctr);
 __global__ void k_join_scatter(Side L, Side R, const Rule* rules, uint32_t n_rules,
                                unsigned long long* rule_base, unsigned long long* items_total);
 // ------------------------------------------------------------------ evaluation

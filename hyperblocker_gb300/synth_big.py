@@ -419,3 +419,29 @@ def c4_requests(right: BlobTable, n_requests: int, rate: float = 200.0, min_rows
             cols = _append(cols, perturbed_copies(g, right, src, base + n - k))
         out.append(Request(float(t[i]), int(rules[i]), cols))
     return out
+
+
+def write_files(w: BigWorkload, out_dir: str) -> None:
+    """Writes a workload as the reference's CLI reads it: l.csv and r.csv
+    (every cell quoted, the header line first) and rules/<k>.yaml."""
+    import os
+
+    os.makedirs(os.path.join(out_dir, "rules"), exist_ok=True)
+    for name, t in (("l.csv", w.left), ("r.csv", w.right)):
+        with open(os.path.join(out_dir, name), "wb") as f:
+            for i in range(t.n_rows):  # the header line is row 0
+                f.write(b",".join(b'"' + bytes(b[o[i]:o[i + 1]]) + b'"' for b, o in t.cols) + b"\n")
+    for k, doc in enumerate(w.rules):
+        with open(os.path.join(out_dir, "rules", f"{k}.yaml"), "w") as f:
+            f.write(doc)
+
+
+if __name__ == "__main__":
+    # python -m hyperblocker_gb300.synth_big c3|c5 ROWS OUT_DIR: the workload at
+    # ROWS x ROWS as CSV files and a rule directory; prints its partition count
+    import sys
+
+    kind, n, out = sys.argv[1], int(sys.argv[2]), sys.argv[3]
+    wl = (c3 if kind == "c3" else c5)(n, n, max(1, n // 50))
+    write_files(wl, out)
+    print(wl.n_partitions)
