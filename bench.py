@@ -376,7 +376,7 @@ def bench_c2(args, ctx, dev):
         for mode in ("batched", "plain"):
             for _ in range(3):
                 sess.run_device(mode, out_l.data_ptr(), out_r.data_ptr(), cap, stream.cuda_stream)
-            ms, ms_eval = [], []
+            ms, ms_eval, ms_join = [], [], []
             torch.cuda.nvtx.range_push(f"c2_{mode}")  # names the timed launches for profilers
             with torch.cuda.stream(stream):
                 for _ in range(args.c2_steps):
@@ -390,11 +390,12 @@ def bench_c2(args, ctx, dev):
                     e1.synchronize()
                     ms.append(e0.elapsed_time(e1))
                     ms_eval.append(sess.stats().ms_eval)
+                    ms_join.append(sess.stats().ms_join)
             torch.cuda.nvtx.range_pop()
             st = sess.stats()
             res[mode] = {"value": st.pair_comparisons / (statistics.mean(ms) / 1000.0),
                          "ms_per_step": statistics.mean(ms), "ms_eval": statistics.mean(ms_eval),
-                         "launches_per_step": int(st.n_launches)}
+                         "ms_join": statistics.mean(ms_join), "launches_per_step": int(st.n_launches)}
         st = sess.stats()
         got = sorted_pairs(np.stack([out_l[:n].cpu().numpy().view(np.uint32),
                                      out_r[:n].cpu().numpy().view(np.uint32)], axis=1))

@@ -19,6 +19,7 @@
 #include <filesystem>
 #include <fstream>
 #include <functional>
+#include <utility>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -211,6 +212,26 @@ uint64_t upload_host_encoding(hbx_session* S) {
 }
 
 std::vector<dev::Rule> group_rules(const std::vector<dev::Rule>& singles);
+
+// Launches k with programmatic stream serialization: its blocks may start
+// while the kernel before it on the stream finishes (they wait in
+// dev::pdl_wait before reading its results), so a chain of short dependent
+// kernels does not pay a full launch gap per kernel.
+template <typename... KArgs, typename... Args>
+void launch_dependent(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                      Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  HBX_CUDA(cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...));
+}
 
 // Chunks of kScanChunk keys in the largest left key domain of the session's
 // rules (the fused join's scan grid).
@@ -527,11 +548,11 @@ uint32_t enqueue_join(hbx_session* S, cudaStream_t st, const dev::Rule* rules) {
     const dim3 grid(row_grid(std::max(nL, nR), n_sm), n_rules, 2);
     const uint32_t nb = fused_chunks(S);
     unsigned long long* comparisons = &S->d_ctr.p->comparisons;
-    dev::k_join_count<<<grid, 256, smem, st>>>(S->side_l, S->side_r, rules);
-    dev::k_join_scan<<<dim3(nb, 3, n_rules), 1024, 0, st>>>(rules, S->tile_right, nb,
-                                                            S->scan_sync.p, comparisons, S->d_ctr.p);
-    dev::k_join_scatter<<<grid, 256, 0, st>>>(S->side_l, S->side_r, rules, n_rules,
-                                               S->d_rule_base.p, &S->d_ctr.p->items_total);
+    launch_dependent(dev::k_join_count, grid, dim3(256), smem, st, S->side_l, S->side_r, rules);
+    launch_dependent(dev::k_join_scan, dim3(nb, 3, n_rules), dim3(1024), 0, st, rules,
+                     S->tile_right, nb, S->scan_sync.p, comparisons, S->d_ctr.p);
+    launch_dependent(dev::k_join_scatter, grid, dim3(256), 0, st, S->side_l, S->side_r, rules,
+                     n_rules, S->d_rule_base.p, &S->d_ctr.p->items_total);
     launch_check("join kernels");
     return launches + 3;
   }

@@ -192,6 +192,16 @@ __global__ void k_items_final(const Rule* rules, uint32_t rule, uint32_t tile_ri
   }
 }
 
+// Programmatic dependent launch: a kernel launched with the programmatic
+// stream serialization attribute (launch_dependent) may start while the
+// kernel before it still runs; it waits here before it reads anything that
+// kernel writes (every write of the earlier grid is visible after the wait).
+// Without the attribute both are no-ops.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// Lets the next kernel in the stream start its blocks (they wait in
+// pdl_wait); called once every block of this grid has started.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;"); }
+
 // ---- fused join for small key domains (every rule's left key domain at most
 // kFusedJoinMaxDomain): one launch for keys + histograms, one for offsets +
 // work items, one for the scatter, each covering every rule and both
@@ -203,6 +213,8 @@ __global__ void k_items_final(const Rule* rules, uint32_t rule, uint32_t tile_ri
 // domains up to kSharedHistKeys are kept per block in shared memory.
 __global__ void k_join_count(Side L, Side R, const Rule* rules) {
   extern __shared__ uint32_t s_cnt[];
+  pdl_trigger();
+  pdl_wait();  // the histograms are cleared (k_reset)
   const int side = blockIdx.z;
   const Side& S = side ? R : L;
   if ((unsigned long long)blockIdx.x * blockDim.x >= S.n_rows) return;  // whole block
@@ -268,6 +280,8 @@ __global__ void k_join_scan(const Rule* rules, uint32_t tile_right, uint32_t nb,
   __shared__ unsigned long long s_w64[32];
   __shared__ unsigned long long s_t64, s_base;
   __shared__ uint32_t s_chunk;
+  pdl_trigger();
+  pdl_wait();  // the histograms are complete (k_join_count)
   const uint32_t y = blockIdx.y, r = blockIdx.z;
   // sync: per (rule, y) nb chunk totals, then one ticket counter each
   unsigned long long* totals = sync + ((size_t)r * 3 + y) * nb;
@@ -330,6 +344,8 @@ __global__ void k_join_scan(const Rule* rules, uint32_t tile_right, uint32_t nb,
 // their first similarity column's metadata), and the rules' item bases.
 __global__ void k_join_scatter(Side L, Side R, const Rule* rules, uint32_t n_rules,
                                unsigned long long* rule_base, unsigned long long* items_total) {
+  pdl_trigger();
+  pdl_wait();  // offsets and work items are complete (k_join_scan)
   if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0) {
     unsigned long long acc = 0;
     for (uint32_t r = 0; r < n_rules; r++) {
@@ -344,31 +360,16 @@ __global__ void k_join_scatter(Side L, Side R, const Rule* rules, uint32_t n_rul
   const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x;
   const Rule& Q = rules[blockIdx.y];
   if (!Q.n_members) return;  // evaluated in another rule's group: counted, never enumerated
-  // a warp's rows with the same key take their slots with one atomic (few
-  // keys, e.g. a year, would otherwise serialise every row on a handful of
-  // counters); the loop runs while any lane of the warp has a row
-  const int lane = threadIdx.x & 31;
-  const unsigned lt = (1u << lane) - 1u;
-  const bool left = blockIdx.z == 0;
-  const uint32_t n = left ? L.n_rows : R.n_rows;
-  const uint32_t* keys = left ? Q.key_l : Q.key_r;
-  uint32_t* cur = left ? Q.cur_l : Q.cur_r;
-  const uint32_t* off = left ? Q.off_l : Q.off_r;
-  const StrMeta* meta_in = R.str_meta + (size_t)Q.sim_r[0] * R.n_rows;
-  for (uint32_t w0 = t0 - (uint32_t)lane; w0 < n; w0 += stride) {
-    const uint32_t row = w0 + (uint32_t)lane;
-    const bool valid = row < n;
-    const uint32_t k = valid ? keys[row] : 0xffffffffu;
-    const unsigned peers = __match_any_sync(kFull, k);
-    const int leader = __ffs(peers) - 1;
-    uint32_t base = 0;
-    if (valid && lane == leader) base = atomicAdd(cur + k, (uint32_t)__popc(peers));
-    base = __shfl_sync(kFull, base, leader);
-    if (!valid) continue;
-    const uint32_t pos = off[k] + base + (uint32_t)__popc(peers & lt);
-    if (left) {
-      Q.sorted_l[pos] = row;
-    } else {
+  if (blockIdx.z == 0) {
+    for (uint32_t row = t0; row < L.n_rows; row += stride) {
+      const uint32_t k = Q.key_l[row];
+      Q.sorted_l[Q.off_l[k] + atomicAdd(Q.cur_l + k, 1u)] = row;
+    }
+  } else {
+    const StrMeta* meta_in = R.str_meta + (size_t)Q.sim_r[0] * R.n_rows;
+    for (uint32_t row = t0; row < R.n_rows; row += stride) {
+      const uint32_t k = Q.key_r[row];
+      const uint32_t pos = Q.off_r[k] + atomicAdd(Q.cur_r + k, 1u);
       Q.sorted_r[pos] = row;
       if (Q.sorted_meta_r) Q.sorted_meta_r[pos] = sorted_meta(R, Q, meta_in, row);
     }
@@ -391,6 +392,8 @@ __global__ void k_rule_base(const Rule* rules, uint32_t n_rules, unsigned long l
 __global__ void k_reset(Counters* ctr, uint32_t* counts, uint64_t n_counts,
                         unsigned long long* seen, uint64_t n_seen, unsigned long long* zero64,
                         uint64_t n_zero64) {
+  pdl_trigger();
+  pdl_wait();  // the previous run has finished with what this clears
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   const uint64_t t0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   constexpr uint64_t kCtrWords = sizeof(Counters) / 8;
@@ -1625,6 +1628,7 @@ __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
 template <int W, bool G>
 __device__ __forceinline__ void eval_body(const EvalParams& P) {
   extern __shared__ __align__(16) uint32_t smem[];
+  pdl_wait();  // the join is complete (launched after it with launch_dependent)
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   uint32_t* region = smem + (size_t)warp * P.warp_words;
