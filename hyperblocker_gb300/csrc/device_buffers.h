@@ -56,17 +56,43 @@ struct PoolScope {
   PoolScope& operator=(const PoolScope&) = delete;
 };
 
+// A bump allocator over device memory the caller owns (hbx_block_static's
+// scratch array).  While an ArenaScope is active on the thread, every DBuf
+// takes its memory from it: 256-byte aligned pieces; freeing the most
+// recent piece gives its bytes back, the others stay taken until the arena
+// is dropped.  A piece that does not fit refuses the input
+// (HBX_ERR_INVALID_ARG) before anything is written to it.
+struct DevArena {
+  unsigned char* base = nullptr;
+  size_t cap = 0, used = 0, peak = 0;
+};
+
+inline DevArena*& current_arena() {
+  thread_local DevArena* a = nullptr;
+  return a;
+}
+
+struct ArenaScope {
+  DevArena* prev;
+  explicit ArenaScope(DevArena* a) : prev(current_arena()) { current_arena() = a; }
+  ~ArenaScope() { current_arena() = prev; }
+  ArenaScope(const ArenaScope&) = delete;
+  ArenaScope& operator=(const ArenaScope&) = delete;
+};
+
 template <class T>
 struct DBuf {
   T* p = nullptr;
   size_t n = 0;
   DevPool from{};  // pool and stream of the allocation (pool null: cudaMalloc)
+  DevArena* arena = nullptr;  // the arena the piece came from (then nothing is freed)
   DBuf() = default;
   DBuf(const DBuf&) = delete;
   DBuf& operator=(const DBuf&) = delete;
-  DBuf(DBuf&& o) noexcept : p(o.p), n(o.n), from(o.from) {
+  DBuf(DBuf&& o) noexcept : p(o.p), n(o.n), from(o.from), arena(o.arena) {
     o.p = nullptr;
     o.n = 0;
+    o.arena = nullptr;
   }
   DBuf& operator=(DBuf&& o) noexcept {
     if (this != &o) {
@@ -74,14 +100,20 @@ struct DBuf {
       p = o.p;
       n = o.n;
       from = o.from;
+      arena = o.arena;
       o.p = nullptr;
       o.n = 0;
+      o.arena = nullptr;
     }
     return *this;
   }
   ~DBuf() { reset(); }
   void reset() {
-    if (p) {
+    if (p && arena) {
+      unsigned char* end = reinterpret_cast<unsigned char*>(p) + n * sizeof(T);
+      if (end == arena->base + arena->used)
+        arena->used = (size_t)(reinterpret_cast<unsigned char*>(p) - arena->base);
+    } else if (p) {
       if (from.pool)
         cudaFreeAsync(p, from.stream);
       else
@@ -89,10 +121,24 @@ struct DBuf {
     }
     p = nullptr;
     n = 0;
+    arena = nullptr;
   }
   void alloc(size_t count) {
     reset();
     if (count == 0) count = 1;
+    if (DevArena* a = current_arena()) {
+      const size_t start = (a->used + 255) / 256 * 256;
+      if (start + count * sizeof(T) > a->cap)
+        fail(HBX_ERR_INVALID_ARG,
+             "input needs more device scratch for its encoding than the static scratch holds (" +
+                 std::to_string(a->cap) + " bytes)");
+      p = reinterpret_cast<T*>(a->base + start);
+      n = count;
+      arena = a;
+      a->used = start + count * sizeof(T);
+      a->peak = a->used > a->peak ? a->used : a->peak;
+      return;
+    }
     const DevPool* dp = current_pool();
     if (dp) {
       HBX_CUDA(cudaMallocFromPoolAsync((void**)&p, count * sizeof(T), dp->pool, dp->stream));

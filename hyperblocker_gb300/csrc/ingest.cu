@@ -435,7 +435,8 @@ void unpin_table(hbx_table* t) {
 }
 
 bool device_encode(const hbx_table* left, const hbx_table* right, Encoded* Ep, SideBufs* LB,
-                   SideBufs* RB, int n_sm, cudaStream_t st, uint64_t* h2d, std::string* why) {
+                   SideBufs* RB, int n_sm, cudaStream_t st, uint64_t* h2d, std::string* why,
+                   bool pin) {
   Encoded& E = *Ep;
   const Table& TL = left->t;
   const Table& TR = right->t;
@@ -445,8 +446,10 @@ bool device_encode(const hbx_table* left, const hbx_table* right, Encoded* Ep, S
     *why = "more than 2^30 rows in the two tables";
     return false;
   }
-  pin_table(left);
-  pin_table(right);
+  if (pin) {
+    pin_table(left);
+    pin_table(right);
+  }
   *h2d = 0;
 
   // ---- copy the columns the plan reads

@@ -67,7 +67,7 @@ int grid_for(uint64_t n, int n_sm, int per_sm = 8);
 // Fails with HBX_ERR_CUDA if the last launch failed.
 void check_launch(const char* what);
 // Exclusive scan of n >= 1 u32 values into out (the join's scan kernels);
-// its scratch comes from the current pool.
+// its scratch comes from the current pool (or arena).
 void scan_u32(const uint32_t* in, uint32_t n, uint32_t* out, cudaStream_t st);
 
 // Seed of the dictionaries' first hash; a rebuild after a collision uses
@@ -95,9 +95,11 @@ constexpr unsigned long long kDictSeed = 0xc70f6907ull;
 // dictionaries are then rebuilt with another seed.  Returns false, with the
 // reason in *why, only when the input is beyond the device path (2^30 rows
 // or more, or collisions under four seeds); the side buffers are then left
-// empty.
+// empty.  pin = false leaves the host tables pageable (no cudaHostRegister:
+// the entry point without device allocation copies from pageable memory).
 bool device_encode(const hbx_table* left, const hbx_table* right, Encoded* E, SideBufs* L,
-                   SideBufs* R, int n_sm, cudaStream_t st, uint64_t* h2d, std::string* why);
+                   SideBufs* R, int n_sm, cudaStream_t st, uint64_t* h2d, std::string* why,
+                   bool pin = true);
 
 // Partition bucket of every row of a table (data_mngr.h:150-202) computed on
 // the device from the partition and prefix columns only, in chunks of rows.

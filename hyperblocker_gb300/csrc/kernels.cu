@@ -1149,13 +1149,18 @@ __device__ __forceinline__ uint32_t filter_batch(const EvalParams& P, WarpCtl* C
     const uint32_t nx = R->n_xslots;
     if ((int32_t)loc.z == C->i_lcode[0]) eqm |= 1u;
     if (nx > 1 && (int32_t)loc.w == C->i_lcode[1]) eqm |= 2u;
-    for (uint32_t j = 2; j < nx; j++)
-      if (P.R.eq_codes[(size_t)R->xslot[j] * P.R.n_rows + rrow] == C->i_lcode[j]) eqm |= 1u << j;
-    for (uint32_t x = all; x; x &= x - 1) {
-      const uint32_t k = (uint32_t)__ffs(x) - 1u;
-      if (R->mem[k].xmask & ~eqm) live &= ~(1u << k);
+    if (nx <= 2u) {  // the group's table (Rule::x_live, x_thr)
+      live = R->x_live[eqm];
+      if (live != all) thr = R->x_thr[eqm];
+    } else {
+      for (uint32_t j = 2; j < nx; j++)
+        if (P.R.eq_codes[(size_t)R->xslot[j] * P.R.n_rows + rrow] == C->i_lcode[j]) eqm |= 1u << j;
+      for (uint32_t x = all; x; x &= x - 1) {
+        const uint32_t k = (uint32_t)__ffs(x) - 1u;
+        if (R->mem[k].xmask & ~eqm) live &= ~(1u << k);
+      }
+      if (live != all) thr = live_thr(R, live);
     }
-    if (live != all) thr = live_thr(R, live);
   }
   if (live) head = meta[e].head;
   uint32_t pass1 = 0;  // members that passed the first column without a scan

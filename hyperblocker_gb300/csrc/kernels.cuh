@@ -156,7 +156,30 @@ struct Rule {
   uint32_t xslot[kMaxEq];
   float thr_min;  // smallest member threshold on the first column
   Member mem[kMaxMembers];
+  // Groups with at most two extra slots: for each pattern of the extra slots
+  // that hold (bit j: xslot[j]), the members still live and the smallest of
+  // their first-column thresholds (fill_extras_table), so that the filter
+  // looks them up instead of walking the members for every pair.
+  uint32_t x_live[4];
+  float x_thr[4];
 };
+
+// Host: fills Rule::x_live / x_thr from the members, with the device's
+// live-threshold rule (the smallest threshold; NaN when any is NaN).
+inline void fill_extras_table(Rule* g) {
+  for (uint32_t eqm = 0; eqm < 4; eqm++) {
+    uint32_t live = 0;
+    float t = 3.0e38f;
+    for (uint32_t k = 0; k < g->n_members; k++) {
+      if (g->mem[k].xmask & ~eqm) continue;
+      live |= 1u << k;
+      const float u = g->mem[k].thr_first;
+      t = (u != u || t != t) ? __builtin_nanf("") : (u < t ? u : t);
+    }
+    g->x_live[eqm] = live;
+    g->x_thr[eqm] = t;
+  }
+}
 
 // Host: a rule as the only member of its own group (the plain form, serving,
 // and any rule no group takes in).
@@ -174,6 +197,7 @@ inline void make_singleton(Rule* d) {
     m.rest_thr[k - 1] = d->thr[k];
   }
   d->thr_min = m.thr_first;
+  fill_extras_table(d);
 }
 
 constexpr uint32_t kWordClasses = 5;

@@ -6,28 +6,33 @@
 // a process running under a fixed device-memory budget, or a latency-critical
 // loop that cannot afford cudaMalloc/cudaFree, which may synchronize the whole
 // device.  For them this entry point runs the same kernels as hbx_block (the
-// equality join, the Jaro-Winkler evaluation and the duplicate set), but every
-// buffer they need -- the encoded tables, the join's histograms, offsets and
-// sorted rows, the counters and the duplicate set -- is carved out of one
-// file-scope device array of kStaticScratchBytes (64 MiB).  The caller passes
+// device encoder of the tables, the equality join, the Jaro-Winkler
+// evaluation and the duplicate set), but every buffer they need -- the
+// columns the plan reads, the encoded tables and the encoder's temporaries,
+// the join's histograms, offsets and sorted rows, the counters and the
+// duplicate set -- is carved out of one file-scope device array of
+// kStaticScratchBytes (64 MiB).  The caller passes
 // the tables and the output buffers; nothing here calls cudaMalloc, cudaFree,
 // or any other allocating routine (no streams, events or graphs are created).
 //
 // Costs and limits, stated for the caller:
 //   * every GPU that loads libhbx.so holds the 64 MiB array until the process
 //     exits;
-//   * an input whose encoding, join state and duplicate set do not fit is
-//     refused with HBX_ERR_INVALID_ARG and a message with the bytes needed;
+//   * an input whose columns, encoding, join state and duplicate set do not
+//     fit is refused with HBX_ERR_INVALID_ARG (the encoding is refused while
+//     the encoder places it, the rest before any join work);
 //   * every call shares the one array and keeps the previous call's contents
 //     (whatever must start at zero is cleared by the call itself), so calls
 //     whose work overlaps on the GPU -- from several host threads, or on
 //     several streams without ordering between them -- race and corrupt each
 //     other;
 //   * the first call on a device looks up the array's device address (once
-//     per device and CUDA context, with that device current); make that
-//     first call before any stream capture begins.  A later call that finds
-//     another context current on the device (after cudaDeviceReset, say,
-//     which reloads the module and may move the array) looks it up again.
+//     per device and CUDA context, with that device current).  A later call
+//     that finds another context current on the device (after
+//     cudaDeviceReset, say, which reloads the module and may move the array)
+//     looks it up again;
+//   * a call cannot be captured into a CUDA graph: it copies from pageable
+//     host memory and synchronizes its stream.
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -38,8 +43,10 @@
 #include <string>
 #include <vector>
 
+#include "device_buffers.h"
 #include "encode.h"
 #include "hbx_core.h"
+#include "ingest.h"
 #include "kernels.cuh"
 
 namespace {
@@ -126,31 +133,6 @@ struct Carve {
   }
 };
 
-template <class T>
-std::vector<T> flat(const std::vector<std::vector<T>>& v) {
-  std::vector<T> out;
-  for (auto& x : v) out.insert(out.end(), x.begin(), x.end());
-  return out;
-}
-
-std::vector<hbx::dev::StrMeta> string_meta(const hbx::SideEnc& se, uint32_t n) {
-  std::vector<hbx::dev::StrMeta> meta;
-  meta.reserve(se.str_off.size() * (size_t)n);
-  for (size_t slot = 0; slot < se.str_off.size(); slot++)
-    for (uint32_t i = 0; i < n; i++) {
-      const uint32_t off = se.str_off[slot][i], len = se.str_len[slot][i];
-      uint32_t w[4] = {0, 0, 0, 0};
-      for (uint32_t k = 0; k < 16 && k < len; k++)
-        w[k / 4] |= (uint32_t)se.arena[(size_t)off * 16 + k] << (8 * (k % 4));
-      hbx::dev::StrMeta m;
-      m.loc = make_uint4(off, len, 0, 0);
-      m.head = make_uint4(w[0], w[1], w[2], w[3]);
-      hbx::dev::make_sig(se.arena.data() + (size_t)off * 16, len, m.sig);
-      meta.push_back(m);
-    }
-  return meta;
-}
-
 struct Layout {
   hbx::dev::Side L{}, R{};
   std::vector<hbx::dev::Rule> rules;
@@ -168,23 +150,12 @@ struct Layout {
   uint32_t tile_right = 128;
 };
 
-// Places every buffer; with c.base == nullptr it only measures.  The
-// duplicate set (plans with several rules) is placed last by place_seen.
-void place(Carve& c, const hbx::Encoded& E, size_t smem_cap, Layout* Y,
-           const std::vector<hbx::dev::StrMeta>& ml, const std::vector<hbx::dev::StrMeta>& mr) {
+// Places the join state, the Peq tables and the counters after the encoded
+// tables (c.used starts past them); with c.base == nullptr it only measures.
+// The duplicate set (plans with several rules) is placed last by place_seen.
+void place(Carve& c, const hbx::Encoded& E, size_t smem_cap, Layout* Y) {
   namespace dev = hbx::dev;
   const uint32_t nL = (uint32_t)E.L.n_rows, nR = (uint32_t)E.R.n_rows;
-  auto side = [&](const hbx::SideEnc& se, dev::Side& ds, uint32_t n,
-                  const std::vector<dev::StrMeta>& m) {
-    ds.bucket = c.take<uint32_t>(n);
-    ds.eq_codes = c.take<int32_t>(se.eq_codes.size() * (size_t)n);
-    ds.comp_codes = c.take<int32_t>(se.comp_codes.size() * (size_t)n);
-    ds.arena = c.take<uint8_t>(se.arena.size());
-    ds.str_meta = c.take<dev::StrMeta>(m.size());
-    ds.n_rows = n;
-  };
-  side(E.L, Y->L, nL, ml);
-  side(E.R, Y->R, nR, mr);
   uint32_t max_len = 1;
   Y->rules.assign(E.rules.size(), dev::Rule{});
   Y->nb.assign(E.rules.size(), 0);
@@ -274,17 +245,54 @@ void run_static(int device, const hbx_plan* plan, const hbx_table* left, const h
     hbx::fail(HBX_ERR_INVALID_ARG, "prefix_idx out of range");
   if (out->capacity && (!out->l_row || !out->r_row))
     hbx::fail(HBX_ERR_INVALID_ARG, "null output pointer");
-  const hbx::Encoded E = hbx::encode(plan->p, left->t, right->t, n_partitions, prefix_idx);
-  const uint32_t nL = (uint32_t)E.L.n_rows, nR = (uint32_t)E.R.n_rows;
-  const std::vector<hbx::dev::StrMeta> ml = string_meta(E.L, nL), mr = string_meta(E.R, nR);
-
   int n_sm = 0, smem_optin = 0;
   HBX_STATIC_CUDA(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, device));
   HBX_STATIC_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
   const size_t smem_cap = std::min<size_t>((size_t)smem_optin, 200 * 1024);
+
+  int prev = 0;
+  HBX_STATIC_CUDA(cudaGetDevice(&prev));
+  HBX_STATIC_CUDA(cudaSetDevice(device));
+  struct Restore {
+    int d;
+    ~Restore() { cudaSetDevice(d); }
+  } restore{prev};
+  unsigned char* const base = scratch_on(device);
+  // Once work is queued on the scratch, a failure waits for the stream before
+  // it returns, so the scratch is free again when the call returns.
+  struct DrainOnError {
+    cudaStream_t st;
+    bool armed = false;
+    ~DrainOnError() {
+      if (armed) cudaStreamSynchronize(st);
+    }
+  } drain{st};
+
+  // The tables are encoded on the device, into the front of the scratch: the
+  // device encoder's buffers come from an arena over it (the columns the plan
+  // reads, then the encoded sides; an input they do not fit is refused there)
+  hbx::Encoded E = hbx::encode_schema(plan->p, left->t, right->t, n_partitions, prefix_idx);
+  hbx::DevArena arena;
+  arena.base = base;
+  arena.cap = kStaticScratchBytes;
+  hbx::SideBufs SL, SR;
+  uint64_t h2d = 0;
+  {
+    hbx::ArenaScope in_scratch(&arena);
+    std::string why;
+    drain.armed = true;
+    if (!hbx::device_encode(left, right, &E, &SL, &SR, n_sm, st, &h2d, &why, /*pin=*/false))
+      hbx::fail(HBX_ERR_UNSUPPORTED, "the device encoder cannot take this input: " + why);
+  }
+  const uint32_t nL = (uint32_t)E.L.n_rows, nR = (uint32_t)E.R.n_rows;
   Layout Y;
+  Y.L = dev::Side{SL.bucket.p, SL.eq.p, SL.comp.p, SL.arena.p, SL.meta.p, nL};
+  Y.R = dev::Side{SR.bucket.p, SR.eq.p, SR.comp.p, SR.arena.p, SR.meta.p, nR};
+
+  // the join state, Peq tables and counters after the encoded tables
   Carve measure{nullptr};
-  place(measure, E, smem_cap, &Y, ml, mr);
+  measure.used = arena.used;
+  place(measure, E, smem_cap, &Y);
   if (measure.used > kStaticScratchBytes)
     hbx::fail(HBX_ERR_INVALID_ARG,
               "input needs " + std::to_string(measure.used) + " bytes of device scratch for its "
@@ -296,45 +304,15 @@ void run_static(int device, const hbx_plan* plan, const hbx_table* left, const h
     hbx::fail(HBX_ERR_INVALID_ARG,
               "input needs " + std::to_string(measure.used) + " bytes of device scratch; the "
               "static scratch holds " + std::to_string(kStaticScratchBytes));
-
-  int prev = 0;
-  HBX_STATIC_CUDA(cudaGetDevice(&prev));
-  HBX_STATIC_CUDA(cudaSetDevice(device));
-  struct Restore {
-    int d;
-    ~Restore() { cudaSetDevice(d); }
-  } restore{prev};
-  Carve carve{scratch_on(device)};
-  place(carve, E, smem_cap, &Y, ml, mr);
+  Carve carve{base};
+  carve.used = arena.used;
+  place(carve, E, smem_cap, &Y);
   place_seen(carve, &Y, seen_slots);
-  // Once work is queued on the scratch, a failure waits for the stream before
-  // it returns, so the scratch is free again when the call returns.
-  struct DrainOnError {
-    cudaStream_t st;
-    bool armed = false;
-    ~DrainOnError() {
-      if (armed) cudaStreamSynchronize(st);
-    }
-  } drain{st};
 
-  uint64_t h2d = 0;
   auto up = [&](void* dst, const void* src, size_t bytes) {
-    drain.armed = true;
     if (bytes) HBX_STATIC_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
     h2d += bytes;
   };
-  auto up_side = [&](const hbx::SideEnc& se, const dev::Side& ds,
-                     const std::vector<dev::StrMeta>& m) {
-    up((void*)ds.bucket, se.bucket.data(), se.bucket.size() * 4);
-    const std::vector<int32_t> eq = flat(se.eq_codes), comp = flat(se.comp_codes);
-    up((void*)ds.eq_codes, eq.data(), eq.size() * 4);
-    up((void*)ds.comp_codes, comp.data(), comp.size() * 4);
-    up((void*)ds.arena, se.arena.data(), se.arena.size());
-    up((void*)ds.str_meta, m.data(), m.size() * sizeof(dev::StrMeta));
-    HBX_STATIC_CUDA(cudaStreamSynchronize(st));  // host vectors of this scope end here
-  };
-  up_side(E.L, Y.L, ml);
-  up_side(E.R, Y.R, mr);
   up(Y.d_rules, Y.rules.data(), Y.rules.size() * sizeof(dev::Rule));
 
   // counters, histograms, cursors and the duplicate set start from zero/empty
@@ -432,6 +410,7 @@ void run_static(int device, const hbx_plan* plan, const hbx_table* left, const h
     stats->scan_warp_steps = c.scan_warp_steps;
     stats->rest_scans = c.rest_scans;
     stats->h2d_bytes = h2d;  // bytes copied to the device by this call
+    stats->ingest_on_device = 1;
     stats->n_windows = 1;
   }
   if (c.seen_overflow)

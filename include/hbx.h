@@ -307,9 +307,10 @@ const char* hbx_serve_last_error(const hbx_server* s);
  * runtime or pool, a process under a fixed device-memory budget, or a
  * latency-critical loop that cannot pay for cudaMalloc/cudaFree, which may
  * synchronize the device.  Same result as hbx_block, but every buffer the
- * kernels need comes from one static device array of 64 MiB inside
- * libhbx.so (held on every GPU that loads the library until exit); this call
- * allocates no device memory and creates no stream, event or graph.
+ * kernels need (the device encoder's included: the tables are encoded on the
+ * device, as hbx_block does) comes from one static device array of 64 MiB
+ * inside libhbx.so (held on every GPU that loads the library until exit);
+ * this call allocates no device memory and creates no stream, event or graph.
  *   - out holds DEVICE pointers owned by the caller; stream may be NULL;
  *   - inputs whose encoding, join state and duplicate set exceed the 64 MiB
  *     are refused with HBX_ERR_INVALID_ARG (hbx_static_last_error() gives the
@@ -317,8 +318,10 @@ const char* hbx_serve_last_error(const hbx_server* s);
  *   - all calls share the array: calls whose GPU work overlaps (other host
  *     threads, unordered streams) race; each call clears what must start at
  *     zero itself;
- *   - the first call on a device looks up the array's address on that
- *     device; make it before any stream capture begins.
+ *   - the call cannot be captured into a CUDA graph: it copies from pageable
+ *     host memory and synchronizes the stream; on a failure after its first
+ *     launch it still waits for its kernels, so the array is free when it
+ *     returns.
  * Returns when the pairs are in out (synchronous on the stream). */
 hbx_status hbx_block_static(int device, const hbx_plan* plan, const hbx_table* left,
                             const hbx_table* right, uint64_t n_partitions, int64_t prefix_idx,

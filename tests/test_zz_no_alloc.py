@@ -80,6 +80,7 @@ def test_static_scratch_matches_hbx_block_twice(case):
         assert st.pair_comparisons == st_want.pair_comparisons
         assert st.n_matches == len(want)
         assert 0 < st.h2d_bytes < 64 << 20  # bytes this call copied to the device
+        assert st.ingest_on_device == 1  # encoded by the device encoder, inside the scratch
     # the second call (the array's address already looked up) allocates no
     # device memory
     assert free[0] == free[1]
