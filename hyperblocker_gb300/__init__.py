@@ -461,7 +461,7 @@ class Session:
 
 def block(ctx: Context, plan: Plan, left: Table, right: Table, n_partitions: int = 1,
           prefix_idx: int = INT_MAX, mode="batched", capacity: Optional[int] = None,
-          stream_ptr: Optional[int] = None, out=None):
+          stream_ptr: Optional[int] = None, out=None, stack: bool = True):
     """Host tables -> (pairs (n, 2) uint32 of (left row, right row), stats).
 
     ``hbx_block`` writes nothing when the output buffer is too small (it
@@ -469,7 +469,9 @@ def block(ctx: Context, plan: Plan, left: Table, right: Table, n_partitions: int
     ``capacity`` the buffer is sized from the largest result seen on this
     context, with a quarter of headroom.  ``out`` = (left rows, right rows),
     two uint32 host arrays the caller keeps between calls, is used when it is
-    large enough (the returned pairs are then views of them).
+    large enough.  With ``stack=False`` the pairs come back as the two row
+    arrays the C ABI fills, (left rows, right rows), views of ``out`` when it
+    is given, without the copy into one (n, 2) array.
     """
     if capacity is None:
         capacity = getattr(ctx, "_capacity_hint", 1 << 16)
@@ -492,6 +494,8 @@ def block(ctx: Context, plan: Plan, left: Table, right: Table, n_partitions: int
         n = int(p.n_written)
         if n + n // 4 > getattr(ctx, "_capacity_hint", 1 << 16):
             ctx._capacity_hint = n + n // 4
+        if not stack:
+            return (ol[:n], orr[:n]), s
         return np.stack([ol[:n], orr[:n]], axis=1), s
 
 
