@@ -772,7 +772,10 @@ __device__ __forceinline__ const uint32_t* peq_table(const EvalParams& P, uint32
 // records per warp:
 //   {right row, right offset / 16, right length, tag}
 //   {first 16 symbols of the right string}
-//   {left row, left length, left offset / 16, rule}
+//   {left row, left length | rule << 16, left offset / 16, threshold bits}
+//   for a plain entry (its left string has a Peq table: length <= 256), the
+//   threshold its need was computed for; {left row, left length, left
+//   offset / 16, rule} for a kAdvance entry.
 // tag = need | p << 10 | s << 15 | kAdvance? | live << 19 | member << 27.
 // A plain entry waits for the scan of its group's first column: `live` holds
 // the members whose extra equalities hold, need the matches the smallest of
@@ -1219,7 +1222,8 @@ __device__ __forceinline__ uint32_t filter_batch(const EvalParams& P, WarpCtl* C
                               : (ring_tag(0, 0, 0, pass1, (uint32_t)__ffs(pass1) - 1u) | kAdvance);
     en[0] = make_uint4(rrow, loc.x, loc.y, tag);
     en[1] = head;
-    en[2] = make_uint4(lrow, la, a_off, C->i_rule);
+    en[2] = scan ? make_uint4(lrow, la | (C->i_rule << 16), a_off, __float_as_uint(thr))
+                 : make_uint4(lrow, la, a_off, C->i_rule);
   }
   emit(P, C, done, lrow, rrow, lane);
   return __popc(qm);
@@ -1533,11 +1537,11 @@ __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
       const uint4 e0 = en[0], e2 = en[2];
       rrow = e0.x;
       lrow = e2.x;
-      rule = e2.w;
       live = tag_live(e0.w);
       memo = kNoMemo;
       int st = 0;
       if (e0.w & kAdvance) {
+        rule = e2.w;
         first = false;
         mi = tag_member(e0.w);
         s = tag_s(e0.w);
@@ -1547,14 +1551,15 @@ __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
           st = advance_rule<W>(P, rule, &s, lrow, rrow, z, ops);
       } else {
         // the group's first column at the smallest live threshold (without
-        // groups: the rule's first predicate)
+        // groups: the rule's first predicate), as the filter computed it
+        rule = e2.y >> 16;
         first = true;
         s = 0;
         const Rule* R = P.rules + rule;
         const uint32_t p = (e0.w >> 10) & 31u;
         st = scan_begin<W>(z, peq_table(P, R->sim_l[0], lrow), P.L.arena + 16ull * e2.z,
-                           P.R.arena + 16ull * e0.y, en[1], e2.y, e0.z, p, (int)(e0.w & 1023u),
-                           G ? live_thr(R, live) : R->thr[0], ops)
+                           P.R.arena + 16ull * e0.y, en[1], e2.y & 0xffffu, e0.z, p,
+                           (int)(e0.w & 1023u), __uint_as_float(e2.w), ops)
                  ? 2
                  : 0;
       }
