@@ -1059,6 +1059,7 @@ struct ItemDesc {
   const StrMeta* lm_src;
   uint32_t lrow, rule, n, shift, kind;
   float thr0;
+  int32_t lcode[2];  // the left row's codes of the group's first two extra slots
 };
 constexpr uint32_t kOutBuf = 64;  // matches a warp holds before writing them out
 struct WarpCtl {
@@ -1067,6 +1068,7 @@ struct WarpCtl {
   uint32_t c_n[kMaxStageBufs], c_shift[kMaxStageBufs];    // (n = 0: none)
   uint32_t c_kind[kMaxStageBufs];
   float c_thr[kMaxStageBufs];
+  int32_t c_lcode[kMaxStageBufs][2];
   // the item being filtered; i_lcode: its left row's codes of the group's
   // extra equality slots
   uint32_t i_rule, i_lrow, i_kind, i_fast, i_all;
@@ -1346,7 +1348,10 @@ __device__ __forceinline__ uint32_t claim_chunk(const EvalParams& P, WarpCtl* C,
   ItemDesc d;
   const bool sim = R.n_sim != 0;
   d.kind = (sim ? kItemSim : 0u) | (R.n_xslots ? kItemExtras : 0u) |
-           (R.n_sim > 1 ? kItemMore : 0u) | (R.n_members << 8);
+           (R.n_sim > 1 ? kItemMore : 0u) | (R.n_members << 8) | (R.n_xslots << 12);
+  // loaded here, a claim ahead of the item's filtering
+  d.lcode[0] = R.n_xslots > 0 ? P.L.eq_codes[(size_t)R.xslot[0] * P.L.n_rows + lrow] : 0;
+  d.lcode[1] = R.n_xslots > 1 ? P.L.eq_codes[(size_t)R.xslot[1] * P.L.n_rows + lrow] : 0;
   d.meta_src = sim ? R.sorted_meta_r + rb0 : nullptr;
   d.rows_src = R.sorted_r + a0;
   d.lm_src = sim ? P.L.str_meta + (size_t)R.sim_l[0] * P.L.n_rows + lrow : nullptr;
@@ -1415,6 +1420,8 @@ __device__ __forceinline__ void claim_item(const EvalParams& P, WarpCtl* C, uint
     C->c_shift[b] = d.shift;
     C->c_kind[b] = d.kind;
     C->c_thr[b] = d.thr0;
+    C->c_lcode[b][0] = d.lcode[0];
+    C->c_lcode[b][1] = d.lcode[1];
     return;
   }
   C->c_n[b] = 0;
@@ -1522,9 +1529,13 @@ __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
       C->i_all = (1u << item_members(kind)) - 1u;
       C->i_fast = has_table(P, la) ? 1u : 0u;
       if (G && (kind & kItemExtras)) {  // the left row's codes of the extra equality slots
-        const Rule* R = P.rules + ir;
-        if ((uint32_t)lane < R->n_xslots)
+        const uint32_t nx = (kind >> 12) & 15u;
+        if (lane < 2) {
+          C->i_lcode[lane] = C->c_lcode[cb][lane];  // loaded with the claim
+        } else if ((uint32_t)lane < nx) {
+          const Rule* R = P.rules + ir;
           C->i_lcode[lane] = P.L.eq_codes[(size_t)R->xslot[lane] * P.L.n_rows + il];
+        }
       }
       __syncwarp();
     }

@@ -242,7 +242,7 @@ constexpr uint32_t kMaxStageBufs = 4;
 struct WarpLayout {
   uint32_t n_bufs, buf_off, buf_words, buf_rows_off, buf_lmeta_off, mbar_off, ctl_off, warp_words;
 };
-constexpr uint32_t kWarpCtlWords = 360;  // the warp's control block (kernels.cu: WarpCtl)
+constexpr uint32_t kWarpCtlWords = 400;  // the warp's control block (kernels.cu: WarpCtl)
 
 inline WarpLayout warp_layout(uint32_t tile_right, uint32_t n_bufs) {
   WarpLayout w;
