@@ -1094,7 +1094,9 @@ namespace {
 // Copies bytes from src to dst with up to one thread per host core for
 // large copies (the first touch of a caller's fresh pages and the copy
 // itself both scale with threads; one thread copied C3's 4.1 GB of pairs at
-// about 2.5 GB/s).
+// about 2.5 GB/s).  The device-to-host copy itself goes to page-locked
+// staging: straight into a caller's pageable arrays it ran at 5.5 GB/s on
+// GB300 (C3 end to end 1.37 s against 1.00 s this way).
 void parallel_copy(void* dst, const void* src, size_t bytes) {
   constexpr size_t kPerThread = 64ull << 20;
   const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
