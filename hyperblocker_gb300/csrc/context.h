@@ -18,6 +18,8 @@ struct hbx_ctx {
   std::string err;
   std::string device_name;  // keys the autotuner's cache
   void* h_ctr = nullptr;    // page-locked counters of the context's session runs
-  void* h_out = nullptr;    // page-locked staging of one-shot results (grown as needed)
-  size_t h_out_n = 0;
+  // page-locked staging of one-shot results: two chunks of kOutChunkBytes,
+  // each with the event of its device-to-host copy (allocated on first use)
+  void* h_out = nullptr;
+  cudaEvent_t h_out_ev[2] = {nullptr, nullptr};
 };

@@ -1094,9 +1094,7 @@ namespace {
 // Copies bytes from src to dst with up to one thread per host core for
 // large copies (the first touch of a caller's fresh pages and the copy
 // itself both scale with threads; one thread copied C3's 4.1 GB of pairs at
-// about 2.5 GB/s).  The device-to-host copy itself goes to page-locked
-// staging: straight into a caller's pageable arrays it ran at 5.5 GB/s on
-// GB300 (C3 end to end 1.37 s against 1.00 s this way).
+// about 2.5 GB/s).
 void parallel_copy(void* dst, const void* src, size_t bytes) {
   constexpr size_t kPerThread = 64ull << 20;
   const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
@@ -1114,6 +1112,48 @@ void parallel_copy(void* dst, const void* src, size_t bytes) {
     });
   std::memcpy(dst, src, std::min(bytes, part));
   for (auto& t : th) t.join();
+}
+
+// Device -> caller's host memory through the context's two page-locked
+// chunks: the copy of chunk i + 1 runs while the host threads move chunk i
+// into place.  (Straight into a caller's pageable arrays the copy ran at
+// 5.5 GB/s on GB300; through one staging buffer of the whole output it
+// slowed from 190 to about 30 GB/s once the host had read that buffer.)
+constexpr size_t kOutChunkBytes = 256ull << 20;
+void copy_out(hbx_ctx* ctx, cudaStream_t st, void* const* dst, const void* const* src,
+              const size_t* bytes, int n_arrays) {
+  if (!ctx->h_out) {
+    HBX_CUDA(cudaHostAlloc(&ctx->h_out, 2 * kOutChunkBytes, cudaHostAllocPortable));
+    for (cudaEvent_t& e : ctx->h_out_ev)
+      HBX_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
+  struct Piece {
+    char* dst;
+    const char* src;
+    size_t n;
+  };
+  std::vector<Piece> pieces;
+  for (int a = 0; a < n_arrays; a++)
+    for (size_t off = 0; off < bytes[a]; off += kOutChunkBytes)
+      pieces.push_back({static_cast<char*>(dst[a]) + off, static_cast<const char*>(src[a]) + off,
+                        std::min(kOutChunkBytes, bytes[a] - off)});
+  char* slot[2] = {static_cast<char*>(ctx->h_out), static_cast<char*>(ctx->h_out) + kOutChunkBytes};
+  auto issue = [&](size_t i) {
+    HBX_CUDA(cudaMemcpyAsync(slot[i & 1], pieces[i].src, pieces[i].n, cudaMemcpyDeviceToHost, st));
+    HBX_CUDA(cudaEventRecord(ctx->h_out_ev[i & 1], st));
+  };
+  try {
+    if (!pieces.empty()) issue(0);
+    for (size_t i = 0; i < pieces.size(); i++) {
+      // slot (i + 1) & 1 last held piece i - 1, already moved into place
+      if (i + 1 < pieces.size()) issue(i + 1);
+      HBX_CUDA(cudaEventSynchronize(ctx->h_out_ev[i & 1]));
+      parallel_copy(pieces[i].dst, slot[i & 1], pieces[i].n);
+    }
+  } catch (...) {
+    cudaStreamSynchronize(st);  // no copy into the chunks is left running
+    throw;
+  }
 }
 
 hbx_status guard(hbx_ctx* ctx, const std::function<void()>& f) {
@@ -1184,6 +1224,8 @@ hbx_status hbx_ctx_destroy(hbx_ctx* ctx) {
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   if (ctx->h_ctr) cudaFreeHost(ctx->h_ctr);
   if (ctx->h_out) cudaFreeHost(ctx->h_out);
+  for (cudaEvent_t e : ctx->h_out_ev)
+    if (e) cudaEventDestroy(e);
   delete ctx;
   return HBX_OK;
 }
@@ -1279,23 +1321,10 @@ hbx_status hbx_block(hbx_ctx* ctx, const hbx_plan* plan, const hbx_table* left,
     if (n > out->capacity) hbx::fail(HBX_ERR_CAPACITY, "output capacity below the match count");
     if (n) {
       if (!out->l_row || !out->r_row) hbx::fail(HBX_ERR_INVALID_ARG, "null output pointer");
-      // through the context's page-locked staging (copies at link speed)
-      const size_t bytes = n * 8;
-      if (ctx->h_out_n < bytes) {
-        if (ctx->h_out) cudaFreeHost(ctx->h_out);
-        ctx->h_out = nullptr;
-        ctx->h_out_n = 0;
-        size_t want = 1 << 20;
-        while (want < bytes) want *= 2;
-        HBX_CUDA(cudaHostAlloc(&ctx->h_out, want, cudaHostAllocPortable));
-        ctx->h_out_n = want;
-      }
-      uint32_t* hl = static_cast<uint32_t*>(ctx->h_out);
-      HBX_CUDA(cudaMemcpyAsync(hl, s->out_l.p, n * 4, cudaMemcpyDeviceToHost, st));
-      HBX_CUDA(cudaMemcpyAsync(hl + n, s->out_r.p, n * 4, cudaMemcpyDeviceToHost, st));
-      HBX_CUDA(cudaStreamSynchronize(st));
-      parallel_copy(out->l_row, hl, n * 4);
-      parallel_copy(out->r_row, hl + n, n * 4);
+      void* dst[2] = {out->l_row, out->r_row};
+      const void* src[2] = {s->out_l.p, s->out_r.p};
+      const size_t bytes[2] = {n * 4, n * 4};
+      copy_out(ctx, st, dst, src, bytes, 2);
     }
     out->n_written = n;
   });
