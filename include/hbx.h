@@ -186,7 +186,10 @@ hbx_status hbx_session_destroy(hbx_session* s);
  * out holds HOST pointers.  The tables are encoded on the context's stream;
  * the run and the copy of the pairs go to `stream` (a cudaStream_t, NULL =
  * the context's stream), the stream the reference's AsyncSubmit takes
- * (host_producer.h:109-112).  Returns when the pairs are in out. */
+ * (host_producer.h:109-112).  The pairs come back through 512 MiB of
+ * page-locked host memory the context allocates on its first call (two
+ * chunks, each copied into out while the next one transfers).  Returns when
+ * the pairs are in out. */
 hbx_status hbx_block(hbx_ctx* ctx, const hbx_plan* plan, const hbx_table* left,
                      const hbx_table* right, uint64_t n_partitions, int64_t prefix_idx,
                      hbx_mode mode, hbx_pairs* out, hbx_stats* stats, void* stream);
