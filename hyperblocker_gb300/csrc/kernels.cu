@@ -556,8 +556,10 @@ __device__ __forceinline__ int m_need_lo(uint32_t ls, uint32_t ll, uint32_t p, f
   // of mr stays below 1e-6, under 3e-4 matches for ls <= 256, far inside the
   // 0.05 margin below
   const float jn = __fdividef(thr - c, 1.0f - c);
-  const float inv = __fdividef(1.0f, (float)ls) + __fdividef(1.0f, (float)ll);
-  const float mr = __fdividef(3.0f * jn - 1.0f, inv);
+  // m = (3 jn - 1) / (1/ls + 1/ll) = (3 jn - 1) ls ll / (ls + ll): one
+  // quotient, each factor within an ulp or two, so the bound's error stays
+  // far inside the margin below as well
+  const float mr = __fdividef((3.0f * jn - 1.0f) * (float)ls * (float)ll, (float)ls + (float)ll);
   const float v = ceilf(mr - 0.05f);
   if (!(v > 0.0f)) return 0;
   return v > 1.0e6f ? 1000000 : (int)v;
@@ -772,10 +774,11 @@ __device__ __forceinline__ const uint32_t* peq_table(const EvalParams& P, uint32
 // records per warp:
 //   {right row, right offset / 16, right length, tag}
 //   {first 16 symbols of the right string}
-//   {left row, left length | rule << 16, left offset / 16, threshold bits}
-//   for a plain entry (its left string has a Peq table: length <= 256), the
-//   threshold its need was computed for; {left row, left length, left
-//   offset / 16, rule} for a kAdvance entry.
+//   {left row, left length | Peq slot << 9 | rule << 16, left offset / 16,
+//   threshold bits} for a plain entry (its left string has a Peq table:
+//   length <= 256; slot 127 = read it from the rule), with the threshold its
+//   need was computed for; {left row, left length, left offset / 16, rule}
+//   for a kAdvance entry.
 // tag = need | p << 10 | s << 15 | kAdvance? | live << 19 | member << 27.
 // A plain entry waits for the scan of its group's first column: `live` holds
 // the members whose extra equalities hold, need the matches the smallest of
@@ -1224,7 +1227,8 @@ __device__ __forceinline__ uint32_t filter_batch(const EvalParams& P, WarpCtl* C
                               : (ring_tag(0, 0, 0, pass1, (uint32_t)__ffs(pass1) - 1u) | kAdvance);
     en[0] = make_uint4(rrow, loc.x, loc.y, tag);
     en[1] = head;
-    en[2] = scan ? make_uint4(lrow, la | (C->i_rule << 16), a_off, __float_as_uint(thr))
+    en[2] = scan ? make_uint4(lrow, la | (min(R->sim_l[0], 127u) << 9) | (C->i_rule << 16), a_off,
+                              __float_as_uint(thr))
                  : make_uint4(lrow, la, a_off, C->i_rule);
   }
   emit(P, C, done, lrow, rrow, lane);
@@ -1566,10 +1570,11 @@ __device__ __forceinline__ void eval_loop(const EvalParams& P, uint32_t* region,
         rule = e2.y >> 16;
         first = true;
         s = 0;
-        const Rule* R = P.rules + rule;
+        uint32_t sl0 = (e2.y >> 9) & 127u;  // 127: the slot did not fit, read it from the rule
+        if (sl0 == 127u) sl0 = P.rules[rule].sim_l[0];
         const uint32_t p = (e0.w >> 10) & 31u;
-        st = scan_begin<W>(z, peq_table(P, R->sim_l[0], lrow), P.L.arena + 16ull * e2.z,
-                           P.R.arena + 16ull * e0.y, en[1], e2.y & 0xffffu, e0.z, p,
+        st = scan_begin<W>(z, peq_table(P, sl0, lrow), P.L.arena + 16ull * e2.z,
+                           P.R.arena + 16ull * e0.y, en[1], e2.y & 511u, e0.z, p,
                            (int)(e0.w & 1023u), __uint_as_float(e2.w), ops)
                  ? 2
                  : 0;
