@@ -146,6 +146,52 @@ def test_rule_groups_against_oracle(ctx, rule_set, seed):
         assert st.fma_ambiguous == 0
 
 
+def _rule8(eq_cols, sims):
+    """synth.rule_yaml over tables of 8 columns (id, s1, s2, k1, ..., k5)."""
+    return synth.rule_yaml(eq_cols, sims).replace("[0, 0, 1, 2, 3, 4]", "[0, 0, 1, 2, 3, 4, 5, 6, 7]") \
+        .replace("[1, 0, 1, 2, 3, 4]", "[1, 0, 1, 2, 3, 4, 5, 6, 7]")
+
+
+def _tables8(seed):
+    """random_tables plus three more equality columns k3, k4, k5 (2-3 values each)."""
+    cl, cr = _util.random_tables(seed, 90, 200, b"abcdefgh ", 60, n_eq_values=2)
+    rng = np.random.Generator(np.random.PCG64(seed + 7))
+
+    def more(t, n):
+        for name, k in ((b"k3", 2), (b"k4", 3), (b"k5", 2)):
+            t.append([name] + [str(int(x)).encode() for x in rng.integers(0, k, size=n)])
+        return t
+
+    return more(cl, 90), more(cr, 200)
+
+
+# groups whose members add extra equality slots: exactly two slots in all
+# (the members' live set is looked up per pattern of slots that hold), and
+# four (walked member by member)
+EXTRA_SLOT_SETS = [
+    [_rule8([3], [(1, 0.70)]), _rule8([3, 4], [(1, 0.62), (2, 0.5)]), _rule8([3, 5], [(1, 0.66)]),
+     _rule8([3, 4, 5], [(1, 0.6)])],
+    [_rule8([3], [(1, 0.70)]), _rule8([3, 4, 5], [(1, 0.62)]), _rule8([3, 6, 7], [(1, 0.66), (2, 0.55)]),
+     _rule8([3, 4, 5, 6, 7], [(1, 0.6)])],
+]
+
+
+@pytest.mark.parametrize("seed", range(3))
+@pytest.mark.parametrize("rule_set", range(len(EXTRA_SLOT_SETS)))
+def test_rule_groups_with_extra_slots_against_oracle(ctx, rule_set, seed):
+    """Group members with one to four extra equality slots: both forms give
+    the oracle's set and pair-comparison count."""
+    cl, cr = _tables8(900 + 10 * rule_set + seed)
+    docs = EXTRA_SLOT_SETS[rule_set]
+    n_part = 1 + seed
+    want = api.run_block(api.CTable(cl), api.CTable(cr), _oracle_plan(docs), n_part)
+    assert len(want.pairs) > 0
+    for mode in MODES:
+        got, st = _engine_pairs(ctx, docs, cl, cr, n_part, _util.INT_MAX, mode)
+        assert np.array_equal(got, want.pairs), mode
+        assert st.pair_comparisons == want.pair_comparisons, mode
+
+
 def test_planner_puts_the_selective_predicate_first(built):
     """The reference evaluates a rule's similarity predicates in YAML order
     (execution_plan_generator.h:111-137; its Prioritizer, :223, is declared
