@@ -23,6 +23,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import math
 import re
 from dataclasses import dataclass, field
 from typing import Dict, List, Optional, Tuple
@@ -140,12 +141,30 @@ def _stoi(s: str) -> int:
 
 
 def _stof(s: str) -> float:
-    m = re.match(r"^\s*([+-]?(\d+\.?\d*([eE][+-]?\d+)?|\.\d+([eE][+-]?\d+)?))", s)
-    if not m:
-        raise RuleError(f"stof: invalid argument {s!r}")
+    """std::stof: strtof's longest valid prefix -- decimal, hexadecimal
+    (0x...p...), inf/infinity or nan/nan(...), case-insensitive, after
+    leading white space -- rounded to float."""
     import numpy as np
 
-    return float(np.float32(m.group(1)))
+    m = re.match(r"^\s*([+-]?)(0[xX](?:[0-9a-fA-F]+\.?[0-9a-fA-F]*|\.[0-9a-fA-F]+)(?:[pP][+-]?\d+)?"
+                 r"|(?i:infinity|inf|nan(?:\([0-9A-Za-z_]*\))?)"
+                 r"|\d+\.?\d*(?:[eE][+-]?\d+)?|\.\d+(?:[eE][+-]?\d+)?)", s)
+    if not m:
+        raise RuleError(f"stof: invalid argument {s!r}")
+    sign, body = m.group(1), m.group(2)
+    numeric = body[0].isdigit() or body[0] == "."
+    if body[:2] in ("0x", "0X"):
+        v = float.fromhex(body if "p" in body.lower() else body + "p0")
+    elif numeric:
+        v = float(body)
+    else:
+        v = float(body.split("(")[0])
+    v = -v if sign == "-" else v
+    if numeric:  # strtof sets ERANGE (std::stof throws) when a number over- or underflows
+        f = abs(float(np.float32(v))) if np.isfinite(v) else math.inf
+        if math.isinf(f) or (v != 0.0 and f < float(np.finfo(np.float32).tiny)):
+            raise RuleError(f"stof: out of range {s!r}")
+    return float(np.float32(v))
 
 
 def _strlist(node) -> List[str]:

@@ -192,6 +192,22 @@ def test_rule_groups_with_extra_slots_against_oracle(ctx, rule_set, seed):
         assert st.pair_comparisons == want.pair_comparisons, mode
 
 
+@pytest.mark.parametrize("thr", ["nan", "inf", "-inf", "0x1.8p-1"])
+def test_thresholds_stof_reads_besides_decimals(ctx, thr):
+    """A threshold of nan never fails a pair (JW < nan is false in the
+    reference, global_func.cuh:144), inf always does, -inf never; hexadecimal
+    floats are numbers.  Alone and in a rule group, both forms agree with the
+    oracle."""
+    cl, cr = _util.random_tables(77, 60, 120, b"abcdef ", 40, n_eq_values=2)
+    odd = synth.rule_yaml([3, 4], [(1, 0.5), (2, 0.6)]).replace("0.5, 0.6", f"{thr}, 0.6")
+    for docs in ([odd], [synth.rule_yaml([3], [(1, 0.7)]), odd]):
+        want = api.run_block(api.CTable(cl), api.CTable(cr), _oracle_plan(docs), 2)
+        for mode in MODES:
+            got, st = _engine_pairs(ctx, docs, cl, cr, 2, _util.INT_MAX, mode)
+            assert np.array_equal(got, want.pairs), (thr, len(docs), mode)
+            assert st.pair_comparisons == want.pair_comparisons
+
+
 def test_planner_puts_the_selective_predicate_first(built):
     """The reference evaluates a rule's similarity predicates in YAML order
     (execution_plan_generator.h:111-137; its Prioritizer, :223, is declared

@@ -79,6 +79,9 @@ def _oracle_plan(docs):
     [synth.rule_yaml([3] * (k % 3), [(1, 0.5 + 0.01 * k)]) for k in range(20)],
     # two similarities on the same left column: the first threshold wins
     [README_RULE.replace("[0, 1, 1, 1, 2, 2]", "[0, 1, 1, 1, 1, 2]")],
+    # thresholds std::stof reads besides decimals: nan, infinities, hexadecimal
+    [README_RULE.replace("[0, 1, 0.89, 0.85]", "[0, 1, nan, -inf]"),
+     README_RULE.replace("[0, 1, 0.89, 0.85]", "[0, 1, inf, 0x1.8p-1]")],
 ])
 def test_plan_matches_reference_serialization(built, docs):
     want = _oracle_plan(docs)
@@ -86,7 +89,7 @@ def test_plan_matches_reference_serialization(built, docs):
     pi, pt, th = p.serialized()
     assert pi == want.pred_index
     assert pt == want.pred_type
-    assert np.array_equal(np.float32(th), np.float32(want.pred_threshold))
+    assert np.array_equal(np.float32(th), np.float32(want.pred_threshold), equal_nan=True)
     assert p.n_rules == len(docs)
 
 
