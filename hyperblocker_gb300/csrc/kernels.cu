@@ -392,8 +392,9 @@ __global__ void k_rule_base(const Rule* rules, uint32_t n_rules, unsigned long l
 __global__ void k_reset(Counters* ctr, uint32_t* counts, uint64_t n_counts,
                         unsigned long long* seen, uint64_t n_seen, unsigned long long* zero64,
                         uint64_t n_zero64) {
+  // launched in stream order (after the previous run); lets the join's first
+  // kernel start its blocks early
   pdl_trigger();
-  pdl_wait();  // the previous run has finished with what this clears
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   const uint64_t t0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   constexpr uint64_t kCtrWords = sizeof(Counters) / 8;
