@@ -161,7 +161,8 @@ def _stof(s: str) -> float:
         v = float(body.split("(")[0])
     v = -v if sign == "-" else v
     if numeric:  # strtof sets ERANGE (std::stof throws) when a number over- or underflows
-        f = abs(float(np.float32(v))) if np.isfinite(v) else math.inf
+        with np.errstate(over="ignore"):  # the float32 overflow is the check
+            f = abs(float(np.float32(v))) if np.isfinite(v) else math.inf
         if math.isinf(f) or (v != 0.0 and f < float(np.finfo(np.float32).tiny)):
             raise RuleError(f"stof: out of range {s!r}")
     return float(np.float32(v))

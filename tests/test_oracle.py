@@ -224,3 +224,50 @@ def test_blob_tables_equal_cell_tables():
     b = api.run_block(api.CTable(blobs(cl)), api.CTable(blobs(cr)), plan, 3)
     assert np.array_equal(a.pairs, b.pairs)
     assert (a.pair_comparisons, a.pairs_covered) == (b.pair_comparisons, b.pairs_covered)
+
+
+def test_stof_restatement_matches_libc_strtof():
+    """The reference reads thresholds with std::stof (yaml_config.h:45),
+    which is strtof plus an exception when nothing converts or the value is
+    out of range (ERANGE).  The oracle's restatement (oracle/rules.py _stof)
+    agrees with this host's strtof on every form."""
+    import ctypes
+    import ctypes.util
+    import math
+
+    import numpy as np
+
+    from oracle.rules import RuleError, _stof
+
+    libc = ctypes.CDLL(ctypes.util.find_library("c"), use_errno=True)
+    libc.strtof.restype = ctypes.c_float
+    libc.strtof.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_char_p)]
+
+    def stof(s):
+        b = s.encode()
+        end = ctypes.c_char_p()
+        ctypes.set_errno(0)
+        v = libc.strtof(b, ctypes.byref(end))
+        consumed = ctypes.cast(end, ctypes.c_void_p).value - ctypes.cast(ctypes.c_char_p(b), ctypes.c_void_p).value
+        if consumed == 0 or ctypes.get_errno() == 34:  # no conversion, or ERANGE
+            return None
+        return float(np.float32(v))
+
+    cases = ["0.85", "0.5", " 0.7", "\t.25", "+0.9", "-0.3", "1", "1.", "1e-1", "2.5E+0", "7e-1x",
+             "0.95abc", "nan", "NaN", "-nan", "nan(123)", "inf", "-INF", "Infinity", "infinityx",
+             "0x1.8p-1", "0X10", "0x.8", "0x1p+2", "3.4e38", "3.5e38", "1e400", "1e-50", "1e-38",
+             "1.2e-38", "0", "0.0", "-0", "abc", "", " ", "e5", ".", "+", "0x"]
+    rng = np.random.Generator(np.random.PCG64(11))
+    cases += [f"{x:.{int(rng.integers(1, 9))}g}" for x in rng.random(300)]
+    for s in cases:
+        want = stof(s)
+        try:
+            got = _stof(s)
+        except RuleError:
+            got = None
+        if want is None or got is None:
+            assert want is None and got is None, (s, want, got)
+        elif math.isnan(want):
+            assert math.isnan(got), s
+        else:
+            assert got == want, (s, want, got)
