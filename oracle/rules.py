@@ -134,10 +134,15 @@ def parse_yaml(src: str):
 
 # ----------------------------------------------------------------- decoding
 def _stoi(s: str) -> int:
+    """std::stoi: strtol base 10 after leading white space; out of int range
+    throws."""
     m = re.match(r"^\s*([+-]?\d+)", s)
     if not m:
         raise RuleError(f"stoi: invalid argument {s!r}")
-    return int(m.group(1))
+    v = int(m.group(1))
+    if not -2**31 <= v <= 2**31 - 1:
+        raise RuleError(f"stoi: out of range {s!r}")
+    return v
 
 
 def _stof(s: str) -> float:

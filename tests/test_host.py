@@ -200,3 +200,19 @@ def test_column_ingest_refuses_bad_offsets(built):
     with pytest.raises(ValueError):
         hb.Table.from_columns([[b"a", b"b"], [b"c"]])
 
+
+
+@pytest.mark.parametrize("col,status", [("2147483648", hb.ERR_PARSE), ("99999999999", hb.ERR_PARSE),
+                                        ("-2147483649", hb.ERR_PARSE)])
+def test_out_of_range_column_index_is_refused_like_stoi(built, col, status):
+    """std::stoi throws out_of_range beyond int (yaml_config.h reads column
+    indices with it): the engine refuses the rule, and the oracle's
+    restatement raises."""
+    from oracle import rules
+
+    doc = README_RULE.replace("[0, 1, 4, 4]", f"[0, 1, {col}, 4]")
+    with pytest.raises(hb.HbxError) as e:
+        hb.Plan.from_yaml([doc])
+    assert e.value.status == status
+    with pytest.raises(rules.RuleError):
+        rules.decode_rule(rules.parse_yaml(doc))
