@@ -1104,13 +1104,19 @@ void parallel_copy(void* dst, const void* src, size_t bytes) {
     return;
   }
   const size_t part = (bytes / n + 4095) / 4096 * 4096;
+  auto copy_part = [=](size_t k) {
+    const size_t a = k * part, z = std::min(bytes, a + part);
+    if (a < z) std::memcpy(static_cast<char*>(dst) + a, static_cast<const char*>(src) + a, z - a);
+  };
   std::vector<std::thread> th;
-  for (size_t k = 1; k < n && k * part < bytes; k++)
-    th.emplace_back([=] {
-      const size_t a = k * part, z = std::min(bytes, a + part);
-      std::memcpy(static_cast<char*>(dst) + a, static_cast<const char*>(src) + a, z - a);
-    });
-  std::memcpy(dst, src, std::min(bytes, part));
+  size_t k = 1;
+  try {
+    for (; k < n && k * part < bytes; k++) th.emplace_back(copy_part, k);
+  } catch (...) {
+    // no thread for part k and later: this thread copies them
+  }
+  copy_part(0);
+  for (size_t j = k; j < n; j++) copy_part(j);
   for (auto& t : th) t.join();
 }
 

@@ -777,9 +777,9 @@ __device__ __forceinline__ const uint32_t* peq_table(const EvalParams& P, uint32
 //   {first 16 symbols of the right string}
 //   {left row, left length | Peq slot << 9 | rule << 16, left offset / 16,
 //   threshold bits} for a plain entry (its left string has a Peq table:
-//   length <= 256; slot 127 = read it from the rule), with the threshold its
-//   need was computed for; {left row, left length, left offset / 16, rule}
-//   for a kAdvance entry.
+//   length <= 256; slot 127 = read it from the rule; plans hold at most 64
+//   rules), with the threshold its need was computed for; {left row, left
+//   length, left offset / 16, rule} for a kAdvance entry.
 // tag = need | p << 10 | s << 15 | kAdvance? | live << 19 | member << 27.
 // A plain entry waits for the scan of its group's first column: `live` holds
 // the members whose extra equalities hold, need the matches the smallest of
